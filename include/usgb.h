@@ -1,0 +1,159 @@
+/*
+ * libusgb: GB300-native (sm_103a) STA/TFM delay-and-sum imaging, C ABI.
+ *
+ * Drop-in replacement for the signal-preparation and delay-and-sum stages
+ * that sit behind the reference's processor plugin interface
+ * ArrayProcessor<TPoint>::prepare/process
+ * (src/user/processor/ArrayProcessor.h:28-40), i.e. for
+ *   VectorialSTAProcessor<float, XYZValueFactor<float>>   src/user/processor/VectorialSTAProcessor.h:58-341
+ *   VectorialSTACUDAProcessor                             src/user/processor/VectorialSTACUDAProcessor.h:63-127
+ *   Vectorial3DSTAProcessor<float>                        src/user/processor/Vectorial3DSTAProcessor.h:51-253
+ *   DefaultSTAProcessor<float, XYZValueFactor<float>>     src/user/processor/DefaultSTAProcessor.h:50-227
+ *
+ * Plain C types only. Every function returns a usgb_status; the message of
+ * the last failure is available from usgb_last_error(). No exceptions cross
+ * this boundary. A context is not thread-safe; use one per thread/stream
+ * (the reference's processors are likewise not re-entrant).
+ */
+#ifndef USGB_H
+#define USGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The first three map to the reference's exception types
+ * (src/util/Exception.h): InvalidParameterException, InvalidValueException,
+ * InvalidStateException; USGB_ERR_CUDA to CUDAException (src/util/CUDAUtil.h:13-16). */
+typedef enum usgb_status {
+	USGB_OK = 0,
+	USGB_ERR_INVALID_PARAMETER = 1,
+	USGB_ERR_INVALID_VALUE = 2,
+	USGB_ERR_INVALID_STATE = 3,
+	USGB_ERR_CUDA = 4,
+	USGB_ERR_UNSUPPORTED = 5,
+	USGB_ERR_OUT_OF_MEMORY = 6,
+	USGB_ERR_DEVICE_TIMEOUT = 7
+} usgb_status;
+
+/* Which reference processor's arithmetic to follow. */
+typedef enum usgb_signal_path {
+	/* VectorialSTAProcessor / Vectorial3DSTAProcessor: Kaiser-sinc upsampling
+	 * by `upsampling`, DC removal, Hilbert analytic signal, rx apodization,
+	 * value = |sum|. */
+	USGB_PATH_ANALYTIC = 0,
+	/* DefaultSTAProcessor: fixed 4x FIR, DC removal, real samples, no
+	 * apodization, value = signed sum (`upsampling` must be 4). */
+	USGB_PATH_REAL = 1
+} usgb_signal_path;
+
+/* Coherence factor written to `factor` (1 when none). */
+typedef enum usgb_coherence {
+	USGB_CF_NONE = 0,
+	USGB_CF_PCF = 1, /* phase coherence factor, src/util/CoherenceFactor.h:240-296 */
+	USGB_CF_SCF = 2, /* sign coherence factor, src/util/CoherenceFactor.h:198-236 (on Re for the analytic path) */
+	USGB_CF_MF = 3   /* |sum s|^2 / (N sum |s|^2); no counterpart in the reference */
+} usgb_coherence;
+
+/* Storage type of the prepared signal tensor (accumulation is always FP32). */
+typedef enum usgb_storage {
+	USGB_STORE_F32 = 0,
+	USGB_STORE_F16 = 1,
+	USGB_STORE_BF16 = 2
+} usgb_storage;
+
+/*
+ * Frame description. Mirrors the constructor arguments of
+ * VectorialSTAProcessor(config, acquisition, upsamplingFactor, coherenceFactor,
+ * peakOffset, rxApod) (src/user/processor/VectorialSTAProcessor.h:61-67) with
+ * STAConfiguration's fields (src/user/configuration/STAConfiguration.h:29-48);
+ * element positions are given explicitly so that the linear array
+ * (ArrayGeometry::getElementXCentered2D, src/util/ArrayGeometry.h:37-49) and
+ * the 2D matrix array (ArrayUtil::calculateElementPositions,
+ * src/util/ArrayUtil.h:51-70) use the same entry points.
+ */
+typedef struct usgb_sta_params {
+	uint32_t num_tx;            /* active transmit elements (lastTxElem - firstTxElem + 1) */
+	uint32_t num_rx;            /* receive elements */
+	uint32_t num_samples;       /* samples per A-scan at sampling_frequency */
+	uint32_t upsampling;        /* upsamplingFactor, 1..64 (4 for USGB_PATH_REAL) */
+	uint32_t signal_path;       /* usgb_signal_path */
+	float sampling_frequency;   /* Hz */
+	float propagation_speed;    /* m/s */
+	float center_frequency;     /* Hz */
+	float peak_offset;          /* peakOffset, in periods of center_frequency */
+	float dead_zone_m;          /* m */
+	const float* tx_xy;         /* host, num_tx (x, y) pairs, m */
+	const float* rx_xy;         /* host, num_rx (x, y) pairs, m */
+	const float* rx_apod;       /* host, num_rx weights; NULL = all ones */
+	uint32_t coherence;         /* usgb_coherence */
+	float pcf_gamma;            /* phase_coherence_factor_gamma */
+	float scf_p;                /* sign_coherence_factor_p */
+	uint32_t storage;           /* usgb_storage */
+	float storage_scale;        /* samples are multiplied by this before FP16/BF16 storage; 0 = 1 */
+} usgb_sta_params;
+
+typedef struct usgb_ctx usgb_ctx;
+
+/* Creates a context on the current CUDA device (checks the parameters, builds
+ * the FIR and FFT tables, allocates the per-frame device buffers). */
+int usgb_create(const usgb_sta_params* params, usgb_ctx** ctx);
+void usgb_destroy(usgb_ctx* ctx);
+/* Message of the last failure on `ctx` (or of the last failed usgb_create on
+ * this thread when ctx is NULL). Never NULL. */
+const char* usgb_last_error(const usgb_ctx* ctx);
+
+/* Image grid: ncols * nrows points (x, y, z), column-major like the reference's
+ * Matrix<XYZValueFactor> (point(col, row) at index col * nrows + row,
+ * src/util/Matrix.h:188-198). Host pointer. */
+int usgb_set_grid(usgb_ctx* ctx, const float* xyz, uint32_t ncols, uint32_t nrows);
+
+/* RF of one transmit event, as STAAcquisition::execute delivers it
+ * (src/user/acquisition/STAAcquisition.h:36): num_rx rows of num_samples.
+ * tx is the index among the active transmit elements. Host pointer; the data
+ * is copied into the context's pinned staging buffer. */
+int usgb_submit_rf(usgb_ctx* ctx, uint32_t tx, const float* rf, uint32_t num_rx, uint32_t num_samples);
+
+/* Forms the image from the submitted RF, like ArrayProcessor::process:
+ * value = |sum| / (num_tx * num_rx) (signed sum for USGB_PATH_REAL) and
+ * factor = coherence factor (1 when none), both ncols * nrows floats in the
+ * grid's order, host pointers. Synchronous. */
+int usgb_process(usgb_ctx* ctx, float* value, float* factor);
+
+/* Device-resident forms (asynchronous on the context's stream). d_rf holds
+ * num_tx * num_rx * num_samples floats; d_value and d_factor ncols * nrows. */
+int usgb_set_stream(usgb_ctx* ctx, void* cuda_stream);
+int usgb_set_grid_device(usgb_ctx* ctx, const float* d_xyz, uint32_t ncols, uint32_t nrows);
+int usgb_process_device(usgb_ctx* ctx, const float* d_rf, float* d_value, float* d_factor);
+
+/* The two stages separately. d_signals holds num_tx * num_rx A-scans of
+ * signal_stride samples (complex (re, im) pairs on the analytic path, reals on
+ * the real path) in the context's storage type. */
+int usgb_prepare_signals_device(usgb_ctx* ctx, const float* d_rf, void* d_signals);
+int usgb_delay_and_sum_device(usgb_ctx* ctx, const void* d_signals, float* d_value, float* d_factor);
+
+/* Sizes: signal_length = num_samples * upsampling; fft_size = Hilbert FFT
+ * length N (0 on the real path); signal_stride = samples per A-scan in the
+ * signal tensor; signal_bytes = bytes of the whole tensor. */
+int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft_size,
+		uint32_t* signal_stride, size_t* signal_bytes);
+
+/* Selects the delay-and-sum kernel: 0 = plain (one thread per point, global
+ * gathers), 1 = staged (TMA-staged A-scan windows per pixel tile). */
+int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t tile_cols);
+
+/* Waits for the context's stream and reports a device-side error (a bounded
+ * wait that gave up) as USGB_ERR_DEVICE_TIMEOUT. */
+int usgb_synchronize(usgb_ctx* ctx);
+
+/* Library version string. */
+const char* usgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* USGB_H */

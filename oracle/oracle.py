@@ -1,0 +1,278 @@
+"""ctypes wrapper of the CPU oracle (``liboracle.so``, built from sta_oracle_capi.cpp).
+
+Test infrastructure only: the parity checker of the CUDA library and the CPU
+baseline of bench.py. The arithmetic lives in sta_oracle.hpp, which cites the
+reference file:line of every step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+CF_NONE, CF_PCF, CF_SCF, CF_MF = 0, 1, 2, 3
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the Makefile beside this file."""
+    if force or not os.path.exists(lib_path()) or _stale():
+        subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    return lib_path()
+
+
+def _stale() -> bool:
+    so = lib_path()
+    t = os.path.getmtime(so)
+    for f in ("sta_oracle_capi.cpp", "sta_oracle.hpp"):
+        if os.path.getmtime(os.path.join(_HERE, f)) > t:
+            return True
+    return False
+
+
+def available() -> bool:
+    return os.path.exists(lib_path())
+
+
+def _desc_type(ct):
+    class Desc(C.Structure):
+        _fields_ = [
+            ("num_tx", C.c_uint), ("num_rx", C.c_uint), ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("sampling_frequency", ct), ("propagation_speed", ct), ("center_frequency", ct),
+            ("peak_offset", ct), ("dead_zone_m", ct),
+            ("tx_xy", C.POINTER(ct)), ("rx_xy", C.POINTER(ct)), ("rx_apod", C.POINTER(ct)),
+            ("cf", C.c_int), ("pcf_gamma", ct), ("scf_p", ct),
+            ("real_path", C.c_int), ("nthreads", C.c_int),
+        ]
+    return Desc
+
+
+_Desc32 = _desc_type(C.c_float)
+_Desc64 = _desc_type(C.c_double)
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not available():
+            build()
+        lib = C.CDLL(lib_path())
+        lib.orc_last_error.restype = C.c_char_p
+        lib.orc_next_fast_even_size.restype = C.c_uint
+        lib.orc_next_fast_even_size.argtypes = [C.c_uint]
+        lib.orc_hilbert_fft_size.restype = C.c_uint
+        lib.orc_hilbert_fft_size.argtypes = [C.c_uint]
+        for name, ct, desc in (("f32", C.c_float, _Desc32), ("f64", C.c_double, _Desc64)):
+            p = C.POINTER(ct)
+            f = getattr(lib, "orc_process_" + name)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(desc), p, p, C.c_size_t, p, p, p]
+            f = getattr(lib, "orc_das_" + name)
+            f.restype = C.c_int
+            f.argtypes = [C.POINTER(desc), p, p, C.c_size_t, p, p]
+        lib.orc_scf_f64.restype = C.c_double
+        lib.orc_scf_f64.argtypes = [C.POINTER(C.c_double), C.c_uint, C.c_double]
+        lib.orc_pcf_f64.restype = C.c_double
+        lib.orc_pcf_f64.argtypes = [C.POINTER(C.c_double), C.c_uint, C.c_double]
+        _LIB = lib
+    return _LIB
+
+
+def _ptr(a: Optional[np.ndarray], ct):
+    if a is None:
+        return C.cast(None, C.POINTER(ct))
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _err(rc: int):
+    if rc != 0:
+        raise ValueError(_lib().orc_last_error().decode())
+
+
+@dataclass
+class OracleSpec:
+    """One STA frame: geometry, acquisition parameters and processing choices.
+
+    Field meaning follows STAConfiguration / SA3DConfiguration and the
+    VectorialSTAProcessor constructor arguments of the reference.
+    """
+    tx_xy: np.ndarray                  # (num_tx, 2) active transmit element centres, m
+    rx_xy: np.ndarray                  # (num_rx, 2) receive element centres, m
+    num_samples: int
+    upsampling: int
+    sampling_frequency: float
+    propagation_speed: float
+    center_frequency: float
+    peak_offset: float = 0.0
+    dead_zone_m: float = 0.0
+    rx_apod: Optional[np.ndarray] = None
+    cf: int = CF_NONE
+    pcf_gamma: float = 1.0
+    scf_p: float = 1.0
+    real_path: bool = False
+    nthreads: int = field(default_factory=lambda: os.cpu_count() or 1)
+
+    @property
+    def num_tx(self) -> int:
+        return int(self.tx_xy.shape[0])
+
+    @property
+    def num_rx(self) -> int:
+        return int(self.rx_xy.shape[0])
+
+    @property
+    def signal_length(self) -> int:
+        return self.num_samples * (4 if self.real_path else self.upsampling)
+
+
+def _make_desc(spec: OracleSpec, dtype):
+    desc_t, ct = (_Desc32, C.c_float) if dtype == np.float32 else (_Desc64, C.c_double)
+    keep = {
+        "tx": np.ascontiguousarray(spec.tx_xy, dtype=dtype),
+        "rx": np.ascontiguousarray(spec.rx_xy, dtype=dtype),
+        "apod": np.ascontiguousarray(spec.rx_apod if spec.rx_apod is not None else np.ones(spec.num_rx), dtype=dtype),
+    }
+    d = desc_t(
+        spec.num_tx, spec.num_rx, spec.num_samples, spec.upsampling,
+        spec.sampling_frequency, spec.propagation_speed, spec.center_frequency,
+        spec.peak_offset, spec.dead_zone_m,
+        _ptr(keep["tx"], ct), _ptr(keep["rx"], ct), _ptr(keep["apod"], ct),
+        spec.cf, spec.pcf_gamma, spec.scf_p, int(spec.real_path), int(spec.nthreads),
+    )
+    return d, keep, ct
+
+
+def process(spec: OracleSpec, rf: np.ndarray, grid_xyz: Optional[np.ndarray], dtype=np.float64,
+            want_signals: bool = False):
+    """Run the whole processor. rf: (num_tx, num_rx, num_samples). grid_xyz: (..., 3).
+
+    Returns (value, factor, signals); value/factor have grid_xyz.shape[:-1];
+    signals is the analytic tensor (complex, (num_tx, num_rx, L)) or the real
+    tensor for the real path, when want_signals.
+    """
+    d, keep, ct = _make_desc(spec, dtype)
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    assert rf.shape == (spec.num_tx, spec.num_rx, spec.num_samples), rf.shape
+    L = spec.signal_length
+    npix = 0
+    g = None
+    if grid_xyz is not None:
+        g = np.ascontiguousarray(grid_xyz, dtype=dtype).reshape(-1, 3)
+        npix = g.shape[0]
+    value = np.zeros(max(npix, 1), dtype=dtype)
+    factor = np.ones(max(npix, 1), dtype=dtype)
+    sig = None
+    if want_signals:
+        width = 1 if spec.real_path else 2
+        sig = np.zeros(spec.num_tx * spec.num_rx * L * width, dtype=dtype)
+    f = getattr(_lib(), "orc_process_" + ("f32" if dtype == np.float32 else "f64"))
+    _err(f(C.byref(d), _ptr(rf, ct), _ptr(g, ct), npix, _ptr(value, ct), _ptr(factor, ct), _ptr(sig, ct)))
+    if sig is not None:
+        if spec.real_path:
+            sig = sig.reshape(spec.num_tx, spec.num_rx, L)
+        else:
+            sig = sig.view(np.complex64 if dtype == np.float32 else np.complex128).reshape(spec.num_tx, spec.num_rx, L)
+    shape = grid_xyz.shape[:-1] if grid_xyz is not None else (0,)
+    return value[:npix].reshape(shape), factor[:npix].reshape(shape), sig
+
+
+def das(spec: OracleSpec, signals: np.ndarray, grid_xyz: np.ndarray, dtype=np.float64):
+    """Delay-and-sum only, on prepared signals (complex analytic or real tensor)."""
+    d, keep, ct = _make_desc(spec, dtype)
+    if spec.real_path:
+        s = np.ascontiguousarray(signals, dtype=dtype)
+    else:
+        s = np.ascontiguousarray(signals, dtype=np.complex64 if dtype == np.float32 else np.complex128).view(dtype)
+    g = np.ascontiguousarray(grid_xyz, dtype=dtype).reshape(-1, 3)
+    npix = g.shape[0]
+    value = np.zeros(npix, dtype=dtype)
+    factor = np.ones(npix, dtype=dtype)
+    f = getattr(_lib(), "orc_das_" + ("f32" if dtype == np.float32 else "f64"))
+    _err(f(C.byref(d), _ptr(s, ct), _ptr(g, ct), npix, _ptr(value, ct), _ptr(factor, ct)))
+    return value.reshape(grid_xyz.shape[:-1]), factor.reshape(grid_xyz.shape[:-1])
+
+
+def interp_taps(U: int, half_transition: float = 0.2, dtype=np.float64) -> np.ndarray:
+    cap = 8192
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    out = np.zeros(cap, dtype=dtype)
+    n = C.c_uint(0)
+    f = _lib().orc_interp_taps_f32 if dtype == np.float32 else _lib().orc_interp_taps_f64
+    f.argtypes = [C.c_uint, ct, C.POINTER(ct), C.c_uint, C.POINTER(C.c_uint)]
+    _err(f(U, half_transition, _ptr(out, ct), cap, C.byref(n)))
+    return out[: n.value].copy()
+
+
+def interp4x_taps() -> np.ndarray:
+    out = np.zeros(81, dtype=np.float64)
+    f = _lib().orc_interp4x_taps_f64
+    f.argtypes = [C.POINTER(C.c_double)]
+    n = f(_ptr(out, C.c_double))
+    return out[:n]
+
+
+def upsample(x: np.ndarray, U: int, taps: np.ndarray) -> np.ndarray:
+    dtype = taps.dtype
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    x = np.ascontiguousarray(x, dtype=dtype)
+    taps = np.ascontiguousarray(taps)
+    out = np.zeros(x.size * U, dtype=dtype)
+    f = _lib().orc_upsample_f32 if dtype == np.float32 else _lib().orc_upsample_f64
+    f.argtypes = [C.POINTER(ct), C.c_uint, C.c_uint, C.POINTER(ct), C.c_uint, C.POINTER(ct)]
+    f(_ptr(x, ct), x.size, U, _ptr(taps, ct), taps.size, _ptr(out, ct))
+    return out
+
+
+def hilbert(x: np.ndarray, dtype=np.float64) -> np.ndarray:
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    x = np.ascontiguousarray(x, dtype=dtype)
+    out = np.zeros(2 * x.size, dtype=dtype)
+    f = _lib().orc_hilbert_f32 if dtype == np.float32 else _lib().orc_hilbert_f64
+    f.argtypes = [C.POINTER(ct), C.c_uint, C.POINTER(ct)]
+    _err(f(_ptr(x, ct), x.size, _ptr(out, ct)))
+    return out.view(np.complex64 if dtype == np.float32 else np.complex128)
+
+
+def fft(x: np.ndarray, sign: int = -1) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    out = np.zeros_like(x)
+    f = _lib().orc_fft_f64
+    f.argtypes = [C.POINTER(C.c_double), C.c_uint, C.c_int, C.POINTER(C.c_double)]
+    f(_ptr(x.view(np.float64), C.c_double), x.size, sign, _ptr(out.view(np.float64), C.c_double))
+    return out
+
+
+def remove_dc(x: np.ndarray, begin: int) -> np.ndarray:
+    y = np.ascontiguousarray(x, dtype=np.float64).copy()
+    f = _lib().orc_remove_dc_f64
+    f.argtypes = [C.POINTER(C.c_double), C.c_uint, C.c_uint]
+    _err(f(_ptr(y, C.c_double), y.size, begin))
+    return y
+
+
+def scf(values: np.ndarray, p: float) -> float:
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    return float(_lib().orc_scf_f64(_ptr(v, C.c_double), v.size, p))
+
+
+def pcf(values: np.ndarray, gamma: float) -> float:
+    v = np.ascontiguousarray(values, dtype=np.complex128)
+    return float(_lib().orc_pcf_f64(_ptr(v.view(np.float64), C.c_double), v.size, gamma))
+
+
+def hilbert_fft_size(n: int) -> int:
+    return int(_lib().orc_hilbert_fft_size(n))
+
+
+def next_fast_even_size(n: int) -> int:
+    return int(_lib().orc_next_fast_even_size(n))

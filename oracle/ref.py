@@ -1,0 +1,106 @@
+"""ctypes wrapper of oracle/_ref/libref.so: the reference's own STA processors
+compiled from their sources with the shim headers of oracle/refbuild/.
+
+Test infrastructure only. The library exists only where the reference sources
+were present at build time (this container), so every user checks
+``available()`` first.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(_HERE, "_ref", "libref.so")
+REF_SRC = "/root/reference/src"
+_lib = None
+
+
+def build(force: bool = False) -> bool:
+    """Compile libref.so when the reference sources are present."""
+    if not os.path.isdir(REF_SRC):
+        return False
+    cmd = ["make", "-s", "-C", os.path.join(_HERE, "refbuild")]
+    if force:
+        cmd.append("-B")
+    subprocess.run(cmd, check=True)
+    return os.path.exists(LIB)
+
+
+def available() -> bool:
+    return os.path.exists(LIB)
+
+
+def _desc(ct):
+    class RefDesc(C.Structure):
+        _fields_ = [
+            ("num_elements", C.c_uint), ("first_tx_elem", C.c_uint), ("last_tx_elem", C.c_uint), ("pitch", ct),
+            ("is_3d", C.c_int), ("tx_nx", C.c_uint), ("tx_ny", C.c_uint), ("rx_nx", C.c_uint), ("rx_ny", C.c_uint),
+            ("tx_pitch_x", ct), ("tx_pitch_y", ct), ("rx_pitch_x", ct), ("rx_pitch_y", ct),
+            ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("sampling_frequency", ct), ("propagation_speed", ct), ("center_frequency", ct),
+            ("peak_offset", ct), ("dead_zone_m", ct), ("rx_apod", C.POINTER(ct)),
+            ("cf", C.c_int), ("pcf_gamma", ct), ("scf_p", ct), ("real_path", C.c_int),
+        ]
+    return RefDesc
+
+
+_D32, _D64 = _desc(C.c_float), _desc(C.c_double)
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB)
+        _lib.ref_last_error.restype = C.c_char_p
+        for name, ct, d in (("f32", C.c_float, _D32), ("f64", C.c_double, _D64)):
+            f = getattr(_lib, "ref_process_" + name)
+            p = C.POINTER(ct)
+            f.argtypes = [C.POINTER(d), p, p, C.c_uint, C.c_uint, p, p]
+            f.restype = C.c_int
+    return _lib
+
+
+def process(*, rf: np.ndarray, grid_xyz: np.ndarray, num_samples: int, upsampling: int, fs: float, c: float,
+            fc: float, peak_offset: float = 0.0, dead_zone_m: float = 0.0, rx_apod=None, cf: int = 0,
+            pcf_gamma: float = 1.0, scf_p: float = 1.0, real_path: bool = False,
+            num_elements: int = 0, first_tx: int = 0, last_tx: int = 0, pitch: float = 0.0,
+            matrix=None, dtype=np.float32, threads: int = 0):
+    """Run the reference processor. 2D: num_elements/first_tx/last_tx/pitch.
+    3D: matrix = (nx, ny, pitch_x, pitch_y) for both tx and rx arrays.
+    cf: 0 none, 1 PCF (analytic path), 2 SCF (real path).
+    Returns (value, factor) with grid_xyz.shape[:2]."""
+    lib = _load()
+    if threads:
+        os.environ["USGB_REF_THREADS"] = str(threads)
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    D = _D32 if dtype == np.float32 else _D64
+    nrx = num_elements if matrix is None else matrix[0] * matrix[1]
+    apod = np.ascontiguousarray(np.ones(nrx) if rx_apod is None else rx_apod, dtype=dtype)
+    d = D()
+    d.num_elements, d.first_tx_elem, d.last_tx_elem, d.pitch = num_elements, first_tx, last_tx, pitch
+    if matrix is not None:
+        d.is_3d = 1
+        d.tx_nx = d.rx_nx = matrix[0]
+        d.tx_ny = d.rx_ny = matrix[1]
+        d.tx_pitch_x = d.rx_pitch_x = matrix[2]
+        d.tx_pitch_y = d.rx_pitch_y = matrix[3]
+    d.num_samples, d.upsampling = num_samples, upsampling
+    d.sampling_frequency, d.propagation_speed, d.center_frequency = fs, c, fc
+    d.peak_offset, d.dead_zone_m = peak_offset, dead_zone_m
+    d.rx_apod = apod.ctypes.data_as(C.POINTER(ct))
+    d.cf, d.pcf_gamma, d.scf_p, d.real_path = cf, pcf_gamma, scf_p, int(real_path)
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    g = np.ascontiguousarray(grid_xyz, dtype=dtype)
+    n1, n2 = g.shape[0], g.shape[1]
+    value = np.zeros((n1, n2), dtype)
+    factor = np.zeros((n1, n2), dtype)
+    f = lib.ref_process_f32 if dtype == np.float32 else lib.ref_process_f64
+    rc = f(C.byref(d), rf.ctypes.data_as(C.POINTER(ct)), g.ctypes.data_as(C.POINTER(ct)), n1, n2,
+           value.ctypes.data_as(C.POINTER(ct)), factor.ctypes.data_as(C.POINTER(ct)))
+    if rc != 0:
+        raise RuntimeError(lib.ref_last_error().decode())
+    return value, factor

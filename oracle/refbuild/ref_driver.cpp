@@ -1,0 +1,204 @@
+// Driver that runs the reference's own STA processors, compiled from their
+// unchanged sources (src/user/processor/{VectorialSTAProcessor,
+// Vectorial3DSTAProcessor,DefaultSTAProcessor}.h), on in-memory RF.
+// TEST INFRASTRUCTURE ONLY: it produces golden outputs for the parity tests
+// and validates the oracle restatement; nothing in the product uses it.
+//
+// The processors are constructed exactly as STAMethod / STA3DMethod construct
+// them (src/user/method/STAMethod.cpp:191-229, STA3DMethod.cpp:146-163),
+// with coherence-factor objects built from ParameterMap files the same way
+// the reference's project files configure them.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <unistd.h>
+
+#include "DefaultSTAProcessor.h"
+#include "Vectorial3DSTAProcessor.h"
+#include "VectorialSTAProcessor.h"
+#include "XYZValueFactor.h"
+
+using namespace Lab;
+
+namespace {
+
+thread_local std::string g_err;
+
+// STAAcquisition over a caller-owned (numTx, numRx, numSamples) RF block.
+template<typename T>
+class MemoryAcquisition : public STAAcquisition<T> {
+public:
+	MemoryAcquisition(const T* rf, unsigned firstTx, unsigned numRx, unsigned ns)
+		: rf_(rf), firstTx_(firstTx), numRx_(numRx), ns_(ns) {}
+	void execute(unsigned int txElement, typename STAAcquisition<T>::AcquisitionDataType& acqData) override
+	{
+		acqData.resize(numRx_, ns_);
+		const T* src = rf_ + static_cast<std::size_t>(txElement - firstTx_) * numRx_ * ns_;
+		for (unsigned r = 0; r < numRx_; ++r) {
+			for (unsigned s = 0; s < ns_; ++s) acqData(r, s) = src[static_cast<std::size_t>(r) * ns_ + s];
+		}
+	}
+private:
+	const T* rf_;
+	unsigned firstTx_, numRx_, ns_;
+};
+
+// Temporary key=value file for ParameterMap.
+struct TempParamFile {
+	std::string path;
+	explicit TempParamFile(const std::string& text)
+	{
+		char tmpl[] = "/tmp/usgb_ref_pm_XXXXXX";
+		const int fd = mkstemp(tmpl);
+		if (fd < 0) throw std::runtime_error("mkstemp failed");
+		close(fd);
+		path = tmpl;
+		std::ofstream out(path);
+		out << text;
+	}
+	~TempParamFile() { std::remove(path.c_str()); }
+};
+
+template<typename T>
+struct RefDesc {
+	// 2D linear array (STAConfiguration) ...
+	unsigned num_elements, first_tx_elem, last_tx_elem;
+	T pitch;
+	// ... or 3D matrix array (SA3DConfiguration), used when is_3d != 0.
+	int is_3d;
+	unsigned tx_nx, tx_ny, rx_nx, rx_ny;
+	T tx_pitch_x, tx_pitch_y, rx_pitch_x, rx_pitch_y;
+	// Common acquisition parameters.
+	unsigned num_samples, upsampling;
+	T sampling_frequency, propagation_speed, center_frequency, peak_offset, dead_zone_m;
+	const T* rx_apod;
+	int cf;  // 0 none, 1 PCF (analytic path), 2 SCF (real path)
+	T pcf_gamma, scf_p;
+	int real_path;
+};
+
+template<typename T>
+void fill_config(const RefDesc<T>& d, STAConfiguration<T>& c)
+{
+	c.numElementsMux = d.num_elements;
+	c.numElements = d.num_elements;
+	c.firstTxElem = d.first_tx_elem;
+	c.lastTxElem = d.last_tx_elem;
+	c.numPulses = 1;
+	c.pitch = d.pitch;
+	c.centerFrequency = d.center_frequency;
+	c.maxFrequency = d.center_frequency * 2;
+	c.acquisitionTime = 1e-4;
+	c.minGain = 0;
+	c.maxGain = 0;
+	c.propagationSpeed = d.propagation_speed;
+	c.acquisitionDelay = 0;
+	c.samplingFrequency = d.sampling_frequency;
+	c.deadZoneM = d.dead_zone_m;
+	c.valueScale = 1;
+}
+
+template<typename T>
+int run(const RefDesc<T>* dp, const T* rf, const T* gridXYZ, unsigned n1, unsigned n2, T* value, T* factor)
+{
+	try {
+		const RefDesc<T>& d = *dp;
+		Matrix<XYZValueFactor<T>> grid(n1, n2);
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				grid(i, j).x = gridXYZ[3 * p];
+				grid(i, j).y = gridXYZ[3 * p + 1];
+				grid(i, j).z = gridXYZ[3 * p + 2];
+			}
+		}
+		if (d.real_path) {
+			STAConfiguration<T> c;
+			fill_config(d, c);
+			const unsigned numRx = c.numElements;
+			MemoryAcquisition<T> acq(rf, c.firstTxElem, numRx, d.num_samples);
+			std::string text = "coherence_factor_method = none\n";
+			if (d.cf == 2) {
+				text = "coherence_factor_method = sign_coherence_factor\nsign_coherence_factor_p = " +
+						std::to_string(static_cast<double>(d.scf_p)) + "\n";
+			}
+			TempParamFile f(text);
+			ParameterMap pm(f.path);
+			CoherenceFactorProcessor<T> cf(pm);
+			DefaultSTAProcessor<T, XYZValueFactor<T>> proc(c, acq, cf, d.peak_offset);
+			proc.prepare(0);
+			proc.process(grid);
+		} else {
+			std::string text = "analytic_signal_coherence_factor_method = none\n";
+			if (d.cf == 1) {
+				char buf[64];
+				std::snprintf(buf, sizeof buf, "%.17g", static_cast<double>(d.pcf_gamma));
+				text = std::string("analytic_signal_coherence_factor_method = phase_coherence_factor\n"
+						"phase_coherence_factor_gamma = ") + buf + "\n";
+			}
+			TempParamFile f(text);
+			ParameterMap pm(f.path);
+			AnalyticSignalCoherenceFactorProcessor<T> cf(pm);
+			if (d.is_3d) {
+				SA3DConfiguration<T> c;
+				c.numElementsMux = 1024;
+				c.numPulses = 1;
+				c.centerFrequency = d.center_frequency;
+				c.maxFrequency = d.center_frequency * 2;
+				c.acquisitionTime = 1e-4;
+				c.minGain = 0;
+				c.maxGain = 0;
+				c.propagationSpeed = d.propagation_speed;
+				c.acquisitionDelay = 0;
+				c.samplingFrequency = d.sampling_frequency;
+				c.deadZoneM = d.dead_zone_m;
+				c.valueScale = 1;
+				ArrayUtil::calculateElementPositions(d.tx_pitch_x, d.tx_nx, T(0), d.tx_pitch_y, d.tx_ny, T(0), c.txElemPos);
+				ArrayUtil::calculateElementPositions(d.rx_pitch_x, d.rx_nx, T(0), d.rx_pitch_y, d.rx_ny, T(0), c.rxElemPos);
+				for (unsigned i = 0; i < c.txElemPos.size(); ++i) c.activeTxElem.push_back(i);
+				for (unsigned i = 0; i < c.rxElemPos.size(); ++i) c.activeRxElem.push_back(i);
+				const unsigned numRx = static_cast<unsigned>(c.rxElemPos.size());
+				std::vector<T> apod(d.rx_apod, d.rx_apod + numRx);
+				MemoryAcquisition<T> acq(rf, 0, numRx, d.num_samples);
+				Vectorial3DSTAProcessor<T> proc(c, acq, d.upsampling, cf, d.peak_offset, apod);
+				proc.prepare(0);
+				proc.process(grid);
+			} else {
+				STAConfiguration<T> c;
+				fill_config(d, c);
+				const unsigned numRx = c.numElements;
+				std::vector<T> apod(d.rx_apod, d.rx_apod + numRx);
+				MemoryAcquisition<T> acq(rf, c.firstTxElem, numRx, d.num_samples);
+				VectorialSTAProcessor<T, XYZValueFactor<T>> proc(c, acq, d.upsampling, cf, d.peak_offset, apod);
+				proc.prepare(0);
+				proc.process(grid);
+			}
+		}
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				value[p] = grid(i, j).value;
+				factor[p] = grid(i, j).factor;
+			}
+		}
+		return 0;
+	} catch (std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+const char* ref_last_error(void) { return g_err.c_str(); }
+int ref_process_f32(const RefDesc<float>* d, const float* rf, const float* grid, unsigned n1, unsigned n2, float* value, float* factor)
+{
+	return run<float>(d, rf, grid, n1, n2, value, factor);
+}
+int ref_process_f64(const RefDesc<double>* d, const double* rf, const double* grid, unsigned n1, unsigned n2, double* value, double* factor)
+{
+	return run<double>(d, rf, grid, n1, n2, value, factor);
+}
+}

@@ -1,0 +1,665 @@
+// CPU oracle for the STA/TFM delay-and-sum path of us_lab4a.
+//
+// TEST INFRASTRUCTURE ONLY. This is a restatement, in plain C++17, of the
+// reference processors' arithmetic. It is the parity checker for the CUDA
+// library and the CPU baseline that bench.py reports; the product never links,
+// loads or calls it.
+//
+// Every function names the reference file:line it follows. TFloat is float for
+// the FP32 parity target (VectorialSTAProcessor<float,...>) and double for the
+// FP64 oracle (VectorialSTAProcessor<double,...>). Expressions that the
+// reference evaluates in mixed float/double are evaluated the same way here.
+#ifndef USGB_STA_ORACLE_HPP
+#define USGB_STA_ORACLE_HPP
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// Sizes.
+// ---------------------------------------------------------------------------
+
+// Smallest even n' >= n whose only prime factors are 2, 3 and 5.
+// Follows src/fft/FFTUtil.h:85-135 (nextFastEvenSize).
+inline unsigned next_fast_even_size(unsigned n)
+{
+	if (n == 0) throw std::invalid_argument("n must be > 0");
+	if (n & 1U) ++n;
+	for (;;) {
+		unsigned m = n;
+		while ((m & 1U) == 0) m >>= 1;
+		while (m % 3 == 0) m /= 3;
+		while (m % 5 == 0) m /= 5;
+		if (m == 1) return n;
+		n += 2;
+	}
+}
+
+// Hilbert FFT size for an A-scan of `len` samples.
+// Follows src/util/HilbertEnvelope.h:152 (minPadding = 1024, at least 2048).
+inline unsigned hilbert_fft_size(unsigned len)
+{
+	return std::max(next_fast_even_size(len + 1024U), 2048U);
+}
+
+// ---------------------------------------------------------------------------
+// Parallel loop (the reference uses tbb::parallel_for over receivers and over
+// grid columns; results do not depend on the partition because every output
+// is computed by one thread in a fixed order).
+// ---------------------------------------------------------------------------
+inline void parallel_for(std::size_t n, int nthreads, const std::function<void(std::size_t, std::size_t)>& body)
+{
+	if (nthreads <= 1 || n < 2) {
+		body(0, n);
+		return;
+	}
+	const std::size_t nt = std::min<std::size_t>(static_cast<std::size_t>(nthreads), n);
+	std::atomic<std::size_t> next{0};
+	const std::size_t grain = std::max<std::size_t>(1, n / (nt * 8));
+	std::vector<std::thread> pool;
+	pool.reserve(nt);
+	for (std::size_t t = 0; t < nt; ++t) {
+		pool.emplace_back([&]() {
+			for (;;) {
+				const std::size_t b = next.fetch_add(grain);
+				if (b >= n) break;
+				body(b, std::min(n, b + grain));
+			}
+		});
+	}
+	for (auto& th : pool) th.join();
+}
+
+// ---------------------------------------------------------------------------
+// Complex FFT (own implementation; the reference links FFTW3, which is absent
+// here). Iterative Stockham autosort, radices 4, 2, 3, 5 and a direct DFT for
+// any other prime factor. Twiddles are evaluated directly in double and then
+// rounded to T, so each twiddle is within half an ulp.
+// sign = -1: forward (FFTW_FORWARD), sign = +1: backward (unnormalised).
+// ---------------------------------------------------------------------------
+template<typename T>
+class FFT {
+public:
+	using C = std::complex<T>;
+
+	FFT() = default;
+	explicit FFT(unsigned n) { init(n); }
+
+	void init(unsigned n)
+	{
+		n_ = n;
+		radices_.clear();
+		unsigned m = n;
+		while (m % 4 == 0) { radices_.push_back(4); m /= 4; }
+		while (m % 2 == 0) { radices_.push_back(2); m /= 2; }
+		while (m % 3 == 0) { radices_.push_back(3); m /= 3; }
+		while (m % 5 == 0) { radices_.push_back(5); m /= 5; }
+		for (unsigned p = 7; m > 1; p += 2) {
+			while (m % p == 0) { radices_.push_back(p); m /= p; }
+		}
+		// Per-stage twiddles w_{l p}^{q k}, k < l, q < p.
+		tw_.clear();
+		stageOffset_.clear();
+		unsigned l = 1;
+		for (unsigned p : radices_) {
+			stageOffset_.push_back(static_cast<unsigned>(tw_.size()));
+			for (unsigned k = 0; k < l; ++k) {
+				for (unsigned q = 0; q < p; ++q) {
+					const double a = -2.0 * kPi * static_cast<double>(q) * static_cast<double>(k) /
+							static_cast<double>(l * p);
+					tw_.emplace_back(static_cast<T>(std::cos(a)), static_cast<T>(std::sin(a)));
+				}
+			}
+			l *= p;
+		}
+		work_.assign(n, C(0));
+	}
+
+	unsigned size() const { return n_; }
+
+	// out may alias in.
+	void execute(const C* in, C* out, int sign)
+	{
+		bufA_.assign(in, in + n_);
+		bufB_.resize(n_);
+		C* x = bufA_.data();
+		C* y = bufB_.data();
+		unsigned l = 1;
+		for (std::size_t s = 0; s < radices_.size(); ++s) {
+			const unsigned p = radices_[s];
+			const unsigned m = n_ / (l * p);
+			const C* tw = tw_.data() + stageOffset_[s];
+			for (unsigned r = 0; r < m; ++r) {
+				for (unsigned k = 0; k < l; ++k) {
+					C v[64];
+					C* vv = v;
+					std::vector<C> big;
+					if (p > 64) { big.resize(p); vv = big.data(); }
+					for (unsigned q = 0; q < p; ++q) {
+						C t = x[k + l * (r + q * m)];
+						C w = tw[k * p + q];
+						if (sign > 0) w = std::conj(w);
+						vv[q] = (q == 0) ? t : t * w;
+					}
+					butterfly(vv, p, sign);
+					for (unsigned q = 0; q < p; ++q) {
+						y[k + l * q + l * p * r] = vv[q];
+					}
+				}
+			}
+			std::swap(x, y);
+			l *= p;
+		}
+		std::copy(x, x + n_, out);
+	}
+
+private:
+	static void butterfly(C* v, unsigned p, int sign)
+	{
+		const T s = static_cast<T>(sign);
+		switch (p) {
+		case 2: {
+			const C a = v[0], b = v[1];
+			v[0] = a + b; v[1] = a - b;
+			return;
+		}
+		case 3: {
+			const T c1 = static_cast<T>(-0.5);
+			const T s1 = static_cast<T>(0.86602540378443864676) * s;  // sin(2pi/3) * sign
+			const C a = v[0], b = v[1], c = v[2];
+			const C t1 = b + c;
+			const C t2 = a + c1 * t1;
+			const C t3 = (b - c) * C(0, s1);
+			v[0] = a + t1; v[1] = t2 + t3; v[2] = t2 - t3;
+			return;
+		}
+		case 4: {
+			const C a = v[0], b = v[1], c = v[2], d = v[3];
+			const C t0 = a + c, t1 = a - c, t2 = b + d;
+			const C t3 = (b - d) * C(0, s);  // multiply by +-i
+			v[0] = t0 + t2; v[2] = t0 - t2;
+			v[1] = t1 + t3; v[3] = t1 - t3;
+			return;
+		}
+		case 5: {
+			const T c1 = static_cast<T>(0.30901699437494742410);   // cos(2pi/5)
+			const T c2 = static_cast<T>(-0.80901699437494742410);  // cos(4pi/5)
+			const T s1 = static_cast<T>(0.95105651629515357212) * s;
+			const T s2 = static_cast<T>(0.58778525229247312917) * s;
+			const C a = v[0];
+			const C b1 = v[1] + v[4], b2 = v[2] + v[3];
+			const C d1 = v[1] - v[4], d2 = v[2] - v[3];
+			const C r1 = a + c1 * b1 + c2 * b2;
+			const C r2 = a + c2 * b1 + c1 * b2;
+			const C i1 = C(0, 1) * (s1 * d1 + s2 * d2);
+			const C i2 = C(0, 1) * (s2 * d1 - s1 * d2);
+			v[0] = a + b1 + b2;
+			v[1] = r1 + i1; v[4] = r1 - i1;
+			v[2] = r2 + i2; v[3] = r2 - i2;
+			return;
+		}
+		default: {
+			std::vector<C> out(p, C(0));
+			for (unsigned k = 0; k < p; ++k) {
+				for (unsigned j = 0; j < p; ++j) {
+					const double a = static_cast<double>(sign) * 2.0 * kPi *
+							static_cast<double>((static_cast<unsigned long long>(j) * k) % p) / static_cast<double>(p);
+					out[k] += v[j] * C(static_cast<T>(std::cos(a)), static_cast<T>(std::sin(a)));
+				}
+			}
+			std::copy(out.begin(), out.end(), v);
+			return;
+		}
+		}
+	}
+
+	unsigned n_ = 0;
+	std::vector<unsigned> radices_;
+	std::vector<unsigned> stageOffset_;
+	std::vector<C> tw_;
+	std::vector<C> work_;
+	std::vector<C> bufA_, bufB_;
+};
+
+// ---------------------------------------------------------------------------
+// Kaiser window helpers. Follow src/util/KaiserWindow.h:45-93.
+// ---------------------------------------------------------------------------
+template<typename T>
+T kaiser_beta(T tolerance_dB)
+{
+	T beta;
+	if (tolerance_dB > 50) {
+		beta = 0.1102 * (tolerance_dB - 8.7);
+	} else if (tolerance_dB > 21) {
+		const double k = tolerance_dB - 21.0;
+		beta = 0.5842 * std::pow(k, 0.4) + 0.07886 * k;
+	} else {
+		beta = 0.0;
+	}
+	return beta;
+}
+
+template<typename T>
+unsigned kaiser_size(T tolerance_dB, T transitionWidth)
+{
+	const double size = std::ceil((tolerance_dB - 7.95) / (2.285 * transitionWidth * kPi) + 1.0);
+	if (size < 2.0 || size >= static_cast<double>(std::numeric_limits<unsigned>::max())) {
+		throw std::invalid_argument("invalid Kaiser window size");
+	}
+	return static_cast<unsigned>(size);
+}
+
+inline double bessel_i0(double x) { return std::cyl_bessel_i(0.0, x); }
+inline float bessel_i0(float x) { return std::cyl_bessel_if(0.0f, x); }
+
+template<typename T>
+void kaiser_window(unsigned size, T beta, std::vector<T>& w)
+{
+	if (size < 2) throw std::invalid_argument("invalid Kaiser window size");
+	w.resize(size);
+	const T c1 = 2 / static_cast<T>(size - 1U);
+	const T c2 = 1 / bessel_i0(beta);
+	for (unsigned n = 0; n < size; ++n) {
+		const T k = c1 * n - 1;
+		T x = 1 - k * k;
+		if (x < 0.0) x = 0.0;
+		w[n] = c2 * bessel_i0(static_cast<T>(beta * std::sqrt(x)));
+	}
+}
+
+// sin(x)/x, evaluated in double (the reference passes a double argument to
+// boost::math::sinc_pi; its series branch near 0 agrees with sin(x)/x to
+// within rounding).
+inline double sinc_of(double x)
+{
+	if (std::abs(x) < 1.0e-5) return 1.0 - x * x / 6.0;
+	return std::sin(x) / x;
+}
+
+// Low-pass FIR of the upsampler: Kaiser-windowed sinc, tolerance 1e-4, length
+// rounded up to a multiple of 2U plus 1.
+// Follows src/util/Interpolator.h:64-111 and Util::fillSequenceFromStartToEndWithSize
+// (src/util/Util.h:328-345).
+template<typename T>
+std::vector<T> interpolator_taps(unsigned U, T halfTransitionWidth)
+{
+	if (U < 2 || U > 64) throw std::invalid_argument("invalid upsampling factor");
+	if (halfTransitionWidth > 1) throw std::invalid_argument("invalid transition width");
+	const double kaiserTolerance = 1.0e-4;
+	const T tol_dB = -20.0 * std::log10(kaiserTolerance);
+	const T beta = kaiser_beta<T>(tol_dB);
+	const T finalTransitionWidth = (halfTransitionWidth * 2) / U;
+	const unsigned windowSize = kaiser_size<T>(tol_dB, finalTransitionWidth);
+	const T twoUp = 2 * U;
+	const unsigned finalSize = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
+
+	std::vector<T> window;
+	kaiser_window<T>(finalSize, beta, window);
+
+	const T numPeriods = (finalSize - 1U) / twoUp;
+	std::vector<T> x(finalSize);
+	{
+		const double step = static_cast<double>(numPeriods - (-numPeriods)) / (finalSize - 1U);
+		x[0] = -numPeriods;
+		for (unsigned i = 1; i < finalSize; ++i) x[i] = -numPeriods + i * step;
+	}
+	std::vector<T> taps(finalSize);
+	for (unsigned i = 0; i < finalSize; ++i) {
+		taps[i] = static_cast<T>(sinc_of(kPi * x[i]));
+	}
+	for (unsigned i = 0; i < finalSize; ++i) taps[i] *= window[i];
+	return taps;
+}
+
+// Fixed 4x low-pass FIR of the real-RF path, regenerated from the recipe
+// stated in src/util/Interpolator4X.h:56-66 (Octave: n = 10 periods * 8,
+// kaiser(n + 1, beta = 5) .* sinc(linspace(-10, 10, n + 1))), in double.
+inline std::vector<double> interpolator4x_taps_double()
+{
+	const unsigned n = 80;
+	const double beta = 5.0;
+	std::vector<double> h(n + 1);
+	const double i0b = std::cyl_bessel_i(0.0, beta);
+	for (unsigned i = 0; i <= n; ++i) {
+		const double r = 2.0 * i / n - 1.0;
+		double arg = 1.0 - r * r;
+		if (arg < 0.0) arg = 0.0;
+		const double w = std::cyl_bessel_i(0.0, beta * std::sqrt(arg)) / i0b;
+		const double xv = -10.0 + 20.0 * i / n;
+		const double s = (xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv);
+		h[i] = s * w;
+	}
+	return h;
+}
+
+// Upsampling by zero stuffing and linear convolution with `taps`, keeping
+// samples [(taps-1)/2, (taps-1)/2 + len*U) of the full convolution.
+// Follows src/util/Interpolator.h:113-138; the overlap-save FFT convolution of
+// src/util/FFTWFilter.h:239-289 computes this same linear convolution.
+template<typename T>
+void upsample(const T* in, unsigned len, unsigned U, const std::vector<T>& taps, T* out)
+{
+	const long ntaps = static_cast<long>(taps.size());
+	const long off = (ntaps - 1) / 2;
+	const long L = static_cast<long>(len) * U;
+	for (long n = 0; n < L; ++n) {
+		const long j = n + off;  // index into the full convolution
+		T acc = 0;
+		// out[n] = sum_m taps[m] * up[j - m], up[i] = in[i / U] if i % U == 0.
+		long mStart = j % U;  // smallest m with (j - m) % U == 0
+		for (long m = mStart; m < ntaps; m += U) {
+			const long src = (j - m) / U;
+			if (src < 0) break;
+			if (src >= static_cast<long>(len)) continue;
+			acc += taps[m] * in[src];
+		}
+		out[n] = acc;
+	}
+}
+
+// Subtract the mean of data[beginOffset, size) from all `size` samples.
+// Follows src/util/Util.h:1009-1018.
+template<typename T>
+void remove_dc(T* data, std::size_t size, std::size_t beginOffset)
+{
+	if (beginOffset >= size) throw std::invalid_argument("invalid beginOffset");
+	T sum = 0;
+	for (std::size_t i = beginOffset; i < size; ++i) sum += data[i];
+	const T term = -sum / static_cast<T>(size - beginOffset);
+	for (std::size_t i = 0; i < size; ++i) data[i] += term;
+}
+
+// Analytic signal by FFT: zero-pad to N, forward FFT, halve bins 0 and N/2,
+// zero bins N/2+1..N-1, backward FFT, scale 2/N, keep the first `len`.
+// Follows src/util/HilbertEnvelope.h:142-197 and :227-251.
+template<typename T>
+class Hilbert {
+public:
+	using C = std::complex<T>;
+	void analytic(const T* x, unsigned len, C* out)
+	{
+		if (len == 0 || len > (1U << 20)) throw std::invalid_argument("invalid Hilbert input size");
+		const unsigned N = hilbert_fft_size(len);
+		if (fft_.size() != N) fft_.init(N);
+		buf_.assign(N, C(0));
+		for (unsigned i = 0; i < len; ++i) buf_[i] = C(x[i], 0);
+		fft_.execute(buf_.data(), buf_.data(), -1);
+		buf_[0] = C(buf_[0].real() * static_cast<T>(0.5), buf_[0].imag());
+		buf_[N / 2] = C(buf_[N / 2].real() * static_cast<T>(0.5), buf_[N / 2].imag());
+		for (unsigned k = N / 2 + 1; k < N; ++k) buf_[k] = C(0);
+		fft_.execute(buf_.data(), buf_.data(), +1);
+		const T coef = 2 / static_cast<T>(N);
+		for (unsigned i = 0; i < len; ++i) out[i] = C(coef * buf_[i].real(), coef * buf_[i].imag());
+	}
+private:
+	FFT<T> fft_;
+	std::vector<C> buf_;
+};
+
+// ---------------------------------------------------------------------------
+// Geometry. Follows src/util/Geometry.h:55-84.
+// ---------------------------------------------------------------------------
+template<typename T>
+T distance3d_z0(T x0, T y0, T x1, T y1, T z1)
+{
+	const T dx = x1 - x0;
+	const T dy = y1 - y0;
+	return std::sqrt(dx * dx + dy * dy + z1 * z1);
+}
+
+// ---------------------------------------------------------------------------
+// Coherence factors.
+// ---------------------------------------------------------------------------
+
+// Population standard deviation, two-pass. Follows src/util/Statistics.h:34-58.
+template<typename T>
+T std_dev(const T* d, std::size_t n)
+{
+	T s = 0;
+	for (std::size_t i = 0; i < n; ++i) s += d[i];
+	const T mean = s / n;
+	T acc = 0;
+	for (std::size_t i = 0; i < n; ++i) {
+		const T e = d[i] - mean;
+		acc += e * e;
+	}
+	return std::sqrt(acc / n);
+}
+
+// Phase coherence factor (Camacho et al. 2009).
+// Follows src/util/CoherenceFactor.h:240-296.
+template<typename T>
+T pcf(const std::complex<T>* d, unsigned n, T factor, std::vector<T>& phi, std::vector<T>& phiAux)
+{
+	phi.resize(n);
+	phiAux.resize(n);
+	for (unsigned i = 0; i < n; ++i) {
+		phi[i] = std::atan2(d[i].imag(), d[i].real());
+		phiAux[i] = phi[i] + ((phi[i] < 0) ? T(kPi) : -T(kPi));
+	}
+	const T sf = std::min(std_dev(phi.data(), n), std_dev(phiAux.data(), n));
+	return std::max<T>(0, 1 - factor * sf);
+}
+
+// Sign coherence factor on real values, sign(0) = +1.
+// Follows src/util/CoherenceFactor.h:217-236.
+template<typename T>
+T scf(const T* d, unsigned size, T p)
+{
+	unsigned n = 0;
+	int signSum = 0;
+	for (unsigned i = 0; i < size; ++i) {
+		if (d[i] >= 0) ++signSum; else --signSum;
+		++n;
+	}
+	const T k = static_cast<T>(signSum) / n;
+	const T m = 1 - std::sqrt(1 - k * k);
+	return std::pow(std::abs(m), p);
+}
+
+// Mallart-Fink coherence factor |sum s|^2 / (N sum |s|^2). The reference has
+// no such factor; this definition is the library's own.
+template<typename T>
+T mallart_fink_cf(const std::complex<T>* d, unsigned n)
+{
+	std::complex<T> s(0);
+	T e = 0;
+	for (unsigned i = 0; i < n; ++i) {
+		s += d[i];
+		e += std::norm(d[i]);
+	}
+	if (e == 0) return 0;
+	return std::norm(s) / (static_cast<T>(n) * e);
+}
+
+enum CFKind { CF_NONE = 0, CF_PCF = 1, CF_SCF = 2, CF_MF = 3 };
+
+// ---------------------------------------------------------------------------
+// Whole processor.
+// ---------------------------------------------------------------------------
+template<typename T>
+struct StaDesc {
+	unsigned numTx = 0;          // active transmit elements
+	unsigned numRx = 0;          // receive elements
+	unsigned numSamples = 0;     // samples per A-scan at fs
+	unsigned upsampling = 1;     // 1 = no upsampling
+	T samplingFrequency = 0;
+	T propagationSpeed = 0;
+	T centerFrequency = 0;
+	T peakOffset = 0;
+	T deadZoneM = 0;
+	const T* txXY = nullptr;     // numTx (x, y) pairs, metres
+	const T* rxXY = nullptr;     // numRx (x, y) pairs, metres
+	const T* rxApod = nullptr;   // numRx weights (analytic path)
+	int cf = CF_NONE;
+	T pcfGamma = 1;
+	T scfP = 1;
+	bool realPath = false;       // DefaultSTAProcessor semantics
+	int nthreads = 1;
+};
+
+// deadZoneSamplesUp, evaluated as in src/user/processor/VectorialSTAProcessor.h:138.
+template<typename T>
+unsigned dead_zone_samples(const StaDesc<T>& d, unsigned U)
+{
+	return static_cast<unsigned>((U * d.samplingFrequency) * 2.0 * d.deadZoneM / d.propagationSpeed);
+}
+
+// Signal preparation of every A-scan into `tensor` (numTx * numRx * L).
+// Analytic path: follows src/user/processor/VectorialSTAProcessor.h:169-235.
+// Real path: follows src/user/processor/DefaultSTAProcessor.h:121-156.
+template<typename T>
+void prepare_signals(const StaDesc<T>& d, const T* rf, std::vector<std::complex<T>>* analytic, std::vector<T>* real)
+{
+	const unsigned U = d.realPath ? 4U : d.upsampling;
+	const unsigned L = d.numSamples * U;
+	const unsigned dz = dead_zone_samples(d, U);
+	if (dz >= L) throw std::invalid_argument("invalid dead zone");
+	std::vector<T> taps;
+	if (d.realPath) {
+		const std::vector<double> h = interpolator4x_taps_double();
+		taps.assign(h.begin(), h.end());
+	} else if (U > 1) {
+		taps = interpolator_taps<T>(U, static_cast<T>(0.2));
+	}
+	const std::size_t numSig = static_cast<std::size_t>(d.numTx) * d.numRx;
+	if (analytic) analytic->assign(numSig * L, std::complex<T>(0));
+	if (real) real->assign(numSig * L, T(0));
+	parallel_for(numSig, d.nthreads, [&](std::size_t b, std::size_t e) {
+		std::vector<T> sig(L);
+		Hilbert<T> hil;
+		for (std::size_t a = b; a < e; ++a) {
+			const T* src = rf + a * d.numSamples;
+			if (U > 1) {
+				upsample<T>(src, d.numSamples, U, taps, sig.data());
+			} else {
+				std::copy(src, src + d.numSamples, sig.begin());
+			}
+			remove_dc<T>(sig.data(), L, dz);
+			if (d.realPath) {
+				std::copy(sig.begin(), sig.end(), real->begin() + a * L);
+			} else {
+				hil.analytic(sig.data(), L, analytic->data() + a * L);
+			}
+		}
+	});
+}
+
+// Delay-and-sum over every tx x rx pair for each grid point, with optional
+// coherence factor.
+// Analytic path: follows src/user/processor/VectorialSTAProcessor.h:237-338
+// (with the 3D delay of src/user/processor/Vectorial3DSTAProcessor.h:208-242;
+// for y = 0 it equals distance2DY0 bit for bit).
+// Real path: follows src/user/processor/DefaultSTAProcessor.h:158-223.
+// gridXYZ: npix (x, y, z) triples. value/factor: npix each.
+template<typename T>
+void delay_and_sum(const StaDesc<T>& d, const std::complex<T>* analytic, const T* real, unsigned L,
+		const T* gridXYZ, std::size_t npix, T* value, T* factor)
+{
+	const unsigned U = d.realPath ? 4U : d.upsampling;
+	const T invCT = (d.samplingFrequency * U) / d.propagationSpeed;
+	const T signalOffset = (d.samplingFrequency * U) * d.peakOffset / d.centerFrequency;
+	const std::size_t numSignals = static_cast<std::size_t>(d.numTx) * d.numRx;
+	T pcfFactor = 0;
+	if (d.cf == CF_PCF) {
+		const T sigma0 = kPi / std::sqrt(3.0);
+		pcfFactor = d.pcfGamma / sigma0;
+	}
+	parallel_for(npix, d.nthreads, [&](std::size_t b, std::size_t e) {
+		std::vector<T> txDelay(d.numTx), rxDelay(d.numRx);
+		std::vector<std::complex<T>> rxSum(d.numRx);
+		std::vector<T> rxSumReal(d.numRx);
+		std::vector<T> phi, phiAux;
+		for (std::size_t p = b; p < e; ++p) {
+			const T px = gridXYZ[3 * p], py = gridXYZ[3 * p + 1], pz = gridXYZ[3 * p + 2];
+			for (unsigned i = 0; i < d.numTx; ++i) {
+				txDelay[i] = distance3d_z0<T>(d.txXY[2 * i], d.txXY[2 * i + 1], px, py, pz) * invCT;
+			}
+			for (unsigned i = 0; i < d.numRx; ++i) {
+				rxDelay[i] = distance3d_z0<T>(d.rxXY[2 * i], d.rxXY[2 * i + 1], px, py, pz) * invCT;
+			}
+			T f = 1;
+			T v;
+			if (d.realPath) {
+				std::fill(rxSumReal.begin(), rxSumReal.end(), T(0));
+				for (unsigned tx = 0; tx < d.numTx; ++tx) {
+					const T txD = txDelay[tx];
+					for (unsigned rx = 0; rx < d.numRx; ++rx) {
+						const T delay = signalOffset + txD + rxDelay[rx];
+						const std::size_t idx = static_cast<std::size_t>(delay);
+						const T k = delay - idx;
+						if (idx + 1U < L) {
+							const T* s = real + (static_cast<std::size_t>(tx) * d.numRx + rx) * L + idx;
+							rxSumReal[rx] += (1 - k) * s[0] + k * s[1];
+						}
+					}
+				}
+				if (d.cf == CF_SCF) f = scf<T>(rxSumReal.data(), d.numRx, d.scfP);
+				T acc = 0;
+				for (unsigned rx = 0; rx < d.numRx; ++rx) acc += rxSumReal[rx];
+				v = acc;
+			} else if (d.cf == CF_NONE) {
+				std::complex<T> sum(0);
+				for (unsigned tx = 0; tx < d.numTx; ++tx) {
+					const T txD = txDelay[tx];
+					for (unsigned rx = 0; rx < d.numRx; ++rx) {
+						const T delay = signalOffset + txD + rxDelay[rx];
+						const std::size_t idx = static_cast<std::size_t>(delay);
+						const T k = delay - idx;
+						if (idx + 1U < L) {
+							const std::complex<T>* s = analytic + (static_cast<std::size_t>(tx) * d.numRx + rx) * L + idx;
+							sum += ((1 - k) * s[0] + k * s[1]) * d.rxApod[rx];
+						}
+					}
+				}
+				v = std::abs(sum);
+			} else {
+				std::fill(rxSum.begin(), rxSum.end(), std::complex<T>(0));
+				for (unsigned tx = 0; tx < d.numTx; ++tx) {
+					const T txD = txDelay[tx];
+					for (unsigned rx = 0; rx < d.numRx; ++rx) {
+						const T delay = signalOffset + txD + rxDelay[rx];
+						const std::size_t idx = static_cast<std::size_t>(delay);
+						const T k = delay - idx;
+						if (idx + 1U < L) {
+							const std::complex<T>* s = analytic + (static_cast<std::size_t>(tx) * d.numRx + rx) * L + idx;
+							rxSum[rx] += ((1 - k) * s[0] + k * s[1]) * d.rxApod[rx];
+						}
+					}
+				}
+				if (d.cf == CF_PCF) {
+					f = pcf<T>(rxSum.data(), d.numRx, pcfFactor, phi, phiAux);
+				} else if (d.cf == CF_SCF) {
+					// Analytic-path SCF: the reference's sign coherence factor
+					// applied to the real parts of the per-receiver sums.
+					for (unsigned rx = 0; rx < d.numRx; ++rx) rxSumReal[rx] = rxSum[rx].real();
+					f = scf<T>(rxSumReal.data(), d.numRx, d.scfP);
+				} else if (d.cf == CF_MF) {
+					f = mallart_fink_cf<T>(rxSum.data(), d.numRx);
+				}
+				std::complex<T> acc(0);
+				for (unsigned rx = 0; rx < d.numRx; ++rx) acc += rxSum[rx];
+				v = std::abs(acc);
+			}
+			value[p] = v * (T(1) / numSignals);
+			factor[p] = f;
+		}
+	});
+}
+
+}  // namespace orc
+
+#endif  // USGB_STA_ORACLE_HPP

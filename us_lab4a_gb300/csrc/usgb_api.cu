@@ -1,0 +1,642 @@
+// C-ABI implementation of libusgb: parameter checks (with the reference's
+// error semantics), FIR/FFT table construction, device buffers and the
+// per-frame launch sequence (signal preparation, then delay-and-sum).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/usgb.h"
+#include "usgb_common.cuh"
+#include "usgb_internal.h"
+
+namespace {
+
+thread_local std::string g_createError;
+
+constexpr double kPi = 3.14159265358979323846;
+
+struct Failure {
+	int code;
+	std::string msg;
+};
+
+#define USGB_FAIL(CODE, STREAM_EXPR)            \
+	do {                                        \
+		std::ostringstream os_;                 \
+		os_ << STREAM_EXPR;                     \
+		throw Failure{(CODE), os_.str()};       \
+	} while (0)
+
+#define USGB_CUDA(CALL)                                                                       \
+	do {                                                                                      \
+		const cudaError_t e_ = (CALL);                                                        \
+		if (e_ != cudaSuccess) {                                                              \
+			USGB_FAIL(e_ == cudaErrorMemoryAllocation ? USGB_ERR_OUT_OF_MEMORY : USGB_ERR_CUDA, \
+					#CALL << ": " << cudaGetErrorString(e_));                                 \
+		}                                                                                     \
+	} while (0)
+
+// FFTUtil::nextFastEvenSize (src/fft/FFTUtil.h:85-135).
+unsigned next_fast_even_size(unsigned n)
+{
+	if (n & 1U) ++n;
+	for (;;) {
+		unsigned m = n;
+		while ((m & 1U) == 0) m >>= 1;
+		while (m % 3 == 0) m /= 3;
+		while (m % 5 == 0) m /= 5;
+		if (m == 1) return n;
+		n += 2;
+	}
+}
+
+// Kaiser-windowed sinc of Interpolator::prepare (src/util/Interpolator.h:64-111,
+// src/util/KaiserWindow.h:45-93), evaluated in float with the same mixed
+// float/double expressions as Interpolator<float>.
+std::vector<float> interpolator_taps(unsigned U, float halfTransitionWidth)
+{
+	const double kaiserTolerance = 1.0e-4;
+	const float tol_dB = -20.0 * std::log10(kaiserTolerance);
+	float beta;
+	if (tol_dB > 50) {
+		beta = 0.1102 * (tol_dB - 8.7);
+	} else if (tol_dB > 21) {
+		const double k = tol_dB - 21.0;
+		beta = 0.5842 * std::pow(k, 0.4) + 0.07886 * k;
+	} else {
+		beta = 0.0;
+	}
+	const float finalTransitionWidth = (halfTransitionWidth * 2) / U;
+	const double sz = std::ceil((tol_dB - 7.95) / (2.285 * finalTransitionWidth * kPi) + 1.0);
+	const unsigned windowSize = static_cast<unsigned>(sz);
+	const float twoUp = 2 * U;
+	const unsigned n = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
+
+	std::vector<float> window(n);
+	const float c1 = 2 / static_cast<float>(n - 1U);
+	const float c2 = 1 / std::cyl_bessel_if(0.0f, beta);
+	for (unsigned i = 0; i < n; ++i) {
+		const float k = c1 * i - 1;
+		float x = 1 - k * k;
+		if (x < 0.0f) x = 0.0f;
+		window[i] = c2 * std::cyl_bessel_if(0.0f, beta * std::sqrt(x));
+	}
+	const float numPeriods = (n - 1U) / twoUp;
+	const double step = static_cast<double>(numPeriods - (-numPeriods)) / (n - 1U);
+	std::vector<float> taps(n);
+	for (unsigned i = 0; i < n; ++i) {
+		const float xi = (i == 0) ? -numPeriods : static_cast<float>(-numPeriods + i * step);
+		const double arg = kPi * xi;
+		const double s = (std::abs(arg) < 1.0e-5) ? 1.0 - arg * arg / 6.0 : std::sin(arg) / arg;
+		taps[i] = static_cast<float>(s);
+		taps[i] *= window[i];
+	}
+	return taps;
+}
+
+// The fixed 4x FIR of the real-RF path, from the recipe stated in
+// src/util/Interpolator4X.h:56-66 (kaiser(81, 5) .* sinc(linspace(-10, 10, 81))).
+std::vector<float> interpolator4x_taps()
+{
+	const unsigned n = 80;
+	const double beta = 5.0;
+	const double i0b = std::cyl_bessel_i(0.0, beta);
+	std::vector<float> h(n + 1);
+	for (unsigned i = 0; i <= n; ++i) {
+		const double r = 2.0 * i / n - 1.0;
+		double arg = 1.0 - r * r;
+		if (arg < 0.0) arg = 0.0;
+		const double w = std::cyl_bessel_i(0.0, beta * std::sqrt(arg)) / i0b;
+		const double xv = -10.0 + 20.0 * i / n;
+		const double s = (xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv);
+		h[i] = static_cast<float>(s * w);
+	}
+	return h;
+}
+
+}  // namespace
+
+struct usgb_ctx {
+	usgb_sta_params prm{};
+	std::vector<float> txXY, rxXY, apod;
+	unsigned numSignals = 0, L = 0, N = 0, M = 0, U = 1, deadZone = 0, tapsPerPhase = 1;
+	unsigned sigStride = 0;
+	size_t sigBytes = 0;
+	size_t elemBytes = 0;
+	float invCT = 0, signalOffset = 0, valueCoef = 0, pcfFactor = 0, scale = 1;
+	bool analytic = true;
+	std::vector<int> radices;
+
+	float* d_txXY = nullptr;
+	float* d_rxXY = nullptr;
+	float* d_apod = nullptr;
+	float* d_polyTaps = nullptr;
+	float2* d_tw = nullptr;
+	float2* d_cs = nullptr;
+	unsigned* d_perm = nullptr;
+	float* d_rf = nullptr;
+	void* d_sig = nullptr;
+	float* d_grid = nullptr;
+	float* d_value = nullptr;
+	float* d_factor = nullptr;
+	unsigned* d_err = nullptr;
+	size_t gridCap = 0;
+	unsigned ncols = 0, nrows = 0, npix = 0;
+	bool gridSet = false;
+
+	float* h_rf = nullptr;  // pinned staging of submitted RF
+	float* h_out = nullptr; // pinned staging of value/factor
+	size_t hOutCap = 0;
+	std::vector<unsigned char> submitted;
+
+	cudaStream_t stream = nullptr;
+	bool ownStream = false;
+	int dasVariant = 0;
+	unsigned tileRows = 8, tileCols = 32;
+	std::string err;
+
+	~usgb_ctx()
+	{
+		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_cs, d_perm, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
+		for (void* p : dev) if (p) cudaFree(p);
+		if (h_rf) cudaFreeHost(h_rf);
+		if (h_out) cudaFreeHost(h_out);
+		if (ownStream && stream) cudaStreamDestroy(stream);
+	}
+};
+
+namespace {
+
+void build_tables(usgb_ctx* c)
+{
+	// FIR.
+	std::vector<float> taps;
+	if (!c->analytic) {
+		taps = interpolator4x_taps();
+	} else if (c->U > 1) {
+		taps = interpolator_taps(c->U, 0.2f);
+	} else {
+		taps = {1.0f};
+	}
+	const unsigned T = static_cast<unsigned>(taps.size());
+	if (c->U > 1 && ((T - 1) % (2 * c->U) != 0)) USGB_FAIL(USGB_ERR_INVALID_STATE, "FIR length " << T << " is not 2*U*K + 1");
+	const unsigned K = (c->U > 1) ? (T - 1) / (2 * c->U) : 0;
+	c->tapsPerPhase = 2 * K + 1;
+	std::vector<float> poly(static_cast<size_t>(c->U) * c->tapsPerPhase, 0.f);
+	for (unsigned r = 0; r < c->U; ++r) {
+		for (unsigned t = 0; t < c->tapsPerPhase; ++t) {
+			const unsigned j = r + t * c->U;
+			poly[r * c->tapsPerPhase + t] = (j < T) ? taps[j] : 0.f;
+		}
+	}
+	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.size() * sizeof(float)));
+	USGB_CUDA(cudaMemcpy(c->d_polyTaps, poly.data(), poly.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+	if (!c->analytic) return;
+	// Hilbert FFT: N = max(nextFastEvenSize(L + 1024), 2048)
+	// (src/util/HilbertEnvelope.h:152), computed as an N/2-point complex FFT.
+	c->N = std::max(next_fast_even_size(c->L + 1024U), 2048U);
+	c->M = c->N / 2;
+	unsigned m = c->M;
+	c->radices.clear();
+	while (m % 4 == 0) { c->radices.push_back(4); m /= 4; }
+	while (m % 2 == 0) { c->radices.push_back(2); m /= 2; }
+	while (m % 3 == 0) { c->radices.push_back(3); m /= 3; }
+	while (m % 5 == 0) { c->radices.push_back(5); m /= 5; }
+	if (m != 1 || c->radices.size() > static_cast<size_t>(usgb::kMaxFFTStages)) {
+		USGB_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << c->M << " not supported");
+	}
+	const unsigned M = c->M;
+	std::vector<float2> tw(M), cs(M / 2 + 1);
+	for (unsigned i = 0; i < M; ++i) {
+		const double a = -2.0 * kPi * static_cast<double>(i) / M;
+		tw[i] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+	}
+	for (unsigned k = 0; k <= M / 2; ++k) {
+		const double a = kPi * static_cast<double>(k) / M;
+		cs[k] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+	}
+	// Digit-reversed position of bin k after the in-place DIF stages:
+	// k = k0 + r0 (k1 + r1 (k2 + ...)) sits at sum_s k_s * M / (r0 ... r_s).
+	std::vector<unsigned> perm(M);
+	for (unsigned k = 0; k < M; ++k) {
+		unsigned kk = k, pos = 0, span = M;
+		for (int r : c->radices) {
+			span /= static_cast<unsigned>(r);
+			pos += (kk % r) * span;
+			kk /= r;
+		}
+		perm[k] = pos;
+	}
+	USGB_CUDA(cudaMalloc(&c->d_tw, M * sizeof(float2)));
+	USGB_CUDA(cudaMalloc(&c->d_cs, (M / 2 + 1) * sizeof(float2)));
+	USGB_CUDA(cudaMalloc(&c->d_perm, M * sizeof(unsigned)));
+	USGB_CUDA(cudaMemcpy(c->d_tw, tw.data(), M * sizeof(float2), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_cs, cs.data(), (M / 2 + 1) * sizeof(float2), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_perm, perm.data(), M * sizeof(unsigned), cudaMemcpyHostToDevice));
+}
+
+void check_and_derive(usgb_ctx* c, const usgb_sta_params* p)
+{
+	if (!p) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null parameters");
+	if (p->num_tx == 0 || p->num_rx == 0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of elements is zero.");
+	if (p->num_tx > 1024 || p->num_rx > 1024) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "More than 1024 elements.");
+	if (p->num_samples == 0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of samples is zero.");
+	if (!p->tx_xy || !p->rx_xy) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Missing element positions.");
+	if (p->signal_path != USGB_PATH_ANALYTIC && p->signal_path != USGB_PATH_REAL) {
+		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid signal path: " << p->signal_path << '.');
+	}
+	c->analytic = p->signal_path == USGB_PATH_ANALYTIC;
+	if (c->analytic) {
+		if (p->upsampling == 0 || p->upsampling > 64) {
+			USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid upsampling factor: " << p->upsampling << ". Must be >= 1 and <= 64.");
+		}
+	} else if (p->upsampling != 4) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "The real-RF path upsamples by 4 (got " << p->upsampling << ").");
+	}
+	if (!(p->sampling_frequency > 0) || !(p->propagation_speed > 0) || !(p->center_frequency > 0)) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Sampling frequency, propagation speed and center frequency must be > 0.");
+	}
+	if (!(p->dead_zone_m >= 0)) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
+	if (p->coherence > USGB_CF_MF) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid coherence factor method: " << p->coherence << '.');
+	if (!c->analytic && p->coherence != USGB_CF_NONE && p->coherence != USGB_CF_SCF) {
+		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The real-RF path supports only the sign coherence factor.");
+	}
+	if (p->coherence == USGB_CF_PCF && !(p->pcf_gamma >= 0 && p->pcf_gamma <= 100)) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid phase_coherence_factor_gamma: " << p->pcf_gamma << '.');
+	}
+	if (p->coherence == USGB_CF_SCF && !(p->scf_p >= 0 && p->scf_p <= 100)) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid sign_coherence_factor_p: " << p->scf_p << '.');
+	}
+	if (p->storage > USGB_STORE_BF16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid storage type: " << p->storage << '.');
+
+	c->prm = *p;
+	c->prm.tx_xy = c->prm.rx_xy = c->prm.rx_apod = nullptr;
+	c->U = p->upsampling;
+	c->numSignals = p->num_tx * p->num_rx;
+	const unsigned long long L = static_cast<unsigned long long>(p->num_samples) * c->U;
+	if (L < 2) USGB_FAIL(USGB_ERR_INVALID_VALUE, "The signal length (" << L << ") must be >= 2.");
+	if (c->analytic && L > (1ULL << 20)) {
+		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of input samples (" << L << ") is greater than " << (1U << 20) << '.');
+	}
+	c->L = static_cast<unsigned>(L);
+	// deadZoneSamplesUp_ (src/user/processor/VectorialSTAProcessor.h:138).
+	const float upFs = c->U * p->sampling_frequency;
+	const double dz = upFs * 2.0 * p->dead_zone_m / p->propagation_speed;
+	if (!(dz < static_cast<double>(std::numeric_limits<unsigned>::max()))) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
+	}
+	c->deadZone = static_cast<unsigned>(dz);
+	if (c->deadZone >= c->L) {
+		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: deadZoneSamplesUp_ (" << c->deadZone
+				<< ") >= signalLength (" << c->L << ").");
+	}
+	// invCT and signalOffset_ (src/user/processor/VectorialSTAProcessor.h:147,241).
+	c->invCT = upFs / p->propagation_speed;
+	c->signalOffset = upFs * p->peak_offset / p->center_frequency;
+	c->valueCoef = 1.0f / static_cast<float>(c->numSignals);
+	const float sigma0 = static_cast<float>(kPi / std::sqrt(3.0));
+	c->pcfFactor = p->pcf_gamma / sigma0;
+	c->scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
+
+	c->txXY.assign(p->tx_xy, p->tx_xy + 2 * p->num_tx);
+	c->rxXY.assign(p->rx_xy, p->rx_xy + 2 * p->num_rx);
+	if (p->rx_apod && c->analytic) {
+		c->apod.assign(p->rx_apod, p->rx_apod + p->num_rx);
+	} else {
+		c->apod.assign(p->num_rx, 1.0f);  // the real-RF path has no apodization
+	}
+	c->elemBytes = (c->analytic ? 2 : 1) * (p->storage == USGB_STORE_F32 ? 4 : 2);
+	c->sigStride = (c->L + 7U) & ~7U;
+	c->sigBytes = static_cast<size_t>(c->numSignals) * c->sigStride * c->elemBytes + 256;
+}
+
+void alloc_frame(usgb_ctx* c)
+{
+	const usgb_sta_params& p = c->prm;
+	USGB_CUDA(cudaMalloc(&c->d_txXY, c->txXY.size() * sizeof(float)));
+	USGB_CUDA(cudaMalloc(&c->d_rxXY, c->rxXY.size() * sizeof(float)));
+	USGB_CUDA(cudaMalloc(&c->d_apod, c->apod.size() * sizeof(float)));
+	USGB_CUDA(cudaMemcpy(c->d_txXY, c->txXY.data(), c->txXY.size() * sizeof(float), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_rxXY, c->rxXY.data(), c->rxXY.size() * sizeof(float), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_apod, c->apod.data(), c->apod.size() * sizeof(float), cudaMemcpyHostToDevice));
+	const size_t rfBytes = static_cast<size_t>(c->numSignals) * p.num_samples * sizeof(float);
+	USGB_CUDA(cudaMalloc(&c->d_rf, rfBytes));
+	USGB_CUDA(cudaMalloc(&c->d_sig, c->sigBytes));
+	USGB_CUDA(cudaMemset(c->d_sig, 0, c->sigBytes));
+	USGB_CUDA(cudaMalloc(&c->d_err, sizeof(unsigned)));
+	USGB_CUDA(cudaMemset(c->d_err, 0, sizeof(unsigned)));
+	USGB_CUDA(cudaMallocHost(&c->h_rf, rfBytes));
+	c->submitted.assign(p.num_tx, 0);
+}
+
+usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
+{
+	usgb::PrepParams pp{};
+	pp.rf = d_rf;
+	pp.out = d_sig;
+	pp.outStride = c->sigStride;
+	pp.numSignals = c->numSignals;
+	pp.ns = c->prm.num_samples;
+	pp.U = c->U;
+	pp.L = c->L;
+	pp.tapsPerPhase = c->tapsPerPhase;
+	pp.polyTaps = c->d_polyTaps;
+	pp.deadZone = c->deadZone;
+	pp.outScale = c->scale;
+	pp.M = c->M;
+	pp.numStages = static_cast<int>(c->radices.size());
+	for (size_t i = 0; i < c->radices.size(); ++i) pp.radix[i] = c->radices[i];
+	pp.tw = c->d_tw;
+	pp.cs = c->d_cs;
+	pp.perm = c->d_perm;
+	return pp;
+}
+
+usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value, float* d_factor)
+{
+	usgb::DasParams dp{};
+	dp.sig = d_sig;
+	dp.sigStride = c->sigStride;
+	dp.L = c->L;
+	dp.numTx = c->prm.num_tx;
+	dp.numRx = c->prm.num_rx;
+	dp.txXY = c->d_txXY;
+	dp.rxXY = c->d_rxXY;
+	dp.apod = c->d_apod;
+	dp.grid = c->d_grid;
+	dp.npix = c->npix;
+	dp.ncols = c->ncols;
+	dp.nrows = c->nrows;
+	dp.invCT = c->invCT;
+	dp.signalOffset = c->signalOffset;
+	dp.valueCoef = c->valueCoef;
+	dp.invScale = 1.0f / c->scale;
+	dp.pcfFactor = c->pcfFactor;
+	dp.scfP = c->prm.scf_p;
+	dp.value = d_value;
+	dp.factor = d_factor;
+	dp.errWord = c->d_err;
+	dp.tileRows = c->tileRows;
+	dp.tileCols = c->tileCols;
+	return dp;
+}
+
+void ensure_grid(usgb_ctx* c, uint32_t ncols, uint32_t nrows)
+{
+	if (ncols == 0) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Zero columns in the grid.");
+	if (nrows == 0) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Zero rows in the grid.");
+	const size_t npix = static_cast<size_t>(ncols) * nrows;
+	if (npix > (1ULL << 31)) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Grid too large.");
+	if (npix > c->gridCap) {
+		if (c->d_grid) { cudaFree(c->d_grid); c->d_grid = nullptr; }
+		if (c->d_value) { cudaFree(c->d_value); c->d_value = nullptr; }
+		if (c->d_factor) { cudaFree(c->d_factor); c->d_factor = nullptr; }
+		c->gridCap = 0;
+		USGB_CUDA(cudaMalloc(&c->d_grid, npix * 3 * sizeof(float)));
+		USGB_CUDA(cudaMalloc(&c->d_value, npix * sizeof(float)));
+		USGB_CUDA(cudaMalloc(&c->d_factor, npix * sizeof(float)));
+		c->gridCap = npix;
+	}
+	c->ncols = ncols;
+	c->nrows = nrows;
+	c->npix = static_cast<unsigned>(npix);
+}
+
+void check_prep_fits(const usgb_ctx* c)
+{
+	int dev = 0, maxSmem = 0;
+	USGB_CUDA(cudaGetDevice(&dev));
+	USGB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+	const usgb::PrepParams pp = prep_params(c, nullptr, nullptr);
+	const size_t need = usgb::prep_smem_bytes(pp, c->analytic);
+	if (need > static_cast<size_t>(maxSmem)) {
+		USGB_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation: needs " << need
+				<< " bytes of shared memory, the device offers " << maxSmem << " (signal length " << c->L << ").");
+	}
+	const size_t dasSmem = static_cast<size_t>(c->prm.num_tx) * 128 * sizeof(float);
+	if (dasSmem > static_cast<size_t>(maxSmem)) {
+		USGB_FAIL(USGB_ERR_UNSUPPORTED, "Too many transmit elements for the delay table: " << c->prm.num_tx << '.');
+	}
+}
+
+void run_frame(usgb_ctx* c, const float* d_rf, float* d_value, float* d_factor)
+{
+	if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+	USGB_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+	const usgb::PrepParams pp = prep_params(c, d_rf, c->d_sig);
+	USGB_CUDA(usgb::launch_prep(pp, static_cast<int>(c->prm.storage), c->analytic, c->stream));
+	const usgb::DasParams dp = das_params(c, c->d_sig, d_value, d_factor);
+	USGB_CUDA(usgb::launch_das(dp, static_cast<int>(c->prm.storage), static_cast<int>(c->prm.coherence),
+			c->analytic, c->dasVariant, c->stream));
+}
+
+template<typename F>
+int guarded(usgb_ctx* c, F&& f)
+{
+	if (!c) return USGB_ERR_INVALID_PARAMETER;
+	try {
+		f();
+		return USGB_OK;
+	} catch (const Failure& e) {
+		c->err = e.msg;
+		return e.code;
+	} catch (const std::bad_alloc&) {
+		c->err = "host allocation failed";
+		return USGB_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception& e) {
+		c->err = e.what();
+		return USGB_ERR_INVALID_STATE;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* usgb_version(void) { return "usgb 0.1 (sm_103a)"; }
+
+int usgb_create(const usgb_sta_params* params, usgb_ctx** out)
+{
+	if (!out) {
+		g_createError = "null output pointer";
+		return USGB_ERR_INVALID_PARAMETER;
+	}
+	*out = nullptr;
+	usgb_ctx* c = nullptr;
+	try {
+		c = new usgb_ctx();
+		check_and_derive(c, params);
+		build_tables(c);
+		check_prep_fits(c);
+		alloc_frame(c);
+		USGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+		c->ownStream = true;
+		*out = c;
+		return USGB_OK;
+	} catch (const Failure& e) {
+		g_createError = e.msg;
+		delete c;
+		return e.code;
+	} catch (const std::bad_alloc&) {
+		g_createError = "host allocation failed";
+		delete c;
+		return USGB_ERR_OUT_OF_MEMORY;
+	}
+}
+
+void usgb_destroy(usgb_ctx* c)
+{
+	if (!c) return;
+	if (c->stream) cudaStreamSynchronize(c->stream);
+	delete c;
+}
+
+const char* usgb_last_error(const usgb_ctx* c)
+{
+	return c ? c->err.c_str() : g_createError.c_str();
+}
+
+int usgb_set_stream(usgb_ctx* c, void* s)
+{
+	return guarded(c, [&] {
+		if (c->ownStream && c->stream) {
+			USGB_CUDA(cudaStreamSynchronize(c->stream));
+			USGB_CUDA(cudaStreamDestroy(c->stream));
+		}
+		c->ownStream = false;
+		c->stream = static_cast<cudaStream_t>(s);
+	});
+}
+
+int usgb_set_grid(usgb_ctx* c, const float* xyz, uint32_t ncols, uint32_t nrows)
+{
+	return guarded(c, [&] {
+		if (!xyz) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null grid");
+		ensure_grid(c, ncols, nrows);
+		USGB_CUDA(cudaMemcpyAsync(c->d_grid, xyz, static_cast<size_t>(c->npix) * 3 * sizeof(float),
+				cudaMemcpyHostToDevice, c->stream));
+		USGB_CUDA(cudaStreamSynchronize(c->stream));
+		c->gridSet = true;
+	});
+}
+
+int usgb_set_grid_device(usgb_ctx* c, const float* d_xyz, uint32_t ncols, uint32_t nrows)
+{
+	return guarded(c, [&] {
+		if (!d_xyz) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null grid");
+		ensure_grid(c, ncols, nrows);
+		USGB_CUDA(cudaMemcpyAsync(c->d_grid, d_xyz, static_cast<size_t>(c->npix) * 3 * sizeof(float),
+				cudaMemcpyDeviceToDevice, c->stream));
+		c->gridSet = true;
+	});
+}
+
+int usgb_submit_rf(usgb_ctx* c, uint32_t tx, const float* rf, uint32_t num_rx, uint32_t num_samples)
+{
+	return guarded(c, [&] {
+		if (!rf) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null RF");
+		if (tx >= c->prm.num_tx) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid tx index: " << tx << '.');
+		if (num_rx != c->prm.num_rx || num_samples != c->prm.num_samples) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Data size mismatch.");
+		}
+		const size_t n = static_cast<size_t>(num_rx) * num_samples;
+		std::memcpy(c->h_rf + static_cast<size_t>(tx) * n, rf, n * sizeof(float));
+		c->submitted[tx] = 1;
+	});
+}
+
+int usgb_process(usgb_ctx* c, float* value, float* factor)
+{
+	return guarded(c, [&] {
+		if (!value) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null value output");
+		for (unsigned t = 0; t < c->prm.num_tx; ++t) {
+			if (!c->submitted[t]) USGB_FAIL(USGB_ERR_INVALID_STATE, "RF of tx " << t << " has not been submitted.");
+		}
+		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+		const size_t rfBytes = static_cast<size_t>(c->numSignals) * c->prm.num_samples * sizeof(float);
+		if (c->hOutCap < 2 * static_cast<size_t>(c->npix)) {
+			if (c->h_out) { cudaFreeHost(c->h_out); c->h_out = nullptr; c->hOutCap = 0; }
+			USGB_CUDA(cudaMallocHost(&c->h_out, 2 * static_cast<size_t>(c->npix) * sizeof(float)));
+			c->hOutCap = 2 * static_cast<size_t>(c->npix);
+		}
+		USGB_CUDA(cudaMemcpyAsync(c->d_rf, c->h_rf, rfBytes, cudaMemcpyHostToDevice, c->stream));
+		run_frame(c, c->d_rf, c->d_value, c->d_factor);
+		USGB_CUDA(cudaMemcpyAsync(c->h_out, c->d_value, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+		USGB_CUDA(cudaMemcpyAsync(c->h_out + c->npix, c->d_factor, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+		USGB_CUDA(cudaStreamSynchronize(c->stream));
+		unsigned errWord = 0;
+		USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+		if (errWord) USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+		std::memcpy(value, c->h_out, c->npix * sizeof(float));
+		if (factor) std::memcpy(factor, c->h_out + c->npix, c->npix * sizeof(float));
+	});
+}
+
+int usgb_process_device(usgb_ctx* c, const float* d_rf, float* d_value, float* d_factor)
+{
+	return guarded(c, [&] {
+		if (!d_rf || !d_value || !d_factor) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+		run_frame(c, d_rf, d_value, d_factor);
+	});
+}
+
+int usgb_prepare_signals_device(usgb_ctx* c, const float* d_rf, void* d_signals)
+{
+	return guarded(c, [&] {
+		if (!d_rf || !d_signals) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+		const usgb::PrepParams pp = prep_params(c, d_rf, d_signals);
+		USGB_CUDA(usgb::launch_prep(pp, static_cast<int>(c->prm.storage), c->analytic, c->stream));
+	});
+}
+
+int usgb_delay_and_sum_device(usgb_ctx* c, const void* d_signals, float* d_value, float* d_factor)
+{
+	return guarded(c, [&] {
+		if (!d_signals || !d_value || !d_factor) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+		USGB_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+		const usgb::DasParams dp = das_params(c, d_signals, d_value, d_factor);
+		USGB_CUDA(usgb::launch_das(dp, static_cast<int>(c->prm.storage), static_cast<int>(c->prm.coherence),
+				c->analytic, c->dasVariant, c->stream));
+	});
+}
+
+int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_size, uint32_t* signal_stride, size_t* signal_bytes)
+{
+	if (!c) return USGB_ERR_INVALID_PARAMETER;
+	if (signal_length) *signal_length = c->L;
+	if (fft_size) *fft_size = c->N;
+	if (signal_stride) *signal_stride = c->sigStride;
+	if (signal_bytes) *signal_bytes = c->sigBytes;
+	return USGB_OK;
+}
+
+int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t tile_cols)
+{
+	return guarded(c, [&] {
+		if (variant != 0) USGB_FAIL(USGB_ERR_UNSUPPORTED, "delay-and-sum variant " << variant << " is not available");
+		c->dasVariant = variant;
+		if (tile_rows) c->tileRows = tile_rows;
+		if (tile_cols) c->tileCols = tile_cols;
+	});
+}
+
+int usgb_synchronize(usgb_ctx* c)
+{
+	return guarded(c, [&] {
+		USGB_CUDA(cudaStreamSynchronize(c->stream));
+		unsigned errWord = 0;
+		USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+		if (errWord) USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+	});
+}
+
+}  // extern "C"

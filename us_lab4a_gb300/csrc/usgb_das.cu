@@ -1,0 +1,205 @@
+// Delay-and-sum kernels: per grid point, tx/rx delays, linearly interpolated
+// gather over every tx x rx pair, and the coherence factor over the
+// per-receiver sums.
+//
+// Reference: src/user/processor/VectorialSTAProcessor.h:237-338 (analytic,
+// with the 3D delays of src/user/processor/Vectorial3DSTAProcessor.h:208-242)
+// and src/user/processor/DefaultSTAProcessor.h:158-223 (real RF, SCF);
+// coherence factors src/util/CoherenceFactor.h:217-296.
+//
+// Delays are rounded exactly like the reference's float arithmetic
+// (no FMA contraction, IEEE sqrt): delay = (signalOffset + txDelay) + rxDelay,
+// with txDelay = dist * invCT. The sample index is floor(delay) and the
+// fraction delay - floor(delay) is exact, so every gather reads the same two
+// samples with the same weights as the reference; only the order of the
+// floating-point sums differs. A gather is skipped unless 0 <= idx and
+// idx + 1 < L (src/user/processor/VectorialSTAProcessor.h:277).
+#include <cuda_runtime.h>
+
+#include "usgb_common.cuh"
+#include "usgb_internal.h"
+
+namespace usgb {
+
+namespace {
+
+constexpr int kDirectThreads = 128;
+
+// floor(d) and d - floor(d) for d >= -1 (and d < 2^23): one add with
+// rounding toward -inf against 2^23 puts floor(d) in the mantissa. For
+// -1 <= d < 0 the returned index is negative (-1 or -2), so the unsigned
+// range test below rejects it.
+__device__ __forceinline__ int split_delay(float d, float& frac)
+{
+	const float t = __fadd_rd(d, 8388608.0f);
+	frac = d - (t - 8388608.0f);
+	return __float_as_int(t) - 0x4B000000;
+}
+
+// Per-pixel coherence-factor state over the receivers.
+template<int CF> struct CFState {
+	__device__ void add(float2) {}
+	__device__ float result(unsigned, const DasParams&, float2) const { return 1.0f; }
+};
+
+// PCF (src/util/CoherenceFactor.h:267-286): population standard deviation of
+// the phases phi and of phi -+ pi, accumulated with Welford's update.
+template<> struct CFState<CF_PCF> {
+	unsigned n = 0;
+	float m1 = 0.f, s1 = 0.f, m2 = 0.f, s2 = 0.f;
+	__device__ void add(float2 v)
+	{
+		const float phi = atan2f(v.y, v.x);
+		const float pi = 3.14159265358979323846f;
+		const float aux = phi + ((phi < 0.f) ? pi : -pi);
+		++n;
+		const float inv = 1.0f / static_cast<float>(n);
+		float d = phi - m1;
+		m1 += d * inv;
+		s1 += d * (phi - m1);
+		d = aux - m2;
+		m2 += d * inv;
+		s2 += d * (aux - m2);
+	}
+	__device__ float result(unsigned N, const DasParams& p, float2) const
+	{
+		const float sd1 = sqrtf(s1 / static_cast<float>(N));
+		const float sd2 = sqrtf(s2 / static_cast<float>(N));
+		return fmaxf(0.f, 1.f - p.pcfFactor * fminf(sd1, sd2));
+	}
+};
+
+// SCF (src/util/CoherenceFactor.h:217-236) on the real parts, sign(0) = +1.
+template<> struct CFState<CF_SCF> {
+	int signSum = 0;
+	__device__ void add(float2 v) { signSum += (v.x >= 0.f) ? 1 : -1; }
+	__device__ float result(unsigned N, const DasParams& p, float2) const
+	{
+		const float k = static_cast<float>(signSum) / static_cast<float>(N);
+		const float m = 1.f - sqrtf(1.f - k * k);
+		return powf(fabsf(m), p.scfP);
+	}
+};
+
+// Mallart-Fink CF: |sum s|^2 / (N sum |s|^2) (not in the reference).
+template<> struct CFState<CF_MF> {
+	float energy = 0.f;
+	__device__ void add(float2 v) { energy = fmaf(v.x, v.x, fmaf(v.y, v.y, energy)); }
+	__device__ float result(unsigned N, const DasParams&, float2 total) const
+	{
+		if (energy == 0.f) return 0.f;
+		return (total.x * total.x + total.y * total.y) / (static_cast<float>(N) * energy);
+	}
+};
+
+// Plain form: one thread per grid point, gathers straight from global
+// memory. Receiver-major loop so that each receiver's sum over transmitters
+// is complete before it enters the coherence factor.
+template<int S, int CF, bool ANALYTIC>
+__global__ void __launch_bounds__(kDirectThreads)
+das_direct_kernel(DasParams p)
+{
+	extern __shared__ float txd[];  // [numTx][blockDim.x]
+	const unsigned tid = threadIdx.x;
+	const unsigned pix = blockIdx.x * blockDim.x + tid;
+	const bool active = pix < p.npix;
+	float px = 0.f, py = 0.f, pz = 0.f;
+	if (active) {
+		px = p.grid[3 * pix];
+		py = p.grid[3 * pix + 1];
+		pz = p.grid[3 * pix + 2];
+	}
+	for (unsigned t = 0; t < p.numTx; ++t) {
+		const float dist = distance3d_z0(__ldg(&p.txXY[2 * t]), __ldg(&p.txXY[2 * t + 1]), px, py, pz);
+		txd[t * blockDim.x + tid] = __fadd_rn(p.signalOffset, __fmul_rn(dist, p.invCT));
+	}
+	if (!active) return;
+
+	const unsigned lastIdx = p.L - 2;
+	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
+	float2 total = make_float2(0.f, 0.f);
+	CFState<CF> cf;
+	for (unsigned r = 0; r < p.numRx; ++r) {
+		const float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
+		float2 acc = make_float2(0.f, 0.f);
+		if (ANALYTIC) {
+			using CT = typename Complex<S>::T;
+			const CT* base = reinterpret_cast<const CT*>(p.sig) + static_cast<size_t>(r) * p.sigStride;
+			for (unsigned t = 0; t < p.numTx; ++t) {
+				const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
+				float k;
+				const int i = split_delay(d, k);
+				if (static_cast<unsigned>(i) <= lastIdx) {
+					const CT* s = base + t * txStride + i;
+					const float2 s0 = Complex<S>::load(s);
+					const float2 s1 = Complex<S>::load(s + 1);
+					const float w0 = 1.0f - k;
+					acc.x = fmaf(w0, s0.x, acc.x);
+					acc.y = fmaf(w0, s0.y, acc.y);
+					acc.x = fmaf(k, s1.x, acc.x);
+					acc.y = fmaf(k, s1.y, acc.y);
+				}
+			}
+		} else {
+			using RT = typename Real<S>::T;
+			const RT* base = reinterpret_cast<const RT*>(p.sig) + static_cast<size_t>(r) * p.sigStride;
+			for (unsigned t = 0; t < p.numTx; ++t) {
+				const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
+				float k;
+				const int i = split_delay(d, k);
+				if (static_cast<unsigned>(i) <= lastIdx) {
+					const RT* s = base + t * txStride + i;
+					acc.x = fmaf(1.0f - k, Real<S>::load(s), acc.x);
+					acc.x = fmaf(k, Real<S>::load(s + 1), acc.x);
+				}
+			}
+		}
+		const float w = __ldg(&p.apod[r]) * p.invScale;
+		const float2 rs = make_float2(acc.x * w, acc.y * w);
+		total.x += rs.x;
+		total.y += rs.y;
+		cf.add(rs);
+	}
+	const float v = ANALYTIC ? sqrtf(total.x * total.x + total.y * total.y) : total.x;
+	p.value[pix] = v * p.valueCoef;
+	p.factor[pix] = cf.result(p.numRx, p, total);
+}
+
+template<int S, int CF, bool ANALYTIC>
+cudaError_t launch_direct(const DasParams& p, cudaStream_t stream)
+{
+	const size_t smem = static_cast<size_t>(p.numTx) * kDirectThreads * sizeof(float);
+	cudaError_t e = cudaFuncSetAttribute(das_direct_kernel<S, CF, ANALYTIC>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	const unsigned blocks = (p.npix + kDirectThreads - 1) / kDirectThreads;
+	das_direct_kernel<S, CF, ANALYTIC><<<blocks, kDirectThreads, smem, stream>>>(p);
+	return cudaGetLastError();
+}
+
+template<int S>
+cudaError_t dispatch_cf(const DasParams& p, int cf, bool analytic, cudaStream_t stream)
+{
+	if (!analytic) {
+		return (cf == CF_SCF) ? launch_direct<S, CF_SCF, false>(p, stream) : launch_direct<S, CF_NONE, false>(p, stream);
+	}
+	switch (cf) {
+	case CF_PCF: return launch_direct<S, CF_PCF, true>(p, stream);
+	case CF_SCF: return launch_direct<S, CF_SCF, true>(p, stream);
+	case CF_MF: return launch_direct<S, CF_MF, true>(p, stream);
+	default: return launch_direct<S, CF_NONE, true>(p, stream);
+	}
+}
+
+}  // namespace
+
+cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int /*variant*/, cudaStream_t stream)
+{
+	switch (storage) {
+	case STORE_F16: return dispatch_cf<STORE_F16>(p, cf, analytic, stream);
+	case STORE_BF16: return dispatch_cf<STORE_BF16>(p, cf, analytic, stream);
+	default: return dispatch_cf<STORE_F32>(p, cf, analytic, stream);
+	}
+}
+
+}  // namespace usgb

@@ -1,0 +1,64 @@
+// Internal host/device interfaces of libusgb (not part of the C ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace usgb {
+
+constexpr int kPrepThreads = 512;
+constexpr int kMaxFFTStages = 24;
+
+// One launch of the signal-preparation kernel over `numSignals` A-scans.
+struct PrepParams {
+	const float* rf;             // numSignals x ns, float32
+	void* out;                   // numSignals x outStride samples (storage type)
+	size_t outStride;            // samples per A-scan in `out` (>= L)
+	unsigned numSignals;
+	unsigned ns;                 // samples per A-scan at fs
+	unsigned U;                  // upsampling factor (1: none)
+	unsigned L;                  // ns * U
+	unsigned tapsPerPhase;       // 2K + 1 (1 when U == 1)
+	const float* polyTaps;       // U x tapsPerPhase, polyTaps[r][t] = h[r + tU]
+	unsigned deadZone;           // first sample of the DC mean
+	float outScale;              // applied before storage (1 for FP32)
+	// Hilbert FFT (analytic path): M = N/2 complex points.
+	unsigned M;
+	int numStages;
+	int radix[kMaxFFTStages];    // DIF order
+	const float2* tw;            // M entries, exp(-2 pi i m / M)
+	const float2* cs;            // M/2 + 1 entries, (cos, sin)(pi k / M)
+	const unsigned* perm;        // M entries, digit-reversed position of bin k
+};
+
+size_t prep_smem_bytes(const PrepParams& p, bool analytic);
+cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream);
+
+// One launch of the delay-and-sum kernel over the grid points of one frame.
+struct DasParams {
+	const void* sig;             // numTx x numRx x sigStride samples (storage type)
+	size_t sigStride;            // samples per A-scan
+	unsigned L;                  // valid samples per A-scan
+	unsigned numTx, numRx;
+	const float* txXY;           // numTx (x, y)
+	const float* rxXY;           // numRx (x, y)
+	const float* apod;           // numRx
+	const float* grid;           // npix (x, y, z)
+	unsigned npix, ncols, nrows;
+	float invCT;                 // fs * U / c
+	float signalOffset;          // fs * U * peakOffset / fc
+	float valueCoef;             // 1 / (numTx * numRx)
+	float invScale;              // 1 / storage scale
+	float pcfFactor;             // gamma / sigma0
+	float scfP;
+	float* value;
+	float* factor;
+	unsigned* errWord;
+	// Tiling of the staged kernel (rows x cols of pixels per block).
+	unsigned tileRows, tileCols;
+};
+
+cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
+
+}  // namespace usgb

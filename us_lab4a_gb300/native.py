@@ -1,0 +1,92 @@
+"""ctypes binding of libusgb.so (the C ABI declared in include/usgb.h).
+
+The library is built in-tree (``us_lab4a_gb300/build.py``). There is no CPU
+fallback: if the library is missing or fails to load, every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import errors
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libusgb.so")
+
+USGB_PATH_ANALYTIC, USGB_PATH_REAL = 0, 1
+USGB_CF_NONE, USGB_CF_PCF, USGB_CF_SCF, USGB_CF_MF = 0, 1, 2, 3
+USGB_STORE_F32, USGB_STORE_F16, USGB_STORE_BF16 = 0, 1, 2
+
+_FP = C.POINTER(C.c_float)
+
+
+class StaParams(C.Structure):
+    """Mirror of ``usgb_sta_params``."""
+    _fields_ = [
+        ("num_tx", C.c_uint32), ("num_rx", C.c_uint32), ("num_samples", C.c_uint32),
+        ("upsampling", C.c_uint32), ("signal_path", C.c_uint32),
+        ("sampling_frequency", C.c_float), ("propagation_speed", C.c_float),
+        ("center_frequency", C.c_float), ("peak_offset", C.c_float), ("dead_zone_m", C.c_float),
+        ("tx_xy", _FP), ("rx_xy", _FP), ("rx_apod", _FP),
+        ("coherence", C.c_uint32), ("pcf_gamma", C.c_float), ("scf_p", C.c_float),
+        ("storage", C.c_uint32), ("storage_scale", C.c_float),
+    ]
+
+
+# Every symbol include/usgb.h declares, with (restype, argtypes).
+SIGNATURES = {
+    "usgb_create": (C.c_int, [C.POINTER(StaParams), C.POINTER(C.c_void_p)]),
+    "usgb_destroy": (None, [C.c_void_p]),
+    "usgb_last_error": (C.c_char_p, [C.c_void_p]),
+    "usgb_set_grid": (C.c_int, [C.c_void_p, _FP, C.c_uint32, C.c_uint32]),
+    "usgb_submit_rf": (C.c_int, [C.c_void_p, C.c_uint32, _FP, C.c_uint32, C.c_uint32]),
+    "usgb_process": (C.c_int, [C.c_void_p, _FP, _FP]),
+    "usgb_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "usgb_set_grid_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
+    "usgb_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "usgb_prepare_signals_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "usgb_delay_and_sum_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "usgb_signal_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_uint32), C.POINTER(C.c_size_t)]),
+    "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32]),
+    "usgb_synchronize": (C.c_int, [C.c_void_p]),
+    "usgb_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load libusgb.so (building it first if it is absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise errors.NativeLibraryError(f"{LIB_PATH} is missing; run us_lab4a_gb300.build.build()")
+        from .build import build
+        build()
+    try:
+        lib = C.CDLL(LIB_PATH)
+    except OSError as e:
+        raise errors.NativeLibraryError(f"cannot load {LIB_PATH}: {e}") from e
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int, ctx=None) -> None:
+    """Raise the exception that matches a usgb_status."""
+    if rc == 0:
+        return
+    lib = load()
+    msg = lib.usgb_last_error(ctx).decode(errors="replace")
+    raise errors.from_status(rc, msg)
+
+
+def fptr(addr: int):
+    return C.cast(C.c_void_p(addr), _FP)
