@@ -1,0 +1,356 @@
+"""Benchmark: STA/TFM frames/s on GB300 (one JSON line on rank 0).
+
+A step is one frame through the whole hot path: signal preparation
+(upsampling, DC removal, Hilbert analytic signal) of every A-scan, then the
+delay-and-sum with the coherence factor over every grid point.
+
+Default workload (--workload cf2d): 64-element linear array, 4096 samples at
+40 MHz, 8x upsampling, Blackman apodization, PCF, 512 x 512 grid, FP32; seeded
+synthetic RF (32 point scatterers + 20 000 speckle scatterers).
+
+  value  frames/s with the RF already resident in HBM (device entry point);
+         4 RF buffers (4 x 67 MB) rotate between steps and every step writes
+         and reads the 1.07 GB analytic tensor, so the inputs exceed L2.
+  e2e    the same metric through the host entry points (usgb_submit_rf +
+         usgb_process): RF copied host->device and the image device->host
+         inside every step.
+  --impl reference  times the CPU oracle (the C++ restatement of the
+         reference processor) on the host cores instead.
+Multi-GPU (torchrun): replicas, one frame stream per rank (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "STA/TFM frames/s + p50/p99 latency, mixed-precision vs FP32 at ≤-60 dB error"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def _workload(name: str, storage: str):
+    from us_lab4a_gb300 import workloads
+    if name == "cf2d":
+        fr = workloads.cf2d()
+        desc = "cf2d: 64-element linear array, 4096 samples @40 MHz, 8x upsampling, Blackman, PCF, 512x512 grid"
+    elif name == "plain2d":
+        fr = workloads.plain2d()
+        desc = "plain2d: 32 elements, 2048 samples @40 MHz, 4x, rectangular apodization, no CF, 128x256 grid"
+    elif name == "matrix3d":
+        fr = workloads.matrix3d()
+        desc = "matrix3d: 16x16 matrix array, 1024 samples @24 MHz, 4x, PCF, 64x64x128 voxels"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    fr = workloads.with_storage(fr, storage)
+    return fr, desc
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._proc = None
+        self._thread = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._proc = None
+            return
+
+        def reader():
+            for line in self._proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+        self._thread = threading.Thread(target=reader, daemon=True)
+        self._thread.start()
+
+    def stop(self):
+        if self._proc is None:
+            return None
+        self._proc.terminate()
+        try:
+            self._proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self._proc.kill()
+        if self._thread:
+            self._thread.join(timeout=2)
+        rows = [r for r in self.samples if len(r) >= 7]
+        if not rows:
+            return None
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(frame, threads: int, a_sample: int = 128, p_sample: int = 8192, dtype=np.float32):
+    """Oracle (the C++ restatement of the reference processor) on a bounded
+    sample of the frame: preparation of `a_sample` A-scans and delay-and-sum
+    of `p_sample` grid points, scaled to one frame."""
+    import oracle
+    from us_lab4a_gb300 import synth
+    spec = frame.spec
+    rng = np.random.default_rng(7)
+    # Preparation: a_sample A-scans of one transmit event, synthesized here.
+    tx = int(rng.integers(spec.num_tx))
+    rx_idx = np.sort(rng.choice(spec.num_rx, min(a_sample, spec.num_rx), replace=False))
+    reps = max(1, a_sample // len(rx_idx))
+    rf_rows = synth.synth_rf_numpy(spec.tx_xy[tx:tx + 1], spec.rx_xy[rx_idx], frame.scatterers,
+                                   spec.sampling_frequency, spec.propagation_speed, spec.center_frequency,
+                                   spec.num_samples, np.random.default_rng(frame.seed + 1))
+    cf = {"none": 0, "pcf": 1, "scf": 2, "mf": 3}[spec.coherence]
+    sub = oracle.OracleSpec(tx_xy=spec.tx_xy[tx:tx + 1], rx_xy=spec.rx_xy[rx_idx], num_samples=spec.num_samples,
+                            upsampling=spec.upsampling, sampling_frequency=spec.sampling_frequency,
+                            propagation_speed=spec.propagation_speed, center_frequency=spec.center_frequency,
+                            rx_apod=spec.rx_apod[rx_idx], cf=0, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.process(sub, rf_rows, None, dtype=dtype, want_signals=False)
+    t_prep = (time.perf_counter() - t0) / (reps * len(rx_idx))
+    # Delay-and-sum: p_sample grid points on a tensor of the frame's shape
+    # (its cost does not depend on the sample values).
+    L = spec.num_samples * spec.upsampling
+    full = oracle.OracleSpec(tx_xy=spec.tx_xy, rx_xy=spec.rx_xy, num_samples=spec.num_samples,
+                             upsampling=spec.upsampling, sampling_frequency=spec.sampling_frequency,
+                             propagation_speed=spec.propagation_speed, center_frequency=spec.center_frequency,
+                             rx_apod=spec.rx_apod, cf=cf, nthreads=threads)
+    tensor = np.zeros((spec.num_tx, spec.num_rx, L), np.complex64)
+    idx = rng.choice(frame.npix, min(p_sample, frame.npix), replace=False)
+    pts = frame.grid_xyz.reshape(-1, 3)[idx][:, None, :]
+    t0 = time.perf_counter()
+    oracle.das(full, tensor, pts, dtype=dtype)
+    t_das = (time.perf_counter() - t0) / len(idx)
+    n_sig = spec.num_tx * spec.num_rx
+    sec_per_frame = t_prep * n_sig + t_das * frame.npix
+    return {"value": 1.0 / sec_per_frame, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"prep of {reps * len(rx_idx)} A-scans + delay-and-sum of {len(idx)} grid points "
+                      f"(FP32 oracle, {threads} threads), scaled to {n_sig} A-scans and {frame.npix} points",
+            "sec_per_frame": sec_per_frame}
+
+
+def run_reference(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    frame, desc = _workload(args.workload, "f32")
+    threads = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(frame, threads, a_sample=64, p_sample=4096)
+        if i >= args.warmup:
+            times.append(r["sec_per_frame"])
+    value = 1.0 / statistics.mean(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded point + speckle scatterers)",
+            "config": {"workload": desc, "sample": "per step: bounded sample scaled to one frame"},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    from us_lab4a_gb300 import StaEngine, build
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    build.build()
+    frame, desc = _workload(args.workload, args.storage)
+    spec = frame.spec
+    eng = StaEngine(spec)
+    stream = torch.cuda.Stream(device=dev)
+    eng.set_stream(stream)
+    with torch.cuda.stream(stream):
+        rf0 = frame.make_rf_torch(dev)
+        rfs = [rf0] + [rf0 * (1.0 + 0.01 * i) for i in range(1, 4)]  # 4 distinct resident inputs
+        grid = torch.as_tensor(frame.grid_xyz, device=dev)
+        value = torch.empty(frame.grid_xyz.shape[:2], device=dev)
+        factor = torch.empty_like(value)
+    stream.synchronize()
+    eng.set_grid_device(grid)
+    info = eng.signal_info()
+
+    def step(i):
+        eng.process_device(rfs[i % len(rfs)], value, factor)
+
+    for i in range(args.warmup):
+        step(i)
+    stream.synchronize()
+    eng.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        step(i)
+        evs[i][1].record(stream)
+    t_end.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    eng.synchronize()
+    total_ms = t_start.elapsed_time(t_end)
+    per_step = [a.elapsed_time(b) for a, b in evs]
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # Kernel-level timing of the two stages (roofline of the dominant kernel).
+    sig = torch.empty(info["signal_bytes"] // 4 + 1, dtype=torch.float32, device=dev)
+    kt = {"prep": [], "das": []}
+    for i in range(args.warmup + 5):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        eng.prepare_signals_device(rfs[i % len(rfs)], sig)
+        e1.record(stream)
+        eng.delay_and_sum_device(sig, value, factor)
+        e2.record(stream)
+        stream.synchronize()
+        if i >= args.warmup:
+            kt["prep"].append(e0.elapsed_time(e1))
+            kt["das"].append(e1.elapsed_time(e2))
+    eng.synchronize()
+    n_sig = spec.num_tx * spec.num_rx
+    L = info["signal_length"]
+    esize = {"f32": 8, "f16": 4, "bf16": 4}[spec.storage]
+    prep_bytes = n_sig * spec.num_samples * 4 + n_sig * L * esize
+    das_bytes = n_sig * L * esize + frame.npix * (12 + 8) + (spec.num_tx + spec.num_rx) * 8 + spec.num_rx * 4
+    prep_ms, das_ms = statistics.median(kt["prep"]), statistics.median(kt["das"])
+    peak, peak_kind = _peaks()
+    top = ("das", das_ms, das_bytes) if das_ms >= prep_ms else ("prep", prep_ms, prep_bytes)
+    achieved = top[2] / (top[1] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        tr = json.load(open(tfile)).get(args.workload + "/" + spec.storage + "/" + top[0])
+        if tr:
+            traffic = tr
+    gathers = frame.npix * n_sig
+
+    # End to end through the host entry points (host RF in, host image out).
+    e2e = None
+    if not args.no_e2e:
+        rf_host = rf0.cpu().numpy()
+        for i in range(args.warmup):
+            eng.process_host(rf_host)
+        lat = []
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            s0 = time.perf_counter()
+            eng.process_host(rf_host)
+            lat.append(time.perf_counter() - s0)
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": world * args.steps / e2e_s if world == 1 else None, "unit": "frames/s",
+               "h2d_bytes_per_step": int(rf_host.nbytes), "d2h_bytes_per_step": int(2 * frame.npix * 4),
+               "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99))}
+        if world > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e["value"] = world * args.steps / float(t.item())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(frame, os.cpu_count() or 1)
+        cpu.pop("sec_per_frame", None)
+
+    if rank == 0:
+        fps = world * args.steps / (total_ms * 1e-3)
+        line = {
+            "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": spec.storage if spec.storage != "f32" else "f32",
+            "data": "synthetic (seeded point + speckle scatterers)",
+            "config": {"workload": desc, "storage": spec.storage, "das_kernel": "plain",
+                       "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
+                       "parallelism": f"replicas x{world}"},
+            "voxels_per_s": fps * frame.npix,
+            "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
+            "kernels_ms": {"prep": prep_ms, "das": das_ms},
+            "roofline": {"bound": "hbm", "kernel": top[0], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes": top[2]},
+            "das_gathers_per_s": gathers / (das_ms * 1e-3),
+            "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cf2d", choices=["cf2d", "plain2d", "matrix3d"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -141,9 +141,12 @@ int usgb_delay_and_sum_device(usgb_ctx* ctx, const void* d_signals, float* d_val
 int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft_size,
 		uint32_t* signal_stride, size_t* signal_bytes);
 
-/* Selects the delay-and-sum kernel: 0 = plain (one thread per point, global
- * gathers), 1 = staged (TMA-staged A-scan windows per pixel tile). */
-int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t tile_cols);
+/* Selects the delay-and-sum kernel: 0 = plain (one thread per point, gathers
+ * from global memory), 1 = staged (per tile of 32 columns x tile_rows rows,
+ * the A-scan windows the tile needs are bulk-copied into shared memory,
+ * stage_bytes per pipeline stage). 0 for tile_rows / stage_bytes keeps the
+ * current value. */
+int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes);
 
 /* Waits for the context's stream and reports a device-side error (a bounded
  * wait that gave up) as USGB_ERR_DEVICE_TIMEOUT. */

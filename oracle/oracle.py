@@ -270,6 +270,18 @@ def pcf(values: np.ndarray, gamma: float) -> float:
     return float(_lib().orc_pcf_f64(_ptr(v.view(np.float64), C.c_double), v.size, gamma))
 
 
+def kaiser_beta(tol_db: float) -> float:
+    f = _lib().orc_kaiser_beta_f64
+    f.restype, f.argtypes = C.c_double, [C.c_double]
+    return float(f(tol_db))
+
+
+def kaiser_size(tol_db: float, transition_width: float) -> int:
+    f = _lib().orc_kaiser_size_f64
+    f.restype, f.argtypes = C.c_int, [C.c_double, C.c_double]
+    return int(f(tol_db, transition_width))
+
+
 def hilbert_fft_size(n: int) -> int:
     return int(_lib().orc_hilbert_fft_size(n))
 

@@ -189,6 +189,12 @@ int orc_remove_dc_f64(double* data, unsigned size, unsigned begin)
 	try { orc::remove_dc<double>(data, size, begin); return 0; }
 	catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
+double orc_kaiser_beta_f64(double tol_dB) { return orc::kaiser_beta<double>(tol_dB); }
+int orc_kaiser_size_f64(double tol_dB, double transitionWidth)
+{
+	try { return static_cast<int>(orc::kaiser_size<double>(tol_dB, transitionWidth)); }
+	catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
 double orc_scf_f64(const double* d, unsigned n, double p) { return orc::scf<double>(d, n, p); }
 double orc_pcf_f64(const double* d, unsigned n, double gamma)
 {

@@ -1,0 +1,163 @@
+"""Regenerates the golden fixtures of tests/golden/ (run where the reference
+sources are present; the fixtures are committed and travel with the tests).
+
+1. reference_vectors.npz: the reference's own golden vectors from its test
+   directory (test/*.h5; written by test/gen_*.py with scipy and by
+   TestMethod::testInterpolator4X): Hilbert input/outputs, interpolation 2x/8x/64x,
+   Interpolator4X input/output, Kaiser beta/size tables. The files are
+   chunked, deflate-compressed HDF5 1-D float64 datasets; each chunk is one
+   zlib stream, stored in dataset order, so the data is recovered by
+   inflating every zlib stream in file order (lengths are checked against
+   the shapes the reference's tests expect).
+2. reference_frames.npz: outputs of the reference processors themselves
+   (VectorialSTAProcessor, Vectorial3DSTAProcessor, DefaultSTAProcessor,
+   compiled from their sources by oracle/refbuild) on small seeded frames,
+   with the inputs (RF, grid, parameters) stored beside them.
+
+Usage: python tests/golden/make_golden.py [--reference /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+
+def h5_float64(path: str) -> np.ndarray:
+    data = open(path, "rb").read()
+    out = []
+    i = 0
+    while i < len(data) - 2:
+        if data[i] == 0x78 and ((data[i] << 8) | data[i + 1]) % 31 == 0:
+            d = zlib.decompressobj()
+            try:
+                r = d.decompress(data[i:])
+            except zlib.error:
+                i += 1
+                continue
+            if d.eof and r and len(r) % 8 == 0:
+                out.append(np.frombuffer(r, "<f8"))
+                i = len(data) - len(d.unused_data)
+                continue
+        i += 1
+    if not out:
+        raise RuntimeError(f"no data in {path}")
+    return np.concatenate(out)
+
+
+def reference_vectors(ref_test: str) -> dict:
+    r = lambda n: h5_float64(os.path.join(ref_test, n + ".h5"))  # noqa: E731
+    v = {
+        "hilbert_x": r("hilbert_x"), "hilbert_yr": r("hilbert_yr"), "hilbert_yi": r("hilbert_yi"),
+        "interp_source": r("interp_source"),
+        "interp_2x": r("interp_2x"), "interp_8x": r("interp_8x"), "interp_64x": r("interp_64x"),
+        "interp4x_x": r("interp_x"), "interp4x_y": r("interp_y"),
+        "kaiser_tol_db": r("kaiser_tol_db"), "kaiser_beta": r("kaiser_beta"),
+        "kaiser_size_0.05": r("kaiser_size-trans_width_0.05"), "kaiser_size_0.1": r("kaiser_size-trans_width_0.1"),
+        "kaiser_size_0.5": r("kaiser_size-trans_width_0.5"),
+    }
+    n = v["hilbert_x"].size
+    assert v["hilbert_yr"].size == n and v["hilbert_yi"].size == n
+    m = v["interp_source"].size
+    for U in (2, 8, 64):
+        assert v[f"interp_{U}x"].size == m * U, (U, v[f"interp_{U}x"].size)
+    assert v["interp4x_y"].size == 4 * v["interp4x_x"].size
+    assert v["kaiser_beta"].size == v["kaiser_tol_db"].size
+    return v
+
+
+def _quantized(fr):
+    """RF rounded to FP16 values (exact float32 inputs; halves the fixture size)."""
+    fr.rf = fr.make_rf_numpy().astype(np.float16).astype(np.float32)
+    return fr
+
+
+def reference_frames() -> dict:
+    from oracle import ref
+    from us_lab4a_gb300 import workloads
+    out = {}
+
+    def put(prefix, fr, value, factor, **meta):
+        out[prefix + "/rf"] = fr.make_rf_numpy().astype(np.float16)
+        out[prefix + "/grid"] = fr.grid_xyz
+        out[prefix + "/apod"] = np.asarray(fr.spec.rx_apod if fr.spec.rx_apod is not None else np.ones(fr.spec.num_rx), np.float32)
+        out[prefix + "/value"] = value
+        out[prefix + "/factor"] = factor
+        for k, x in meta.items():
+            out[prefix + "/" + k] = np.asarray(x)
+
+    # VectorialSTAProcessor<float>, no CF.
+    fr = _quantized(workloads.plain2d(tiny=True))
+    n = fr.spec.num_tx
+    kw = dict(num_samples=fr.spec.num_samples, upsampling=fr.spec.upsampling, fs=fr.spec.sampling_frequency,
+              c=fr.spec.propagation_speed, fc=fr.spec.center_frequency, rx_apod=fr.spec.rx_apod,
+              num_elements=n, first_tx=0, last_tx=n - 1, pitch=0.3e-3)
+    v, f = ref.process(rf=fr.make_rf_numpy(), grid_xyz=fr.grid_xyz, cf=0, **kw)
+    put("vectorial_plain", fr, v, f, num_elements=n, upsampling=fr.spec.upsampling, cf=0)
+    # VectorialSTAProcessor<float> with PCF, a peak offset and a dead zone.
+    fr = _quantized(workloads.cf2d(tiny=True))
+    n = fr.spec.num_tx
+    kw = dict(num_samples=fr.spec.num_samples, upsampling=fr.spec.upsampling, fs=fr.spec.sampling_frequency,
+              c=fr.spec.propagation_speed, fc=fr.spec.center_frequency, rx_apod=fr.spec.rx_apod,
+              num_elements=n, first_tx=0, last_tx=n - 1, pitch=0.3e-3)
+    v, f = ref.process(rf=fr.make_rf_numpy(), grid_xyz=fr.grid_xyz, cf=1, pcf_gamma=1.0, peak_offset=1.5,
+                       dead_zone_m=0.5e-3, **kw)
+    put("vectorial_pcf", fr, v, f, num_elements=n, upsampling=fr.spec.upsampling, cf=1, pcf_gamma=1.0,
+        peak_offset=1.5, dead_zone_m=0.5e-3)
+    # Sub-aperture transmit (first_tx_elem..last_tx_elem), U = 1 (no interpolation).
+    fr = _quantized(workloads.plain2d(tiny=True, seed=1010))
+    n = fr.spec.num_tx
+    rf = fr.make_rf_numpy()[3:9]
+    kw = dict(num_samples=fr.spec.num_samples, upsampling=1, fs=fr.spec.sampling_frequency,
+              c=fr.spec.propagation_speed, fc=fr.spec.center_frequency, rx_apod=fr.spec.rx_apod,
+              num_elements=n, first_tx=3, last_tx=8, pitch=0.3e-3)
+    v, f = ref.process(rf=rf, grid_xyz=fr.grid_xyz, cf=1, pcf_gamma=2.0, **kw)
+    out["vectorial_subtx/rf"] = rf.astype(np.float16)
+    out["vectorial_subtx/grid"] = fr.grid_xyz
+    out["vectorial_subtx/apod"] = np.asarray(fr.spec.rx_apod, np.float32)
+    out["vectorial_subtx/value"] = v
+    out["vectorial_subtx/factor"] = f
+    out["vectorial_subtx/first_tx"] = np.asarray(3)
+    out["vectorial_subtx/last_tx"] = np.asarray(8)
+    out["vectorial_subtx/num_elements"] = np.asarray(n)
+    out["vectorial_subtx/pcf_gamma"] = np.asarray(2.0)
+    # DefaultSTAProcessor<float> (real RF, fixed 4x FIR) with SCF p = 2.
+    fr = _quantized(workloads.plain2d(tiny=True, seed=1011))
+    n = fr.spec.num_tx
+    v, f = ref.process(rf=fr.make_rf_numpy(), grid_xyz=fr.grid_xyz, num_samples=fr.spec.num_samples, upsampling=4,
+                       fs=fr.spec.sampling_frequency, c=fr.spec.propagation_speed, fc=fr.spec.center_frequency,
+                       cf=2, scf_p=2.0, real_path=True, num_elements=n, first_tx=0, last_tx=n - 1, pitch=0.3e-3)
+    put("default_scf", fr, v, f, num_elements=n, cf=2, scf_p=2.0)
+    # Vectorial3DSTAProcessor<float> with PCF (6 x 6 matrix array).
+    fr = _quantized(workloads.matrix3d(tiny=True))
+    v, f = ref.process(rf=fr.make_rf_numpy(), grid_xyz=fr.grid_xyz, num_samples=fr.spec.num_samples, upsampling=4,
+                       fs=fr.spec.sampling_frequency, c=fr.spec.propagation_speed, fc=fr.spec.center_frequency,
+                       rx_apod=fr.spec.rx_apod, cf=1, pcf_gamma=1.0, matrix=(4, 4, 0.3e-3, 0.3e-3))
+    put("vectorial3d_pcf", fr, v, f, nx=4, cf=1, pcf_gamma=1.0)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    vec = reference_vectors(os.path.join(args.reference, "test"))
+    np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
+    from oracle import ref
+    if not ref.available():
+        ref.build()
+    frames = reference_frames()
+    np.savez_compressed(os.path.join(HERE, "reference_frames.npz"), **frames)
+    for f in ("reference_vectors.npz", "reference_frames.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,57 @@
+"""Shared helpers of the parity tests: mapping a workload frame to the oracle,
+running it through the library, and error metrics."""
+from __future__ import annotations
+
+import numpy as np
+
+CF_CODE = {"none": 0, "pcf": 1, "scf": 2, "mf": 3}
+
+
+def oracle_spec(oracle_lib, spec, nthreads=None):
+    kw = {}
+    if nthreads:
+        kw["nthreads"] = nthreads
+    return oracle_lib.OracleSpec(
+        tx_xy=spec.tx_xy, rx_xy=spec.rx_xy, num_samples=spec.num_samples,
+        upsampling=4 if spec.real_path else spec.upsampling, sampling_frequency=spec.sampling_frequency,
+        propagation_speed=spec.propagation_speed, center_frequency=spec.center_frequency,
+        peak_offset=spec.peak_offset, dead_zone_m=spec.dead_zone_m,
+        rx_apod=spec.rx_apod if spec.rx_apod is not None else np.ones(spec.num_rx, np.float32),
+        cf=CF_CODE[spec.coherence], pcf_gamma=spec.pcf_gamma, scf_p=spec.scf_p, real_path=spec.real_path, **kw)
+
+
+def run_host(spec, rf, grid_xyz):
+    """Through the host C-ABI path (submit_rf + process)."""
+    from us_lab4a_gb300 import StaEngine
+    with StaEngine(spec) as eng:
+        eng.set_grid(grid_xyz)
+        return eng.process_host(rf)
+
+
+def run_device(spec, rf, grid_xyz, device="cuda:0", variant=None):
+    """Through the device C-ABI path (resident torch tensors)."""
+    import torch
+    from us_lab4a_gb300 import StaEngine
+    with StaEngine(spec) as eng:
+        if variant is not None:
+            eng.set_das_variant(variant)
+        stream = torch.cuda.current_stream()
+        eng.set_stream(stream)
+        g = torch.as_tensor(np.ascontiguousarray(grid_xyz, np.float32), device=device)
+        r = torch.as_tensor(np.ascontiguousarray(rf, np.float32), device=device)
+        v = torch.empty(grid_xyz.shape[:2], dtype=torch.float32, device=device)
+        f = torch.empty_like(v)
+        eng.set_grid_device(g)
+        eng.process_device(r, v, f)
+        eng.synchronize()
+        return v.cpu().numpy(), f.cpu().numpy()
+
+
+def rel_err(a, b) -> float:
+    return float(np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)).max() / np.abs(b).max())
+
+
+def db_err(a, b) -> float:
+    """Peak-relative error in dB: 20 log10(max |a - b| / max |b|)."""
+    e = rel_err(a, b)
+    return -np.inf if e == 0 else 20.0 * np.log10(e)

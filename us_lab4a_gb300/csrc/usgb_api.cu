@@ -159,7 +159,8 @@ struct usgb_ctx {
 	cudaStream_t stream = nullptr;
 	bool ownStream = false;
 	int dasVariant = 0;
-	unsigned tileRows = 8, tileCols = 32;
+	unsigned tileRows = 8;
+	unsigned stageBytes = 16384;
 	std::string err;
 
 	~usgb_ctx()
@@ -385,7 +386,7 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.factor = d_factor;
 	dp.errWord = c->d_err;
 	dp.tileRows = c->tileRows;
-	dp.tileCols = c->tileCols;
+	dp.stageBytes = c->stageBytes;
 	return dp;
 }
 
@@ -592,6 +593,9 @@ int usgb_prepare_signals_device(usgb_ctx* c, const float* d_rf, void* d_signals)
 {
 	return guarded(c, [&] {
 		if (!d_rf || !d_signals) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+		if (reinterpret_cast<uintptr_t>(d_signals) % 16 != 0) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The signal tensor must be 16-byte aligned.");
+		}
 		const usgb::PrepParams pp = prep_params(c, d_rf, d_signals);
 		USGB_CUDA(usgb::launch_prep(pp, static_cast<int>(c->prm.storage), c->analytic, c->stream));
 	});
@@ -602,6 +606,9 @@ int usgb_delay_and_sum_device(usgb_ctx* c, const void* d_signals, float* d_value
 	return guarded(c, [&] {
 		if (!d_signals || !d_value || !d_factor) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
 		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+		if (reinterpret_cast<uintptr_t>(d_signals) % 16 != 0) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The signal tensor must be 16-byte aligned.");
+		}
 		USGB_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
 		const usgb::DasParams dp = das_params(c, d_signals, d_value, d_factor);
 		USGB_CUDA(usgb::launch_das(dp, static_cast<int>(c->prm.storage), static_cast<int>(c->prm.coherence),
@@ -619,13 +626,29 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 	return USGB_OK;
 }
 
-int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t tile_cols)
+int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes)
 {
 	return guarded(c, [&] {
-		if (variant != 0) USGB_FAIL(USGB_ERR_UNSUPPORTED, "delay-and-sum variant " << variant << " is not available");
+		if (variant != 0 && variant != 1) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
+		const unsigned rows = tile_rows ? tile_rows : c->tileRows;
+		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
+		if (variant == 1) {
+			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
+			}
+			int dev = 0, maxSmem = 0;
+			USGB_CUDA(cudaGetDevice(&dev));
+			USGB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+			const size_t need = usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap);
+			if (need > static_cast<size_t>(maxSmem)) {
+				USGB_FAIL(USGB_ERR_UNSUPPORTED, "Staged delay-and-sum needs " << need << " bytes of shared memory (device: "
+						<< maxSmem << "); use fewer tile rows or smaller stages.");
+			}
+		}
 		c->dasVariant = variant;
-		if (tile_rows) c->tileRows = tile_rows;
-		if (tile_cols) c->tileCols = tile_cols;
+		c->tileRows = rows;
+		c->stageBytes = cap;
 	});
 }
 

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "usgb_common.cuh"
+#include "usgb_das_cf.cuh"
 #include "usgb_internal.h"
 
 namespace usgb {
@@ -35,62 +36,6 @@ __device__ __forceinline__ int split_delay(float d, float& frac)
 	frac = d - (t - 8388608.0f);
 	return __float_as_int(t) - 0x4B000000;
 }
-
-// Per-pixel coherence-factor state over the receivers.
-template<int CF> struct CFState {
-	__device__ void add(float2) {}
-	__device__ float result(unsigned, const DasParams&, float2) const { return 1.0f; }
-};
-
-// PCF (src/util/CoherenceFactor.h:267-286): population standard deviation of
-// the phases phi and of phi -+ pi, accumulated with Welford's update.
-template<> struct CFState<CF_PCF> {
-	unsigned n = 0;
-	float m1 = 0.f, s1 = 0.f, m2 = 0.f, s2 = 0.f;
-	__device__ void add(float2 v)
-	{
-		const float phi = atan2f(v.y, v.x);
-		const float pi = 3.14159265358979323846f;
-		const float aux = phi + ((phi < 0.f) ? pi : -pi);
-		++n;
-		const float inv = 1.0f / static_cast<float>(n);
-		float d = phi - m1;
-		m1 += d * inv;
-		s1 += d * (phi - m1);
-		d = aux - m2;
-		m2 += d * inv;
-		s2 += d * (aux - m2);
-	}
-	__device__ float result(unsigned N, const DasParams& p, float2) const
-	{
-		const float sd1 = sqrtf(s1 / static_cast<float>(N));
-		const float sd2 = sqrtf(s2 / static_cast<float>(N));
-		return fmaxf(0.f, 1.f - p.pcfFactor * fminf(sd1, sd2));
-	}
-};
-
-// SCF (src/util/CoherenceFactor.h:217-236) on the real parts, sign(0) = +1.
-template<> struct CFState<CF_SCF> {
-	int signSum = 0;
-	__device__ void add(float2 v) { signSum += (v.x >= 0.f) ? 1 : -1; }
-	__device__ float result(unsigned N, const DasParams& p, float2) const
-	{
-		const float k = static_cast<float>(signSum) / static_cast<float>(N);
-		const float m = 1.f - sqrtf(1.f - k * k);
-		return powf(fabsf(m), p.scfP);
-	}
-};
-
-// Mallart-Fink CF: |sum s|^2 / (N sum |s|^2) (not in the reference).
-template<> struct CFState<CF_MF> {
-	float energy = 0.f;
-	__device__ void add(float2 v) { energy = fmaf(v.x, v.x, fmaf(v.y, v.y, energy)); }
-	__device__ float result(unsigned N, const DasParams&, float2 total) const
-	{
-		if (energy == 0.f) return 0.f;
-		return (total.x * total.x + total.y * total.y) / (static_cast<float>(N) * energy);
-	}
-};
 
 // Plain form: one thread per grid point, gathers straight from global
 // memory. Receiver-major loop so that each receiver's sum over transmitters
@@ -154,8 +99,7 @@ das_direct_kernel(DasParams p)
 				}
 			}
 		}
-		const float w = __ldg(&p.apod[r]) * p.invScale;
-		const float2 rs = make_float2(acc.x * w, acc.y * w);
+		const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
 		total.x += rs.x;
 		total.y += rs.y;
 		cf.add(rs);
@@ -193,8 +137,9 @@ cudaError_t dispatch_cf(const DasParams& p, int cf, bool analytic, cudaStream_t 
 
 }  // namespace
 
-cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int /*variant*/, cudaStream_t stream)
+cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream)
 {
+	if (variant == 1) return launch_das_staged(p, storage, cf, analytic, p.stageBytes, stream);
 	switch (storage) {
 	case STORE_F16: return dispatch_cf<STORE_F16>(p, cf, analytic, stream);
 	case STORE_BF16: return dispatch_cf<STORE_BF16>(p, cf, analytic, stream);

@@ -55,10 +55,15 @@ struct DasParams {
 	float* value;
 	float* factor;
 	unsigned* errWord;
-	// Tiling of the staged kernel (rows x cols of pixels per block).
-	unsigned tileRows, tileCols;
+	// Staged kernel: rows of the 32-column pixel tile, bytes per pipeline stage.
+	unsigned tileRows;
+	unsigned stageBytes;
 };
 
+// variant 0: plain kernel; 1: staged kernel.
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
+cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, unsigned capBytes,
+		cudaStream_t stream);
+size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes);
 
 }  // namespace usgb

@@ -111,8 +111,9 @@ class StaEngine:
         return {"signal_length": L.value, "fft_size": N.value, "signal_stride": stride.value,
                 "signal_bytes": nbytes.value}
 
-    def set_das_variant(self, variant: int, tile_rows: int = 0, tile_cols: int = 0) -> None:
-        self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, tile_cols))
+    def set_das_variant(self, variant: int, tile_rows: int = 0, stage_bytes: int = 0) -> None:
+        """0: plain kernel; 1: staged kernel (tile_rows in {4, 8, 16})."""
+        self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, stage_bytes))
 
     # -- host path (reference data flow) -----------------------------------
     def set_grid(self, xyz: np.ndarray) -> None:

@@ -84,8 +84,10 @@ def grid_xyz3(x0, x1, nx, y0, y1, ny, z0, z1, nz) -> np.ndarray:
     return g
 
 
-def plain2d(seed: int = 1000, small: bool = False) -> Frame:
+def plain2d(seed: int = 1000, small: bool = False, tiny: bool = False) -> Frame:
     n, ns, ncols, nrows = (32, 2048, 128, 256) if not small else (16, 512, 24, 40)
+    if tiny:
+        small, (n, ns, ncols, nrows) = True, (12, 320, 16, 24)
     rng = np.random.default_rng(seed)
     zr = (10e-3, 40e-3) if not small else (5e-3, 9e-3)
     scat = synth.point_scatterers(rng, 8, (-4e-3, 4e-3), zr)
@@ -96,8 +98,11 @@ def plain2d(seed: int = 1000, small: bool = False) -> Frame:
     return Frame("plain2d" + ("-small" if small else ""), spec, g, scat, seed)
 
 
-def cf2d(seed: int = 1001, small: bool = False, coherence: str = "pcf", num_speckle: Optional[int] = None) -> Frame:
+def cf2d(seed: int = 1001, small: bool = False, coherence: str = "pcf", num_speckle: Optional[int] = None,
+         tiny: bool = False) -> Frame:
     n, ns, ncols, nrows, U = (64, 4096, 512, 512, 8) if not small else (16, 640, 32, 32, 8)
+    if tiny:
+        small, (n, ns, ncols, nrows, U) = True, (12, 400, 20, 20, 8)
     rng = np.random.default_rng(seed)
     if small:
         pts = synth.point_scatterers(rng, 6, (-2e-3, 2e-3), (4e-3, 9e-3))
@@ -114,8 +119,11 @@ def cf2d(seed: int = 1001, small: bool = False, coherence: str = "pcf", num_spec
     return Frame("cf2d" + ("-small" if small else ""), spec, g, synth.Scatterers.concat(pts, spk), seed)
 
 
-def matrix3d(seed: int = 1002, small: bool = False, coherence: str = "pcf", storage: str = "f16") -> Frame:
+def matrix3d(seed: int = 1002, small: bool = False, coherence: str = "pcf", storage: str = "f16",
+             tiny: bool = False) -> Frame:
     nx, ns, (gx, gy, gz) = (16, 1024, (64, 64, 128)) if not small else (6, 384, (8, 8, 16))
+    if tiny:
+        small, nx, ns, (gx, gy, gz) = True, 4, 256, (6, 6, 12)
     rng = np.random.default_rng(seed)
     zr = (5e-3, 45e-3) if not small else (4e-3, 12e-3)
     scat = synth.point_scatterers(rng, 64 if not small else 8, (-5e-3, 5e-3), zr, y_range=(-5e-3, 5e-3))
