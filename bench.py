@@ -203,6 +203,8 @@ def run_gpu(args):
     frame, desc = _workload(args.workload, args.storage)
     spec = frame.spec
     eng = StaEngine(spec)
+    if args.das == "staged":
+        eng.set_das_variant(1, args.tile_rows, args.stage_bytes)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream)
     with torch.cuda.stream(stream):
@@ -315,7 +317,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": spec.storage if spec.storage != "f32" else "f32",
             "data": "synthetic (seeded point + speckle scatterers)",
-            "config": {"workload": desc, "storage": spec.storage, "das_kernel": "plain",
+            "config": {"workload": desc, "storage": spec.storage, "das_kernel": args.das + (f" (tile 32x{args.tile_rows}, {args.stage_bytes} B stages)" if args.das == "staged" else ""),
                        "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
                        "parallelism": f"replicas x{world}"},
             "voxels_per_s": fps * frame.npix,
@@ -341,6 +343,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cf2d", choices=["cf2d", "plain2d", "matrix3d"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--das", default="staged", choices=["plain", "staged"])
+    ap.add_argument("--tile-rows", type=int, default=8)
+    ap.add_argument("--stage-bytes", type=int, default=16384)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -126,7 +126,9 @@ std::vector<float> interpolator4x_taps()
 struct usgb_ctx {
 	usgb_sta_params prm{};
 	std::vector<float> txXY, rxXY, apod;
-	unsigned numSignals = 0, L = 0, N = 0, M = 0, U = 1, deadZone = 0, tapsPerPhase = 1;
+	unsigned numSignals = 0, L = 0, N = 0, M = 0, U = 1, deadZone = 0, tapsPerPhase = 1, tapsStride = 4;
+	unsigned twHiCount = 0, csHiCount = 0;
+	std::vector<unsigned long long> divMagic;
 	unsigned sigStride = 0;
 	size_t sigBytes = 0;
 	size_t elemBytes = 0;
@@ -190,11 +192,12 @@ void build_tables(usgb_ctx* c)
 	if (c->U > 1 && ((T - 1) % (2 * c->U) != 0)) USGB_FAIL(USGB_ERR_INVALID_STATE, "FIR length " << T << " is not 2*U*K + 1");
 	const unsigned K = (c->U > 1) ? (T - 1) / (2 * c->U) : 0;
 	c->tapsPerPhase = 2 * K + 1;
-	std::vector<float> poly(static_cast<size_t>(c->U) * c->tapsPerPhase, 0.f);
+	c->tapsStride = (c->tapsPerPhase + 3) & ~3u;
+	std::vector<float> poly(static_cast<size_t>(c->U) * c->tapsStride, 0.f);
 	for (unsigned r = 0; r < c->U; ++r) {
 		for (unsigned t = 0; t < c->tapsPerPhase; ++t) {
 			const unsigned j = r + t * c->U;
-			poly[r * c->tapsPerPhase + t] = (j < T) ? taps[j] : 0.f;
+			poly[r * c->tapsStride + t] = (j < T) ? taps[j] : 0.f;
 		}
 	}
 	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.size() * sizeof(float)));
@@ -215,14 +218,26 @@ void build_tables(usgb_ctx* c)
 		USGB_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << c->M << " not supported");
 	}
 	const unsigned M = c->M;
-	std::vector<float2> tw(M), cs(M / 2 + 1);
-	for (unsigned i = 0; i < M; ++i) {
-		const double a = -2.0 * kPi * static_cast<double>(i) / M;
-		tw[i] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
-	}
-	for (unsigned k = 0; k <= M / 2; ++k) {
-		const double a = kPi * static_cast<double>(k) / M;
-		cs[k] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+	// Two-level twiddle tables: W^m = hi[m / S] * lo[m % S], S = kTwiddleSplit.
+	const unsigned S = usgb::kTwiddleSplit;
+	c->twHiCount = (M + S - 1) / S;
+	c->csHiCount = (M / 2 + 1 + S - 1) / S;
+	std::vector<float2> tw(S + c->twHiCount), cs(S + c->csHiCount);
+	auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
+	for (unsigned j = 0; j < S; ++j) tw[j] = unit(-2.0 * kPi * static_cast<double>(j) / M);
+	for (unsigned q = 0; q < c->twHiCount; ++q) tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
+	for (unsigned j = 0; j < S; ++j) cs[j] = unit(kPi * static_cast<double>(j) / M);
+	for (unsigned q = 0; q < c->csHiCount; ++q) cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
+	// Multiply-shift division by each DIF stage's sub-block length:
+	// floor(b / sub) = (b * ceil(2^40 / sub)) >> 40, exact for b, sub < 2^20.
+	c->divMagic.clear();
+	{
+		unsigned Ms = M;
+		for (int r : c->radices) {
+			const unsigned sub = Ms / static_cast<unsigned>(r);
+			c->divMagic.push_back(((1ULL << 40) + sub - 1) / sub);
+			Ms = sub;
+		}
 	}
 	// Digit-reversed position of bin k after the in-place DIF stages:
 	// k = k0 + r0 (k1 + r1 (k2 + ...)) sits at sum_s k_s * M / (r0 ... r_s).
@@ -236,11 +251,11 @@ void build_tables(usgb_ctx* c)
 		}
 		perm[k] = pos;
 	}
-	USGB_CUDA(cudaMalloc(&c->d_tw, M * sizeof(float2)));
-	USGB_CUDA(cudaMalloc(&c->d_cs, (M / 2 + 1) * sizeof(float2)));
+	USGB_CUDA(cudaMalloc(&c->d_tw, tw.size() * sizeof(float2)));
+	USGB_CUDA(cudaMalloc(&c->d_cs, cs.size() * sizeof(float2)));
 	USGB_CUDA(cudaMalloc(&c->d_perm, M * sizeof(unsigned)));
-	USGB_CUDA(cudaMemcpy(c->d_tw, tw.data(), M * sizeof(float2), cudaMemcpyHostToDevice));
-	USGB_CUDA(cudaMemcpy(c->d_cs, cs.data(), (M / 2 + 1) * sizeof(float2), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
+	USGB_CUDA(cudaMemcpy(c->d_cs, cs.data(), cs.size() * sizeof(float2), cudaMemcpyHostToDevice));
 	USGB_CUDA(cudaMemcpy(c->d_perm, perm.data(), M * sizeof(unsigned), cudaMemcpyHostToDevice));
 }
 
@@ -349,14 +364,20 @@ usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
 	pp.U = c->U;
 	pp.L = c->L;
 	pp.tapsPerPhase = c->tapsPerPhase;
+	pp.tapsStride = c->tapsStride;
 	pp.polyTaps = c->d_polyTaps;
 	pp.deadZone = c->deadZone;
 	pp.outScale = c->scale;
 	pp.M = c->M;
 	pp.numStages = static_cast<int>(c->radices.size());
-	for (size_t i = 0; i < c->radices.size(); ++i) pp.radix[i] = c->radices[i];
+	for (size_t i = 0; i < c->radices.size(); ++i) {
+		pp.radix[i] = c->radices[i];
+		pp.divMagic[i] = c->divMagic[i];
+	}
 	pp.tw = c->d_tw;
+	pp.twHiCount = c->twHiCount;
 	pp.cs = c->d_cs;
+	pp.csHiCount = c->csHiCount;
 	pp.perm = c->d_perm;
 	return pp;
 }

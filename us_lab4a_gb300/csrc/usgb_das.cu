@@ -104,7 +104,7 @@ das_direct_kernel(DasParams p)
 		total.y += rs.y;
 		cf.add(rs);
 	}
-	const float v = ANALYTIC ? sqrtf(total.x * total.x + total.y * total.y) : total.x;
+	const float v = ANALYTIC ? magnitude(total) : total.x;
 	p.value[pix] = v * p.valueCoef;
 	p.factor[pix] = cf.result(p.numRx, p, total);
 }

@@ -18,6 +18,13 @@ __device__ __forceinline__ float2 receiver_sum(float2 acc, float w)
 	return make_float2(fmaf(acc.x, w, 0.0f), fmaf(acc.y, w, 0.0f));
 }
 
+// |total| with explicit rounding (no contraction choice left to the
+// compiler), so every kernel variant returns the same bits.
+__device__ __forceinline__ float magnitude(float2 v)
+{
+	return __fsqrt_rn(__fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)));
+}
+
 template<int CF> struct CFState {
 	__device__ void add(float2) {}
 	__device__ float result(unsigned, const DasParams&, float2) const { return 1.0f; }
@@ -34,19 +41,19 @@ template<> struct CFState<CF_PCF> {
 		const float pi = 3.14159265358979323846f;
 		const float aux = phi + ((phi < 0.f) ? pi : -pi);
 		++n;
-		const float inv = 1.0f / static_cast<float>(n);
-		float d = phi - m1;
-		m1 += d * inv;
-		s1 += d * (phi - m1);
-		d = aux - m2;
-		m2 += d * inv;
-		s2 += d * (aux - m2);
+		const float inv = __frcp_rn(static_cast<float>(n));
+		float d = __fsub_rn(phi, m1);
+		m1 = __fmaf_rn(d, inv, m1);
+		s1 = __fmaf_rn(d, __fsub_rn(phi, m1), s1);
+		d = __fsub_rn(aux, m2);
+		m2 = __fmaf_rn(d, inv, m2);
+		s2 = __fmaf_rn(d, __fsub_rn(aux, m2), s2);
 	}
 	__device__ float result(unsigned N, const DasParams& p, float2) const
 	{
-		const float sd1 = sqrtf(s1 / static_cast<float>(N));
-		const float sd2 = sqrtf(s2 / static_cast<float>(N));
-		return fmaxf(0.f, 1.f - p.pcfFactor * fminf(sd1, sd2));
+		const float sd1 = __fsqrt_rn(__fdiv_rn(s1, static_cast<float>(N)));
+		const float sd2 = __fsqrt_rn(__fdiv_rn(s2, static_cast<float>(N)));
+		return fmaxf(0.f, __fsub_rn(1.f, __fmul_rn(p.pcfFactor, fminf(sd1, sd2))));
 	}
 };
 
@@ -56,8 +63,8 @@ template<> struct CFState<CF_SCF> {
 	__device__ void add(float2 v) { signSum += (v.x >= 0.f) ? 1 : -1; }
 	__device__ float result(unsigned N, const DasParams& p, float2) const
 	{
-		const float k = static_cast<float>(signSum) / static_cast<float>(N);
-		const float m = 1.f - sqrtf(1.f - k * k);
+		const float k = __fdiv_rn(static_cast<float>(signSum), static_cast<float>(N));
+		const float m = __fsub_rn(1.f, __fsqrt_rn(__fsub_rn(1.f, __fmul_rn(k, k))));
 		return powf(fabsf(m), p.scfP);
 	}
 };
@@ -65,11 +72,12 @@ template<> struct CFState<CF_SCF> {
 // Mallart-Fink CF: |sum s|^2 / (N sum |s|^2) (not in the reference).
 template<> struct CFState<CF_MF> {
 	float energy = 0.f;
-	__device__ void add(float2 v) { energy = fmaf(v.x, v.x, fmaf(v.y, v.y, energy)); }
+	__device__ void add(float2 v) { energy = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, energy)); }
 	__device__ float result(unsigned N, const DasParams&, float2 total) const
 	{
 		if (energy == 0.f) return 0.f;
-		return (total.x * total.x + total.y * total.y) / (static_cast<float>(N) * energy);
+		const float num = __fadd_rn(__fmul_rn(total.x, total.x), __fmul_rn(total.y, total.y));
+		return __fdiv_rn(num, __fmul_rn(static_cast<float>(N), energy));
 	}
 };
 

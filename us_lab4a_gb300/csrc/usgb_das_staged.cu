@@ -29,7 +29,7 @@ namespace usgb {
 namespace {
 
 constexpr int kStages = 4;          // pipeline depth
-constexpr int kMaxWindows = 8;      // windows per stage
+constexpr int kMaxWindows = 32;     // windows per stage (one per producer lane)
 constexpr int kGlobalWindow = -1;   // window too large for a stage: gather from global memory
 constexpr int kEmptyWindow = -2;    // no valid sample can be reached
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
@@ -37,9 +37,8 @@ constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 struct StageMeta {
 	int count;
 	int lastOfRx;
-	int tx[kMaxWindows];
-	int lo[kMaxWindows];
-	int off[kMaxWindows];
+	int pad[2];
+	int4 win[kMaxWindows];  // (tx, lo, off, 0) per window
 };
 
 // Shared-memory layout (byte offsets), computed identically on host and device.
@@ -93,7 +92,7 @@ __device__ __forceinline__ int floor_to_int(float v)
 }
 
 template<int S, int CF, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32)
+__global__ void __launch_bounds__((TROWS + 1) * 32, 1)
 das_staged_kernel(DasParams p, unsigned capBytes)
 {
 	using SP = Sample<ANALYTIC, S>;
@@ -177,80 +176,87 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 	const T* sig = reinterpret_cast<const T*>(p.sig);
 
 	if (producer) {
-		if (lane != 0) return;
-		// ------------------------------------------------------------- producer
+		// -------------------------------------------------------------- producer
+		// The 32 lanes size 32 consecutive transmit windows of the current
+		// receiver at once; a prefix sum packs as many as fit into the stage,
+		// lane 0 arms the stage's barrier with the total byte count and every
+		// lane issues its own bulk copy.
 		int it = 0;
 		bool ok = true;
 		for (unsigned r = 0; r < p.numRx && ok; ++r) {
-			unsigned t = 0;
-			while (t < p.numTx) {
+			unsigned t0 = 0;
+			while (t0 < p.numTx) {
 				const int s = it % kStages;
-				if (it >= kStages && !mbar_wait_bounded(&empty[s], ((it / kStages) - 1) & 1, kWaitLimitNs)) {
-					atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-					ok = false;
-					break;
+				if (it >= kStages) {
+					bool w = true;
+					if (lane == 0) w = mbar_wait_bounded(&empty[s], ((it / kStages) - 1) & 1, kWaitLimitNs);
+					w = __shfl_sync(0xffffffffu, w, 0);
+					if (!w) {
+						if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+						ok = false;
+						break;
+					}
 				}
-				StageMeta& m = meta[s];
-				T* buf = reinterpret_cast<T*>(stageBuf + static_cast<size_t>(s) * capBytes);
-				int n = 0;
-				unsigned usedBytes = 0;
-				const T* srcs[kMaxWindows];
-				unsigned nbytes[kMaxWindows];
-				while (t < p.numTx && n < kMaxWindows) {
+				const unsigned t = t0 + lane;
+				int lo = 0, kind = kEmptyWindow;
+				unsigned wb = 0;
+				if (t < p.numTx) {
 					const float a = __fadd_rn(minT[t], minR[r]);
 					const float b = __fadd_rn(maxT[t], maxR[r]);
 					// Window [lo, hi] of sample indices (a valid gather reads idx and idx + 1).
-					float lof = fmaxf(floorf(a), 0.0f);
-					float hif = fminf(floorf(b) + 1.0f, static_cast<float>(L - 1));
-					m.tx[n] = static_cast<int>(t);
-					if (!(lof <= static_cast<float>(L - 2)) || !(hif >= 1.0f) || hif < lof) {
-						m.lo[n] = 0;
-						m.off[n] = kEmptyWindow;
-						nbytes[n] = 0;
-						++n;
-						++t;
-						continue;
-					}
-					int lo = static_cast<int>(lof) & ~(SP::kAlign - 1);
-					const int hi = static_cast<int>(hif);
-					const unsigned cnt = static_cast<unsigned>(hi - lo + 1);
-					const unsigned wb = (cnt * static_cast<unsigned>(sizeof(T)) + 15u) & ~15u;
-					if (usedBytes + wb > capBytes) {
-						if (n == 0) {  // larger than a whole stage: consumers read global memory
-							m.lo[n] = lo;
-							m.off[n] = kGlobalWindow;
-							nbytes[n] = 0;
-							++n;
-							++t;
+					const float lof = fmaxf(floorf(a), 0.0f);
+					const float hif = fminf(floorf(b) + 1.0f, static_cast<float>(L - 1));
+					if (lof <= static_cast<float>(L - 2) && hif >= 1.0f && hif >= lof) {
+						lo = static_cast<int>(lof) & ~(SP::kAlign - 1);
+						const unsigned cnt = static_cast<unsigned>(static_cast<int>(hif) - lo + 1);
+						wb = (cnt * static_cast<unsigned>(sizeof(T)) + 15u) & ~15u;
+						if (wb > capBytes) {  // larger than a whole stage: consumers read global memory
+							kind = kGlobalWindow;
+							wb = 0;
+						} else {
+							kind = 0;
 						}
-						break;
-					}
-					m.lo[n] = lo;
-					m.off[n] = static_cast<int>(usedBytes / sizeof(T));
-					srcs[n] = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
-					nbytes[n] = wb;
-					usedBytes += wb;
-					++n;
-					++t;
-				}
-				m.count = n;
-				m.lastOfRx = (t == p.numTx) ? 1 : 0;
-				mbar_arrive_expect_tx(&full[s], usedBytes);
-				unsigned off = 0;
-				for (int w = 0; w < n; ++w) {
-					if (nbytes[w]) {
-						bulk_copy_g2s(reinterpret_cast<unsigned char*>(buf) + off, srcs[w], nbytes[w], &full[s]);
-						off += nbytes[w];
 					}
 				}
+				unsigned incl = wb;
+				for (int o = 1; o < 32; o <<= 1) {
+					const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+					if (lane >= o) incl += v;
+				}
+				// Lanes that fit form a prefix (incl is non-decreasing); lane 0
+				// always fits, since an oversized window carries no bytes.
+				const bool fits = t < p.numTx && incl <= capBytes;
+				const int n = __popc(__ballot_sync(0xffffffffu, fits));
+				const unsigned total = __shfl_sync(0xffffffffu, incl, n - 1);
+				const unsigned excl = incl - wb;
+				StageMeta& m = meta[s];
+				if (lane < n) {
+					const int off = (kind == 0) ? static_cast<int>(excl / sizeof(T)) : kind;
+					m.win[lane] = make_int4(static_cast<int>(t), lo, off, 0);
+				}
+				if (lane == 0) {
+					m.count = n;
+					m.lastOfRx = (t0 + n == p.numTx) ? 1 : 0;
+				}
+				__threadfence_block();
+				__syncwarp();
+				if (lane == 0) mbar_arrive_expect_tx(&full[s], total);
+				__syncwarp();
+				if (lane < n && wb > 0) {
+					const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
+					bulk_copy_g2s(stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &full[s]);
+				}
+				t0 += static_cast<unsigned>(n);
 				++it;
 			}
 		}
 		// Let every issued copy land before the block can exit.
-		for (int j = (it > kStages ? it - kStages : 0); j < it; ++j) {
-			if (!mbar_wait_bounded(&full[j % kStages], (j / kStages) & 1, kWaitLimitNs)) {
-				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-				break;
+		if (lane == 0) {
+			for (int j = (it > kStages ? it - kStages : 0); j < it; ++j) {
+				if (!mbar_wait_bounded(&full[j % kStages], (j / kStages) & 1, kWaitLimitNs)) {
+					atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+					break;
+				}
 			}
 		}
 		return;
@@ -276,15 +282,16 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 		const T* buf = reinterpret_cast<const T*>(stageBuf + static_cast<size_t>(s) * capBytes);
 		const int n = m.count;
 		for (int w = 0; w < n; ++w) {
-			const int t = m.tx[w];
-			const int off = m.off[w];
+			const int4 wm = m.win[w];
+			const int t = wm.x;
+			const int off = wm.z;
 			const float d = fmaxf(__fadd_rn(txd[t * P + slot], rxd), -1.0f);
 			const float t0 = __fadd_rd(d, 8388608.0f);
 			const float k = d - (t0 - 8388608.0f);
 			const int i = __float_as_int(t0) - 0x4B000000;
 			if (active && static_cast<unsigned>(i) <= lastIdx) {
 				if (off >= 0) {
-					SP::accumulate(buf + (i - m.lo[w] + off), k, acc);
+					SP::accumulate(buf + (i - wm.y + off), k, acc);
 				} else if (off == kGlobalWindow) {
 					SP::accumulate(sig + t * txStride + static_cast<size_t>(r) * p.sigStride + i, k, acc);
 				}
@@ -307,7 +314,7 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 		}
 	}
 	if (ok && active) {
-		const float v = ANALYTIC ? sqrtf(total.x * total.x + total.y * total.y) : total.x;
+		const float v = ANALYTIC ? magnitude(total) : total.x;
 		p.value[pix] = v * p.valueCoef;
 		p.factor[pix] = cf.result(p.numRx, p, total);
 	}

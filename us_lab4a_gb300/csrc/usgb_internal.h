@@ -9,6 +9,7 @@ namespace usgb {
 
 constexpr int kPrepThreads = 512;
 constexpr int kMaxFFTStages = 24;
+constexpr unsigned kTwiddleSplit = 128;   // two-level twiddle tables: W^m = hi[m / 128] * lo[m % 128]
 
 // One launch of the signal-preparation kernel over `numSignals` A-scans.
 struct PrepParams {
@@ -20,15 +21,19 @@ struct PrepParams {
 	unsigned U;                  // upsampling factor (1: none)
 	unsigned L;                  // ns * U
 	unsigned tapsPerPhase;       // 2K + 1 (1 when U == 1)
-	const float* polyTaps;       // U x tapsPerPhase, polyTaps[r][t] = h[r + tU]
+	unsigned tapsStride;         // tapsPerPhase rounded up to a multiple of 4
+	const float* polyTaps;       // U x tapsStride, polyTaps[r][t] = h[r + tU] (zero padded)
 	unsigned deadZone;           // first sample of the DC mean
 	float outScale;              // applied before storage (1 for FP32)
 	// Hilbert FFT (analytic path): M = N/2 complex points.
 	unsigned M;
 	int numStages;
 	int radix[kMaxFFTStages];    // DIF order
-	const float2* tw;            // M entries, exp(-2 pi i m / M)
-	const float2* cs;            // M/2 + 1 entries, (cos, sin)(pi k / M)
+	unsigned long long divMagic[kMaxFFTStages];  // floor(b / sub_s) = (b * divMagic[s]) >> 40
+	const float2* tw;            // twLo (128) then twHi (ceil(M/128)): exp(-2 pi i m / M)
+	unsigned twHiCount;
+	const float2* cs;            // csLo (128) then csHi: (cos, sin)(pi k / M), k <= M/2
+	unsigned csHiCount;
 	const unsigned* perm;        // M entries, digit-reversed position of bin k
 };
 

@@ -11,18 +11,24 @@
 // after removeDC and uses the fixed 4x FIR of src/util/Interpolator4X.h.
 //
 // GB300 design:
-// * The FIR is evaluated directly in polyphase form (the zero-stuffed input
-//   has only ceil(taps/U) non-zero products per output), from the A-scan held
-//   in shared memory; the same linear convolution as the reference's FFT
-//   overlap-save.
+// * The FIR is evaluated directly in polyphase form: the FIR length is
+//   2UK + 1, so output n = bU + r depends on input samples b - K .. b + K
+//   only. A thread takes one input position b, keeps its 2K + 1 input samples
+//   in registers and produces all U phases from them, with the taps read as
+//   broadcast float4 loads from shared memory. This is the same linear
+//   convolution the reference computes with an FFT overlap-save filter.
 // * The N-point real FFT of the zero-padded signal is done as an N/2-point
 //   complex FFT of the even/odd-packed samples, in place in shared memory
 //   (mixed radix 2/3/4/5, decimation in frequency, output in digit-reversed
-//   order). The Hilbert multiplier -i*sgn(k) and the real-FFT split are folded
-//   into one pass over digit-reversed pairs (k, M-k), and the inverse is an
-//   in-place decimation-in-time FFT that consumes the digit-reversed order and
-//   returns the imaginary part y[2n] + i y[2n+1] in natural order.
-//   The real part of the analytic signal is the DC-free input itself.
+//   order; the packed buffer read as floats is the signal itself). The
+//   Hilbert multiplier -i*sgn(k) and the real-FFT split are folded into one
+//   pass over digit-reversed pairs (k, M-k), and the inverse is an in-place
+//   decimation-in-time FFT that consumes the digit-reversed order and returns
+//   the imaginary part y[n] in natural order. The real part of the analytic
+//   signal is the DC-free input itself, recomputed at store time.
+// * Twiddles come from two-level tables in shared memory
+//   (W^m = hi[m / 128] * lo[m % 128]); stage indices use multiply-shift
+//   division by host-computed constants.
 #include <cuda_runtime.h>
 
 #include "usgb_common.cuh"
@@ -102,17 +108,38 @@ template<int SIGN> struct SmallDFT<5, SIGN> {
 	}
 };
 
+// Bit patterns of one stored complex sample as 32-bit words (no address-of,
+// so the values stay in registers).
+__device__ __forceinline__ void sample_words(float2 c, unsigned* w) { w[0] = __float_as_uint(c.x); w[1] = __float_as_uint(c.y); }
+__device__ __forceinline__ void sample_words(__half2 c, unsigned* w)
+{
+	w[0] = static_cast<unsigned>(__half_as_ushort(__low2half(c))) |
+			(static_cast<unsigned>(__half_as_ushort(__high2half(c))) << 16);
+}
+__device__ __forceinline__ void sample_words(__nv_bfloat162 c, unsigned* w)
+{
+	w[0] = static_cast<unsigned>(__bfloat16_as_ushort(__low2bfloat16(c))) |
+			(static_cast<unsigned>(__bfloat16_as_ushort(__high2bfloat16(c))) << 16);
+}
+
+// W^m from the two-level table in shared memory.
+__device__ __forceinline__ float2 twiddle(const float2* lo, const float2* hi, unsigned m)
+{
+	return cmul(hi[m / kTwiddleSplit], lo[m % kTwiddleSplit]);
+}
+
 // One in-place stage over `data` (M points), blocks of span Ms, radix R.
 // Forward (DIF): DFT_R of the R inputs at stride Ms/R, then twiddle
 // W_Ms^(p j). Inverse (DIT, the transpose): conjugate twiddle, then DFT_R.
 template<int R, bool INVERSE>
-__device__ __forceinline__ void fft_stage(float2* data, const float2* __restrict__ tw, unsigned M, unsigned Ms)
+__device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, const float2* twHi, unsigned M,
+		unsigned Ms, unsigned long long magic)
 {
 	const unsigned sub = Ms / R;
 	const unsigned twStride = M / Ms;
 	const unsigned nb = M / R;
 	for (unsigned b = threadIdx.x; b < nb; b += blockDim.x) {
-		const unsigned blk = b / sub;
+		const unsigned blk = static_cast<unsigned>((static_cast<unsigned long long>(b) * magic) >> 40);
 		const unsigned j = b - blk * sub;
 		const unsigned base = blk * Ms + j;
 		float2 v[R];
@@ -120,11 +147,15 @@ __device__ __forceinline__ void fft_stage(float2* data, const float2* __restrict
 		for (int q = 0; q < R; ++q) v[q] = data[base + q * sub];
 		if (!INVERSE) {
 			SmallDFT<R, -1>::run(v);
+			if (j != 0) {
 #pragma unroll
-			for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(&tw[q * j * twStride]));
+				for (int q = 1; q < R; ++q) v[q] = cmul(v[q], twiddle(twLo, twHi, q * j * twStride));
+			}
 		} else {
+			if (j != 0) {
 #pragma unroll
-			for (int q = 1; q < R; ++q) v[q] = cmulc(v[q], __ldg(&tw[q * j * twStride]));
+				for (int q = 1; q < R; ++q) v[q] = cmulc(v[q], twiddle(twLo, twHi, q * j * twStride));
+			}
 			SmallDFT<R, +1>::run(v);
 		}
 #pragma unroll
@@ -133,49 +164,21 @@ __device__ __forceinline__ void fft_stage(float2* data, const float2* __restrict
 }
 
 template<bool INVERSE>
-__device__ void fft_run(float2* data, const PrepParams& p)
+__device__ void fft_run(float2* data, const PrepParams& p, const float2* twLo, const float2* twHi)
 {
-	if (!INVERSE) {
-		unsigned Ms = p.M;
-		for (int s = 0; s < p.numStages; ++s) {
-			switch (p.radix[s]) {
-			case 2: fft_stage<2, false>(data, p.tw, p.M, Ms); break;
-			case 3: fft_stage<3, false>(data, p.tw, p.M, Ms); break;
-			case 4: fft_stage<4, false>(data, p.tw, p.M, Ms); break;
-			default: fft_stage<5, false>(data, p.tw, p.M, Ms); break;
-			}
-			Ms /= p.radix[s];
-			__syncthreads();
+	unsigned spans[kMaxFFTStages];
+	unsigned Ms = p.M;
+	for (int s = 0; s < p.numStages; ++s) { spans[s] = Ms; Ms /= p.radix[s]; }
+	for (int i = 0; i < p.numStages; ++i) {
+		const int s = INVERSE ? p.numStages - 1 - i : i;
+		switch (p.radix[s]) {
+		case 2: fft_stage<2, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
+		case 3: fft_stage<3, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
+		case 4: fft_stage<4, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
+		default: fft_stage<5, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
 		}
-	} else {
-		// Spans of the forward stages, replayed in reverse order.
-		unsigned spans[kMaxFFTStages];
-		unsigned Ms = p.M;
-		for (int s = 0; s < p.numStages; ++s) { spans[s] = Ms; Ms /= p.radix[s]; }
-		for (int s = p.numStages - 1; s >= 0; --s) {
-			switch (p.radix[s]) {
-			case 2: fft_stage<2, true>(data, p.tw, p.M, spans[s]); break;
-			case 3: fft_stage<3, true>(data, p.tw, p.M, spans[s]); break;
-			case 4: fft_stage<4, true>(data, p.tw, p.M, spans[s]); break;
-			default: fft_stage<5, true>(data, p.tw, p.M, spans[s]); break;
-			}
-			__syncthreads();
-		}
+		__syncthreads();
 	}
-}
-
-// Upsampled sample n from the halo-padded A-scan in shared memory:
-// x[n] = sum_t h[r + tU] * rf[n/U + K - t], r = n mod U (the zero-stuffed
-// linear convolution shifted by (taps-1)/2 = U*K).
-__device__ __forceinline__ float upsampled(const float* rfs, const float* taps, unsigned n, unsigned U, unsigned nt)
-{
-	const unsigned b = n / U;
-	const unsigned r = n - b * U;
-	const float* h = taps + r * nt;
-	const float* src = rfs + b + (nt - 1);  // rfs index b + 2K - t, nt = 2K + 1
-	float acc = 0.f;
-	for (unsigned t = 0; t < nt; ++t) acc = fmaf(h[t], src[-static_cast<int>(t)], acc);
-	return acc;
 }
 
 __device__ float block_sum(float v, float* red)
@@ -196,65 +199,221 @@ __device__ float block_sum(float v, float* red)
 	return r;
 }
 
+// Shared-memory layout of the prep kernels (float offsets).
+struct PrepLayout {
+	unsigned data, rfs, taps, twLo, twHi, csLo, csHi, red, total;
+	__host__ __device__ PrepLayout(const PrepParams& p, bool analytic)
+	{
+		const unsigned K = (p.tapsPerPhase - 1) / 2;
+		data = 0;
+		rfs = analytic ? ((2 * p.M + 3) & ~3u) : 0;   // 16-byte aligned for float4 taps after it
+		taps = rfs + ((p.ns + 2 * K + 1 + 3) & ~3u);
+		twLo = taps + p.U * p.tapsStride;
+		twHi = twLo + (analytic ? 2 * kTwiddleSplit : 0);
+		csLo = twHi + (analytic ? 2 * p.twHiCount : 0);
+		csHi = csLo + (analytic ? 2 * kTwiddleSplit : 0);
+		red = csHi + (analytic ? 2 * p.csHiCount : 0);
+		total = red + 32;
+	}
+};
+
 // Loads the A-scan into shared memory with K zeros on each side (and one
-// spare zero at the end), and the polyphase taps.
-__device__ void load_ascan(const PrepParams& p, const float* __restrict__ rf, float* rfs, float* taps)
+// spare zero at the end), the polyphase taps and the twiddle tables.
+__device__ void load_inputs(const PrepParams& p, const PrepLayout& lay, float* sm, const float* __restrict__ rf,
+		bool analytic)
 {
 	const unsigned K = (p.tapsPerPhase - 1) / 2;
+	float* rfs = sm + lay.rfs;
 	const unsigned total = p.ns + 2 * K + 1;
 	for (unsigned i = threadIdx.x; i < total; i += blockDim.x) {
 		const int j = static_cast<int>(i) - static_cast<int>(K);
 		rfs[i] = (j >= 0 && j < static_cast<int>(p.ns)) ? __ldg(&rf[j]) : 0.f;
 	}
-	const unsigned ntaps = p.U * p.tapsPerPhase;
-	for (unsigned i = threadIdx.x; i < ntaps; i += blockDim.x) taps[i] = __ldg(&p.polyTaps[i]);
+	float* taps = sm + lay.taps;
+	for (unsigned i = threadIdx.x; i < p.U * p.tapsStride; i += blockDim.x) taps[i] = __ldg(&p.polyTaps[i]);
+	if (analytic) {
+		const unsigned ntw = 2 * (kTwiddleSplit + p.twHiCount);
+		const float* twg = reinterpret_cast<const float*>(p.tw);
+		for (unsigned i = threadIdx.x; i < ntw; i += blockDim.x) sm[lay.twLo + i] = __ldg(&twg[i]);
+		const unsigned ncs = 2 * (kTwiddleSplit + p.csHiCount);
+		const float* csg = reinterpret_cast<const float*>(p.cs);
+		for (unsigned i = threadIdx.x; i < ncs; i += blockDim.x) sm[lay.csLo + i] = __ldg(&csg[i]);
+	}
 	__syncthreads();
 }
 
-template<int S>
-__global__ void __launch_bounds__(kPrepThreads)
+// 16-byte shared-memory load the compiler may not hoist out of the sample
+// loop (hoisting all U x 28 taps would exhaust the registers).
+__device__ __forceinline__ float4 lds_taps(const float* p)
+{
+	float4 v;
+	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+			: "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(smem_addr(p)));
+	return v;
+}
+
+// The U upsampled outputs of input position b: x[bU + r] = sum_t h[r][t] *
+// rf[b + K - t] (rfs holds rf shifted by K).
+template<int NT, int U>
+__device__ __forceinline__ void fir_outputs(const float* rfs, const float* taps, unsigned b, float* out)
+{
+	constexpr int NTP = (NT + 3) & ~3;
+	float win[NTP];
+#pragma unroll
+	for (int t = 0; t < NT; ++t) win[t] = rfs[b + (NT - 1) - t];
+#pragma unroll
+	for (int t = NT; t < NTP; ++t) win[t] = 0.f;
+#pragma unroll
+	for (int r = 0; r < U; ++r) {
+		const float* h = taps + r * NTP;
+		float acc = 0.f;
+#pragma unroll
+		for (int q = 0; q < NTP / 4; ++q) {
+			const float4 c = lds_taps(h + 4 * q);
+			acc = fmaf(c.x, win[4 * q], acc);
+			if (4 * q + 1 < NT) acc = fmaf(c.y, win[4 * q + 1], acc);
+			if (4 * q + 2 < NT) acc = fmaf(c.z, win[4 * q + 2], acc);
+			if (4 * q + 3 < NT) acc = fmaf(c.w, win[4 * q + 3], acc);
+		}
+		out[r] = acc;
+	}
+}
+
+// Generic form (any FIR length and factor).
+__device__ __forceinline__ float fir_one(const float* rfs, const float* taps, unsigned n, unsigned U, unsigned nt,
+		unsigned stride)
+{
+	const unsigned b = n / U;
+	const unsigned r = n - b * U;
+	const float* h = taps + r * stride;
+	const float* src = rfs + b + (nt - 1);
+	float acc = 0.f;
+	for (unsigned t = 0; t < nt; ++t) acc = fmaf(h[t], src[-static_cast<int>(t)], acc);
+	return acc;
+}
+
+// Pass 1: x[n] for n < L into xs (float view), partial sum of [deadZone, L).
+template<int NT, int U>
+__device__ float fir_pass(const PrepParams& p, const float* rfs, const float* taps, float* xs)
+{
+	float part = 0.f;
+	if constexpr (NT > 0) {
+		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
+			float o[U];
+			fir_outputs<NT, U>(rfs, taps, b, o);
+#pragma unroll
+			for (int r = 0; r < U; ++r) {
+				if (b * U + r >= p.deadZone) part += o[r];
+			}
+			if (xs) {
+				if constexpr (U % 4 == 0) {
+#pragma unroll
+					for (int r = 0; r < U; r += 4) {
+						*reinterpret_cast<float4*>(xs + b * U + r) = make_float4(o[r], o[r + 1], o[r + 2], o[r + 3]);
+					}
+				} else {
+#pragma unroll
+					for (int r = 0; r < U; ++r) xs[b * U + r] = o[r];
+				}
+			}
+		}
+	} else {
+		for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
+			const float x = fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride);
+			if (n >= p.deadZone) part += x;
+			if (xs) xs[n] = x;
+		}
+	}
+	return part;
+}
+
+// Store pass: (x[n] - mean, y[n] / M) for n < L (analytic), or x[n] - mean (real).
+template<int S, bool ANALYTIC, int NT, int U>
+__device__ void store_pass(const PrepParams& p, const float* rfs, const float* taps, const float* ys, float mean,
+		unsigned a)
+{
+	const float invM = ANALYTIC ? 1.0f / static_cast<float>(p.M) : 0.f;
+	const float sc = p.outScale;
+	if (ANALYTIC) {
+		using CT = typename Complex<S>::T;
+		CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+		if constexpr (NT > 0) {
+			for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
+				float o[U];
+				fir_outputs<NT, U>(rfs, taps, b, o);
+				constexpr int perVec = 16 / static_cast<int>(sizeof(CT));  // samples per 16-byte store
+				if constexpr (U % perVec == 0) {
+#pragma unroll
+					for (int r0 = 0; r0 < U; r0 += perVec) {
+						unsigned w[4];
+#pragma unroll
+						for (int j = 0; j < perVec; ++j) {
+							const CT c = Complex<S>::pack((o[r0 + j] - mean) * sc, ys[b * U + r0 + j] * invM * sc);
+							sample_words(c, w + j * (sizeof(CT) / 4));
+						}
+						*reinterpret_cast<uint4*>(out + b * U + r0) = make_uint4(w[0], w[1], w[2], w[3]);
+					}
+				} else {
+#pragma unroll
+					for (int r = 0; r < U; ++r) {
+						out[b * U + r] = Complex<S>::pack((o[r] - mean) * sc, ys[b * U + r] * invM * sc);
+					}
+				}
+			}
+		} else {
+			for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
+				const float x = fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride);
+				out[n] = Complex<S>::pack((x - mean) * sc, ys[n] * invM * sc);
+			}
+		}
+	} else {
+		using RT = typename Real<S>::T;
+		RT* out = reinterpret_cast<RT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+		if constexpr (NT > 0) {
+			for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
+				float o[U];
+				fir_outputs<NT, U>(rfs, taps, b, o);
+#pragma unroll
+				for (int r = 0; r < U; ++r) out[b * U + r] = Real<S>::pack((o[r] - mean) * sc);
+			}
+		} else {
+			for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
+				out[n] = Real<S>::pack((fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride) - mean) * sc);
+			}
+		}
+	}
+}
+
+// NT = 0 selects the generic FIR loop.
+template<int S, int NT, int U>
+__global__ void __launch_bounds__(kPrepThreads, 1)
 prep_analytic_kernel(PrepParams p)
 {
-	extern __shared__ __align__(16) unsigned char smem[];
-	float2* data = reinterpret_cast<float2*>(smem);
-	float* rfs = reinterpret_cast<float*>(data + p.M);
-	const unsigned K = (p.tapsPerPhase - 1) / 2;
-	float* taps = rfs + (p.ns + 2 * K + 1);
-	float* red = taps + p.U * p.tapsPerPhase;
-
+	extern __shared__ __align__(16) float sm[];
+	const PrepLayout lay(p, true);
 	const unsigned a = blockIdx.x;
-	const float* rf = p.rf + static_cast<size_t>(a) * p.ns;
-	load_ascan(p, rf, rfs, taps);
-
+	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, true);
+	float2* data = reinterpret_cast<float2*>(sm + lay.data);
+	float* xs = sm + lay.data;  // the packed complex buffer read as floats: x[n] at n
+	const float* rfs = sm + lay.rfs;
+	const float* taps = sm + lay.taps;
+	const float2* twLo = reinterpret_cast<const float2*>(sm + lay.twLo);
+	const float2* twHi = reinterpret_cast<const float2*>(sm + lay.twHi);
+	const float2* csLo = reinterpret_cast<const float2*>(sm + lay.csLo);
+	const float2* csHi = reinterpret_cast<const float2*>(sm + lay.csHi);
 	const unsigned L = p.L;
-	const unsigned nt = p.tapsPerPhase;
-	// 1. Upsampled signal, packed z[n'] = x[2n'] + i x[2n'+1], zero past L.
-	float part = 0.f;
-	for (unsigned m = threadIdx.x; m < p.M; m += blockDim.x) {
-		const unsigned n0 = 2 * m, n1 = 2 * m + 1;
-		float x0 = 0.f, x1 = 0.f;
-		if (n0 < L) {
-			x0 = upsampled(rfs, taps, n0, p.U, nt);
-			if (n0 >= p.deadZone) part += x0;
-		}
-		if (n1 < L) {
-			x1 = upsampled(rfs, taps, n1, p.U, nt);
-			if (n1 >= p.deadZone) part += x1;
-		}
-		data[m] = make_float2(x0, x1);
-	}
-	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples.
-	const float mean = block_sum(part, red) / static_cast<float>(L - p.deadZone);
-	for (unsigned m = threadIdx.x; m < p.M; m += blockDim.x) {
-		float2 v = data[m];
-		if (2 * m < L) v.x -= mean;
-		if (2 * m + 1 < L) v.y -= mean;
-		data[m] = v;
-	}
+
+	// 1. Upsampled signal into the packed buffer, zero past L.
+	for (unsigned n = L + threadIdx.x; n < 2 * p.M; n += blockDim.x) xs[n] = 0.f;
+	const float part = fir_pass<NT, U>(p, rfs, taps, xs);
+	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
+	//    (block_sum's barriers also order the writes above).
+	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
+	for (unsigned n = threadIdx.x; n < L; n += blockDim.x) xs[n] -= mean;
 	__syncthreads();
 
 	// 3. Forward FFT (digit-reversed output).
-	fft_run<false>(data, p);
+	fft_run<false>(data, p, twLo, twHi);
 
 	// 4. Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
 	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0.
@@ -270,94 +429,79 @@ prep_analytic_kernel(PrepParams p)
 			const unsigned q1 = __ldg(&p.perm[k]);
 			const unsigned q2 = __ldg(&p.perm[p.M - k]);
 			const float2 A = data[q1], B = data[q2];
-			const float2 cs = __ldg(&p.cs[k]);
+			const float2 cs = cmul(csHi[k / kTwiddleSplit], csLo[k % kTwiddleSplit]);
 			data[q1] = make_float2(cs.x * B.x - cs.y * A.y, cs.y * A.x - cs.x * B.y);
 			data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
 		}
 	}
 	__syncthreads();
 
-	// 5. Inverse FFT (natural-order output w[n'] = M * (y[2n'] + i y[2n'+1])).
-	fft_run<true>(data, p);
+	// 5. Inverse FFT (natural-order output: y[n] * M at float index n).
+	fft_run<true>(data, p, twLo, twHi);
 
-	// 6. Store (x[n], y[n]) for n < L.
-	using CT = typename Complex<S>::T;
-	CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
-	const float invM = 1.0f / static_cast<float>(p.M);
-	const float sc = p.outScale;
-	for (unsigned m = threadIdx.x; 2 * m < L; m += blockDim.x) {
-		const float2 w = data[m];
-		const unsigned n0 = 2 * m;
-		const float x0 = upsampled(rfs, taps, n0, p.U, nt) - mean;
-		out[n0] = Complex<S>::pack(x0 * sc, w.x * invM * sc);
-		if (n0 + 1 < L) {
-			const float x1 = upsampled(rfs, taps, n0 + 1, p.U, nt) - mean;
-			out[n0 + 1] = Complex<S>::pack(x1 * sc, w.y * invM * sc);
-		}
-	}
+	// 6. Store (x[n] - mean, y[n]) for n < L; x is recomputed from the A-scan.
+	store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);
 }
 
 // Real-RF path: upsampling (fixed 4x FIR) and DC removal only.
-template<int S>
-__global__ void __launch_bounds__(kPrepThreads)
+template<int S, int NT, int U>
+__global__ void __launch_bounds__(kPrepThreads, 1)
 prep_real_kernel(PrepParams p)
 {
-	extern __shared__ __align__(16) unsigned char smem[];
-	float* rfs = reinterpret_cast<float*>(smem);
-	const unsigned K = (p.tapsPerPhase - 1) / 2;
-	float* taps = rfs + (p.ns + 2 * K + 1);
-	float* red = taps + p.U * p.tapsPerPhase;
+	extern __shared__ __align__(16) float sm[];
+	const PrepLayout lay(p, false);
 	const unsigned a = blockIdx.x;
-	load_ascan(p, p.rf + static_cast<size_t>(a) * p.ns, rfs, taps);
-	const unsigned L = p.L;
-	float part = 0.f;
-	for (unsigned n = p.deadZone + threadIdx.x; n < L; n += blockDim.x) {
-		part += upsampled(rfs, taps, n, p.U, p.tapsPerPhase);
+	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
+	const float part = fir_pass<NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr);
+	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
+	store_pass<S, false, NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr, mean, a);
+}
+
+template<int S, int NT, int U>
+cudaError_t launch_kernel(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
+{
+	const dim3 grid(p.numSignals), block(kPrepThreads);
+	cudaError_t e;
+	if (analytic) {
+		e = cudaFuncSetAttribute(prep_analytic_kernel<S, NT, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		prep_analytic_kernel<S, NT, U><<<grid, block, smem, stream>>>(p);
+	} else {
+		e = cudaFuncSetAttribute(prep_real_kernel<S, NT, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		prep_real_kernel<S, NT, U><<<grid, block, smem, stream>>>(p);
 	}
-	const float mean = block_sum(part, red) / static_cast<float>(L - p.deadZone);
-	using RT = typename Real<S>::T;
-	RT* out = reinterpret_cast<RT*>(p.out) + static_cast<size_t>(a) * p.outStride;
-	for (unsigned n = threadIdx.x; n < L; n += blockDim.x) {
-		out[n] = Real<S>::pack((upsampled(rfs, taps, n, p.U, p.tapsPerPhase) - mean) * p.outScale);
-	}
+	return cudaGetLastError();
+}
+
+template<int S>
+cudaError_t dispatch_fir(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
+{
+	// Specialised FIR shapes: the processors' Kaiser-sinc FIR (half transition
+	// 0.2) has 2K + 1 = 27 taps per phase for every factor; the fixed 4x FIR
+	// of the real path has 21; no upsampling is 1 tap.
+	if (p.tapsPerPhase == 27 && p.U == 8) return launch_kernel<S, 27, 8>(p, analytic, smem, stream);
+	if (p.tapsPerPhase == 27 && p.U == 4) return launch_kernel<S, 27, 4>(p, analytic, smem, stream);
+	if (p.tapsPerPhase == 21 && p.U == 4) return launch_kernel<S, 21, 4>(p, analytic, smem, stream);
+	if (p.tapsPerPhase == 1 && p.U == 1) return launch_kernel<S, 1, 1>(p, analytic, smem, stream);
+	return launch_kernel<S, 0, 1>(p, analytic, smem, stream);
 }
 
 }  // namespace
 
 size_t prep_smem_bytes(const PrepParams& p, bool analytic)
 {
-	const unsigned K = (p.tapsPerPhase - 1) / 2;
-	size_t b = (p.ns + 2 * K + 1) * sizeof(float) + p.U * p.tapsPerPhase * sizeof(float) + 32 * sizeof(float);
-	if (analytic) b += static_cast<size_t>(p.M) * sizeof(float2);
-	return b;
+	return static_cast<size_t>(PrepLayout(p, analytic).total) * sizeof(float);
 }
 
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream)
 {
 	const size_t smem = prep_smem_bytes(p, analytic);
-	const dim3 grid(p.numSignals), block(kPrepThreads);
-	cudaError_t e = cudaSuccess;
-#define USGB_LAUNCH_PREP(KERNEL, S)                                                               \
-	do {                                                                                          \
-		e = cudaFuncSetAttribute(KERNEL<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-		if (e != cudaSuccess) return e;                                                           \
-		KERNEL<S><<<grid, block, smem, stream>>>(p);                                              \
-	} while (0)
-	if (analytic) {
-		switch (storage) {
-		case STORE_F16: USGB_LAUNCH_PREP(prep_analytic_kernel, STORE_F16); break;
-		case STORE_BF16: USGB_LAUNCH_PREP(prep_analytic_kernel, STORE_BF16); break;
-		default: USGB_LAUNCH_PREP(prep_analytic_kernel, STORE_F32); break;
-		}
-	} else {
-		switch (storage) {
-		case STORE_F16: USGB_LAUNCH_PREP(prep_real_kernel, STORE_F16); break;
-		case STORE_BF16: USGB_LAUNCH_PREP(prep_real_kernel, STORE_BF16); break;
-		default: USGB_LAUNCH_PREP(prep_real_kernel, STORE_F32); break;
-		}
+	switch (storage) {
+	case STORE_F16: return dispatch_fir<STORE_F16>(p, analytic, smem, stream);
+	case STORE_BF16: return dispatch_fir<STORE_BF16>(p, analytic, smem, stream);
+	default: return dispatch_fir<STORE_F32>(p, analytic, smem, stream);
 	}
-#undef USGB_LAUNCH_PREP
-	return cudaGetLastError();
 }
 
 }  // namespace usgb
