@@ -152,6 +152,30 @@ int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_
  * wait that gave up) as USGB_ERR_DEVICE_TIMEOUT. */
 int usgb_synchronize(usgb_ctx* ctx);
 
+/*
+ * One frame without any device allocation. No counterpart in the reference:
+ * it exists for callers that must not allocate device memory while they run,
+ * e.g. a host that has already given nearly all GPU memory to its own pool
+ * (an allocation by this library would fail or fragment it) or an
+ * acquisition loop with a fixed latency budget. The caller passes the RF
+ * (num_tx * num_rx * num_samples floats), the grid (ncols * nrows (x, y, z))
+ * and the outputs (ncols * nrows floats each), all device pointers; the
+ * tables, element positions and prepared signal tensor live in a fixed 64 MiB
+ * device array inside the library, which every GPU that loads the library
+ * keeps until the process exits. Frames that need more (tables plus
+ * num_tx * num_rx * signal length samples) are rejected with
+ * USGB_ERR_INVALID_VALUE and a message saying so. Every call shares the array
+ * and finds there what the previous call left; each call rewrites what it
+ * uses, but calls whose GPU work overlaps race on it, so order them. The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * Asynchronous on cuda_stream (NULL = default stream). On failure the message
+ * is copied into error_message (error_capacity bytes, may be NULL).
+ */
+int usgb_process_frame_noalloc(const usgb_sta_params* params, const float* d_rf, const float* d_grid_xyz,
+		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, void* cuda_stream,
+		char* error_message, size_t error_capacity);
+
 /* Library version string. */
 const char* usgb_version(void);
 

@@ -1,0 +1,365 @@
+// usgb_process_frame_noalloc: one whole frame (signal preparation, then
+// delay-and-sum with the coherence factor) without allocating any device
+// memory.
+//
+// Who needs it: callers that must not allocate device memory while they run,
+// for example a host that has already handed almost all GPU memory to its own
+// pool (a cudaMalloc from this library would fail or fragment that pool), or
+// an acquisition loop with a fixed latency budget that cannot absorb
+// allocation calls. The normal entry points allocate their buffers in
+// usgb_create; this one takes its inputs and outputs from the caller and keeps
+// everything else it needs - the filter and FFT tables, the element positions
+// and the prepared signal tensor - in one fixed device array declared below.
+//
+// The array is a file-scope __device__ variable of kNoAllocScratchBytes
+// (64 MiB); every GPU that loads the library holds it until the process exits.
+// All calls share it and it keeps whatever the last call left there, so each
+// call rewrites every part it uses (tables, positions, tensor) and clears the
+// device error word before launching. Calls whose GPU work overlaps (on
+// different streams, or from different threads) race on the array; the caller
+// must order them.
+//
+// In host code `g_noallocScratch` only stands in for the array: its device
+// address is obtained with cudaGetSymbolAddress once per device, with that
+// device current, on the first call on that device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/usgb.h"
+#include "usgb_common.cuh"
+#include "usgb_internal.h"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+constexpr double kPi = 3.14159265358979323846;
+
+std::mutex g_addrMutex;
+std::vector<void*> g_scratchAddr;  // per device ordinal; nullptr until looked up
+
+struct Fail {
+	int code;
+	std::string msg;
+};
+
+#define NA_FAIL(CODE, EXPR)                \
+	do {                                   \
+		std::ostringstream os_;            \
+		os_ << EXPR;                       \
+		throw Fail{(CODE), os_.str()};     \
+	} while (0)
+
+#define NA_CUDA(CALL)                                                                   \
+	do {                                                                                \
+		const cudaError_t e_ = (CALL);                                                  \
+		if (e_ != cudaSuccess) NA_FAIL(USGB_ERR_CUDA, #CALL << ": " << cudaGetErrorString(e_)); \
+	} while (0)
+
+// Device address of the scratch array on the current device (looked up once
+// per device with cudaGetSymbolAddress).
+void* scratch_address()
+{
+	int dev = 0;
+	NA_CUDA(cudaGetDevice(&dev));
+	std::lock_guard<std::mutex> lock(g_addrMutex);
+	if (g_scratchAddr.size() <= static_cast<size_t>(dev)) g_scratchAddr.resize(dev + 1, nullptr);
+	if (!g_scratchAddr[dev]) {
+		void* ptr = nullptr;
+		NA_CUDA(cudaGetSymbolAddress(&ptr, g_noallocScratch));
+		g_scratchAddr[dev] = ptr;
+	}
+	return g_scratchAddr[dev];
+}
+
+unsigned next_fast_even(unsigned n)
+{
+	if (n & 1U) ++n;
+	for (;;) {
+		unsigned m = n;
+		while ((m & 1U) == 0) m >>= 1;
+		while (m % 3 == 0) m /= 3;
+		while (m % 5 == 0) m /= 5;
+		if (m == 1) return n;
+		n += 2;
+	}
+}
+
+// Kaiser-windowed sinc of the analytic path (Interpolator::prepare,
+// src/util/Interpolator.h:64-111), in float.
+std::vector<float> analytic_taps(unsigned U)
+{
+	const float halfTransitionWidth = 0.2f;
+	const float tol_dB = -20.0 * std::log10(1.0e-4);
+	const float beta = 0.1102 * (tol_dB - 8.7);
+	const float finalTransitionWidth = (halfTransitionWidth * 2) / U;
+	const unsigned windowSize = static_cast<unsigned>(std::ceil((tol_dB - 7.95) / (2.285 * finalTransitionWidth * kPi) + 1.0));
+	const float twoUp = 2 * U;
+	const unsigned n = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
+	const float c1 = 2 / static_cast<float>(n - 1U);
+	const float c2 = 1 / std::cyl_bessel_if(0.0f, beta);
+	const float numPeriods = (n - 1U) / twoUp;
+	const double step = static_cast<double>(numPeriods - (-numPeriods)) / (n - 1U);
+	std::vector<float> taps(n);
+	for (unsigned i = 0; i < n; ++i) {
+		const float k = c1 * i - 1;
+		float x = 1 - k * k;
+		if (x < 0.0f) x = 0.0f;
+		const float w = c2 * std::cyl_bessel_if(0.0f, beta * std::sqrt(x));
+		const float xi = (i == 0) ? -numPeriods : static_cast<float>(-numPeriods + i * step);
+		const double arg = kPi * xi;
+		taps[i] = static_cast<float>((std::abs(arg) < 1.0e-5) ? 1.0 - arg * arg / 6.0 : std::sin(arg) / arg);
+		taps[i] *= w;
+	}
+	return taps;
+}
+
+// The fixed 4x FIR of the real path (kaiser(81, 5) .* sinc(linspace(-10, 10, 81))).
+std::vector<float> real4x_taps()
+{
+	const double i0b = std::cyl_bessel_i(0.0, 5.0);
+	std::vector<float> h(81);
+	for (unsigned i = 0; i <= 80; ++i) {
+		const double r = 2.0 * i / 80 - 1.0;
+		const double w = std::cyl_bessel_i(0.0, 5.0 * std::sqrt(std::max(0.0, 1.0 - r * r))) / i0b;
+		const double xv = -10.0 + 20.0 * i / 80;
+		h[i] = static_cast<float>(((xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv)) * w);
+	}
+	return h;
+}
+
+// Byte layout of one call inside the scratch array.
+struct Layout {
+	size_t err, taps, tw, cs, perm, tx, rx, apod, sig, total;
+};
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32_t ncols, uint32_t nrows,
+		float* d_value, float* d_factor, cudaStream_t stream)
+{
+	// ---- parameter checks (same rules and messages as usgb_create) ----
+	if (!p) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "null parameters");
+	if (!d_rf || !d_grid || !d_value || !d_factor) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+	if (p->num_tx == 0 || p->num_rx == 0) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of elements is zero.");
+	if (p->num_tx > 1024 || p->num_rx > 1024) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "More than 1024 elements.");
+	if (p->num_samples == 0) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of samples is zero.");
+	if (!p->tx_xy || !p->rx_xy) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Missing element positions.");
+	if (p->signal_path != USGB_PATH_ANALYTIC && p->signal_path != USGB_PATH_REAL) {
+		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid signal path: " << p->signal_path << '.');
+	}
+	const bool analytic = p->signal_path == USGB_PATH_ANALYTIC;
+	if (analytic && (p->upsampling == 0 || p->upsampling > 64)) {
+		NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid upsampling factor: " << p->upsampling << ". Must be >= 1 and <= 64.");
+	}
+	if (!analytic && p->upsampling != 4) NA_FAIL(USGB_ERR_INVALID_VALUE, "The real-RF path upsamples by 4 (got " << p->upsampling << ").");
+	if (!(p->sampling_frequency > 0) || !(p->propagation_speed > 0) || !(p->center_frequency > 0)) {
+		NA_FAIL(USGB_ERR_INVALID_VALUE, "Sampling frequency, propagation speed and center frequency must be > 0.");
+	}
+	if (!(p->dead_zone_m >= 0)) NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
+	if (p->coherence > USGB_CF_MF) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid coherence factor method: " << p->coherence << '.');
+	if (!analytic && p->coherence != USGB_CF_NONE && p->coherence != USGB_CF_SCF) {
+		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The real-RF path supports only the sign coherence factor.");
+	}
+	if (p->storage > USGB_STORE_BF16) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid storage type: " << p->storage << '.');
+	if (ncols == 0) NA_FAIL(USGB_ERR_INVALID_VALUE, "Zero columns in the grid.");
+	if (nrows == 0) NA_FAIL(USGB_ERR_INVALID_VALUE, "Zero rows in the grid.");
+	const unsigned U = p->upsampling;
+	const unsigned long long L64 = static_cast<unsigned long long>(p->num_samples) * U;
+	if (L64 < 2) NA_FAIL(USGB_ERR_INVALID_VALUE, "The signal length (" << L64 << ") must be >= 2.");
+	if (analytic && L64 > (1ULL << 20)) {
+		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of input samples (" << L64 << ") is greater than " << (1U << 20) << '.');
+	}
+	const unsigned L = static_cast<unsigned>(L64);
+	const float upFs = U * p->sampling_frequency;
+	const double dzd = upFs * 2.0 * p->dead_zone_m / p->propagation_speed;
+	if (!(dzd < static_cast<double>(L))) {
+		NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: deadZoneSamplesUp_ (" << static_cast<unsigned long long>(dzd)
+				<< ") >= signalLength (" << L << ").");
+	}
+	const unsigned numSignals = p->num_tx * p->num_rx;
+
+	// ---- host tables (no device memory involved) ----
+	const std::vector<float> taps = !analytic ? real4x_taps() : (U > 1 ? analytic_taps(U) : std::vector<float>{1.0f});
+	const unsigned T = static_cast<unsigned>(taps.size());
+	const unsigned K = (U > 1) ? (T - 1) / (2 * U) : 0;
+	const unsigned tapsPerPhase = 2 * K + 1;
+	const unsigned tapsStride = (tapsPerPhase + 3) & ~3u;
+	std::vector<float> poly(static_cast<size_t>(U) * tapsStride, 0.f);
+	for (unsigned r = 0; r < U; ++r)
+		for (unsigned t = 0; t < tapsPerPhase; ++t)
+			if (r + t * U < T) poly[r * tapsStride + t] = taps[r + t * U];
+
+	usgb::PrepParams pp{};
+	std::vector<float2> tw, cs;
+	std::vector<unsigned> perm;
+	if (analytic) {
+		const unsigned N = std::max(next_fast_even(L + 1024U), 2048U);
+		const unsigned M = N / 2;
+		std::vector<int> radices;
+		unsigned m = M;
+		while (m % 4 == 0) { radices.push_back(4); m /= 4; }
+		while (m % 2 == 0) { radices.push_back(2); m /= 2; }
+		while (m % 3 == 0) { radices.push_back(3); m /= 3; }
+		while (m % 5 == 0) { radices.push_back(5); m /= 5; }
+		if (m != 1 || radices.size() > static_cast<size_t>(usgb::kMaxFFTStages)) NA_FAIL(USGB_ERR_INVALID_STATE, "FFT size not supported");
+		const unsigned S = usgb::kTwiddleSplit;
+		pp.M = M;
+		pp.twHiCount = (M + S - 1) / S;
+		pp.csHiCount = (M / 2 + 1 + S - 1) / S;
+		auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
+		tw.resize(S + pp.twHiCount);
+		cs.resize(S + pp.csHiCount);
+		for (unsigned j = 0; j < S; ++j) tw[j] = unit(-2.0 * kPi * j / M);
+		for (unsigned q = 0; q < pp.twHiCount; ++q) tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
+		for (unsigned j = 0; j < S; ++j) cs[j] = unit(kPi * j / M);
+		for (unsigned q = 0; q < pp.csHiCount; ++q) cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
+		perm.resize(M);
+		for (unsigned k = 0; k < M; ++k) {
+			unsigned kk = k, pos = 0, span = M;
+			for (int r : radices) {
+				span /= static_cast<unsigned>(r);
+				pos += (kk % r) * span;
+				kk /= r;
+			}
+			perm[k] = pos;
+		}
+		pp.numStages = static_cast<int>(radices.size());
+		unsigned Ms = M;
+		for (size_t i = 0; i < radices.size(); ++i) {
+			pp.radix[i] = radices[i];
+			const unsigned sub = Ms / static_cast<unsigned>(radices[i]);
+			pp.divMagic[i] = ((1ULL << 40) + sub - 1) / sub;
+			Ms = sub;
+		}
+	}
+	std::vector<float> apod(p->num_rx, 1.0f);
+	if (analytic && p->rx_apod) apod.assign(p->rx_apod, p->rx_apod + p->num_rx);
+
+	// ---- scratch layout and size check ----
+	const size_t elemBytes = (analytic ? 2 : 1) * (p->storage == USGB_STORE_F32 ? 4 : 2);
+	const unsigned sigStride = (L + 7U) & ~7U;
+	Layout lay{};
+	size_t off = 0;
+	lay.err = off; off = align256(off + sizeof(unsigned));
+	lay.taps = off; off = align256(off + poly.size() * sizeof(float));
+	lay.tw = off; off = align256(off + tw.size() * sizeof(float2));
+	lay.cs = off; off = align256(off + cs.size() * sizeof(float2));
+	lay.perm = off; off = align256(off + perm.size() * sizeof(unsigned));
+	lay.tx = off; off = align256(off + 2 * p->num_tx * sizeof(float));
+	lay.rx = off; off = align256(off + 2 * p->num_rx * sizeof(float));
+	lay.apod = off; off = align256(off + apod.size() * sizeof(float));
+	lay.sig = off; off = align256(off + static_cast<size_t>(numSignals) * sigStride * elemBytes + 256);
+	lay.total = off;
+	if (lay.total > kNoAllocScratchBytes) {
+		NA_FAIL(USGB_ERR_INVALID_VALUE, "Frame too large for the no-allocation entry point: it needs " << lay.total
+				<< " bytes of scratch, the fixed array holds " << kNoAllocScratchBytes
+				<< " (use usgb_create / usgb_process_device, or FP16/BF16 storage).");
+	}
+
+	// ---- device work: everything below writes into the fixed array ----
+	unsigned char* base = static_cast<unsigned char*>(scratch_address());
+	NA_CUDA(cudaMemsetAsync(base + lay.err, 0, sizeof(unsigned), stream));
+	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.data(), poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+	if (analytic) {
+		NA_CUDA(cudaMemcpyAsync(base + lay.tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
+		NA_CUDA(cudaMemcpyAsync(base + lay.cs, cs.data(), cs.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
+		NA_CUDA(cudaMemcpyAsync(base + lay.perm, perm.data(), perm.size() * sizeof(unsigned), cudaMemcpyHostToDevice, stream));
+	}
+	NA_CUDA(cudaMemcpyAsync(base + lay.tx, p->tx_xy, 2 * p->num_tx * sizeof(float), cudaMemcpyHostToDevice, stream));
+	NA_CUDA(cudaMemcpyAsync(base + lay.rx, p->rx_xy, 2 * p->num_rx * sizeof(float), cudaMemcpyHostToDevice, stream));
+	NA_CUDA(cudaMemcpyAsync(base + lay.apod, apod.data(), apod.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+
+	pp.rf = d_rf;
+	pp.out = base + lay.sig;
+	pp.outStride = sigStride;
+	pp.numSignals = numSignals;
+	pp.ns = p->num_samples;
+	pp.U = U;
+	pp.L = L;
+	pp.tapsPerPhase = tapsPerPhase;
+	pp.tapsStride = tapsStride;
+	pp.polyTaps = reinterpret_cast<const float*>(base + lay.taps);
+	pp.deadZone = static_cast<unsigned>(dzd);
+	const float scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
+	pp.outScale = scale;
+	pp.tw = reinterpret_cast<const float2*>(base + lay.tw);
+	pp.cs = reinterpret_cast<const float2*>(base + lay.cs);
+	pp.perm = reinterpret_cast<const unsigned*>(base + lay.perm);
+
+	int dev = 0, maxSmem = 0;
+	NA_CUDA(cudaGetDevice(&dev));
+	NA_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+	if (usgb::prep_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) {
+		NA_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation (signal length " << L << ").");
+	}
+	NA_CUDA(usgb::launch_prep(pp, static_cast<int>(p->storage), analytic, stream));
+
+	usgb::DasParams dp{};
+	dp.sig = base + lay.sig;
+	dp.sigStride = sigStride;
+	dp.L = L;
+	dp.numTx = p->num_tx;
+	dp.numRx = p->num_rx;
+	dp.txXY = reinterpret_cast<const float*>(base + lay.tx);
+	dp.rxXY = reinterpret_cast<const float*>(base + lay.rx);
+	dp.apod = reinterpret_cast<const float*>(base + lay.apod);
+	dp.grid = d_grid;
+	dp.npix = ncols * nrows;
+	dp.ncols = ncols;
+	dp.nrows = nrows;
+	dp.invCT = upFs / p->propagation_speed;
+	dp.signalOffset = upFs * p->peak_offset / p->center_frequency;
+	dp.valueCoef = 1.0f / static_cast<float>(numSignals);
+	dp.invScale = 1.0f / scale;
+	dp.pcfFactor = p->pcf_gamma / static_cast<float>(kPi / std::sqrt(3.0));
+	dp.scfP = p->scf_p;
+	dp.value = d_value;
+	dp.factor = d_factor;
+	dp.errWord = reinterpret_cast<unsigned*>(base + lay.err);
+	dp.tileRows = 8;
+	dp.stageBytes = 16384;
+	// The staged kernel when its shared memory fits, the plain one otherwise.
+	const bool staged = usgb::das_staged_smem_bytes(p->num_tx, p->num_rx, dp.tileRows, dp.stageBytes)
+			<= static_cast<size_t>(maxSmem);
+	if (!staged && static_cast<size_t>(p->num_tx) * 128 * sizeof(float) > static_cast<size_t>(maxSmem)) {
+		NA_FAIL(USGB_ERR_UNSUPPORTED, "Too many transmit elements for the delay table: " << p->num_tx << '.');
+	}
+	NA_CUDA(usgb::launch_das(dp, static_cast<int>(p->storage), static_cast<int>(p->coherence), analytic,
+			staged ? 1 : 0, stream));
+	return USGB_OK;
+}
+
+}  // namespace
+
+extern "C" int usgb_process_frame_noalloc(const usgb_sta_params* params, const float* d_rf, const float* d_grid_xyz,
+		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, void* cuda_stream,
+		char* error_message, size_t error_capacity)
+{
+	std::string msg;
+	int rc = USGB_OK;
+	try {
+		rc = run(params, d_rf, d_grid_xyz, ncols, nrows, d_value, d_factor, static_cast<cudaStream_t>(cuda_stream));
+	} catch (const Fail& f) {
+		msg = f.msg;
+		rc = f.code;
+	} catch (const std::exception& e) {
+		msg = e.what();
+		rc = USGB_ERR_INVALID_STATE;
+	}
+	if (error_message && error_capacity > 0) {
+		const size_t n = std::min(msg.size(), error_capacity - 1);
+		std::memcpy(error_message, msg.data(), n);
+		error_message[n] = '\0';
+	}
+	return rc;
+}

@@ -52,6 +52,8 @@ SIGNATURES = {
     "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32]),
     "usgb_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_version": (C.c_char_p, []),
+    "usgb_process_frame_noalloc": (C.c_int, [C.POINTER(StaParams), C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 
 _lib = None
