@@ -203,8 +203,10 @@ def run_gpu(args):
     frame, desc = _workload(args.workload, args.storage)
     spec = frame.spec
     eng = StaEngine(spec)
-    if args.das == "staged":
-        eng.set_das_variant(1, args.tile_rows, args.stage_bytes)
+    if args.das == "plain":
+        eng.set_das_variant(0)
+    elif not args.autotune:
+        eng.set_das_variant(1, args.tile_rows, args.stage_bytes, args.stages)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream)
     with torch.cuda.stream(stream):
@@ -216,6 +218,13 @@ def run_gpu(args):
     stream.synchronize()
     eng.set_grid_device(grid)
     info = eng.signal_info()
+    if args.das == "staged" and args.autotune:
+        # Pick the staged kernel's tile / stage shape on this frame (untimed).
+        sig_t = torch.empty(info["signal_bytes"] // 4 + 1, dtype=torch.float32, device=dev)
+        eng.prepare_signals_device(rf0, sig_t)
+        eng.autotune_das(sig_t, value, factor, iterations=2)
+        del sig_t
+    das_cfg = eng.das_config()
 
     def step(i):
         eng.process_device(rfs[i % len(rfs)], value, factor)
@@ -317,7 +326,9 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": spec.storage if spec.storage != "f32" else "f32",
             "data": "synthetic (seeded point + speckle scatterers)",
-            "config": {"workload": desc, "storage": spec.storage, "das_kernel": args.das + (f" (tile 32x{args.tile_rows}, {args.stage_bytes} B stages)" if args.das == "staged" else ""),
+            "config": {"workload": desc, "storage": spec.storage, "das_kernel": ("plain" if das_cfg["variant"] == 0 else
+                           f"staged (tile 32x{das_cfg['tile_rows']}, {das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
+                           + (", autotuned)" if args.autotune else ")")),
                        "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
                        "parallelism": f"replicas x{world}"},
             "voxels_per_s": fps * frame.npix,
@@ -346,6 +357,8 @@ def main():
     ap.add_argument("--das", default="staged", choices=["plain", "staged"])
     ap.add_argument("--tile-rows", type=int, default=8)
     ap.add_argument("--stage-bytes", type=int, default=16384)
+    ap.add_argument("--stages", type=int, default=8)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -143,10 +143,19 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
 
 /* Selects the delay-and-sum kernel: 0 = plain (one thread per point, gathers
  * from global memory), 1 = staged (per tile of 32 columns x tile_rows rows,
- * the A-scan windows the tile needs are bulk-copied into shared memory,
- * stage_bytes per pipeline stage). 0 for tile_rows / stage_bytes keeps the
- * current value. */
-int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes);
+ * the A-scan windows the tile needs are bulk-copied into a shared-memory ring
+ * of `stages` stages of stage_bytes each). 0 for tile_rows / stage_bytes /
+ * stages keeps the current value. New contexts start with the staged kernel
+ * at the deepest ring that fits in shared memory. */
+int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
+int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
+		uint32_t* stages);
+
+/* Times every staged configuration that fits (tile rows x stage bytes x
+ * stages, plus the plain kernel) on the given prepared signals, `iterations`
+ * runs each, keeps the fastest on the context and returns its time. */
+int usgb_autotune_das(usgb_ctx* ctx, const void* d_signals, float* d_value, float* d_factor, uint32_t iterations,
+		float* best_ms);
 
 /* Waits for the context's stream and reports a device-side error (a bounded
  * wait that gave up) as USGB_ERR_DEVICE_TIMEOUT. */
@@ -175,6 +184,33 @@ int usgb_synchronize(usgb_ctx* ctx);
 int usgb_process_frame_noalloc(const usgb_sta_params* params, const float* d_rf, const float* d_grid_xyz,
 		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, void* cuda_stream,
 		char* error_message, size_t error_capacity);
+
+/*
+ * Batches: many frames (different element counts, sample counts, grids and
+ * coherence factors; one storage type and signal path) in two persistent
+ * launches, one over every A-scan of every frame (preparation) and one over
+ * every grid tile of every frame (staged delay-and-sum). Each frame is a
+ * context (geometry, tables, grid, signal tensor) plus its device RF and
+ * outputs. Frame descriptors are copied to the device at each run, so with
+ * use_graph the two launches are captured once into a CUDA graph and the
+ * graph is replayed for every later batch (re-captured only when a batch
+ * needs more shared memory than the captured one). A batch object may have
+ * one run in flight; usgb_batch_run waits for the previous run's descriptor
+ * copy before refilling its descriptors.
+ */
+typedef struct usgb_batch usgb_batch;
+typedef struct usgb_batch_item {
+	usgb_ctx* ctx;          /* frame: parameters, tables, grid, signal tensor */
+	const float* d_rf;      /* device RF, num_tx * num_rx * num_samples */
+	float* d_value;         /* device outputs, ncols * nrows each */
+	float* d_factor;
+} usgb_batch_item;
+int usgb_batch_create(uint32_t max_frames, uint32_t max_elements, uint32_t max_signal_length, usgb_batch** batch);
+void usgb_batch_destroy(usgb_batch* batch);
+const char* usgb_batch_last_error(const usgb_batch* batch);
+int usgb_batch_set_das_config(usgb_batch* batch, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
+int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
+int usgb_batch_synchronize(usgb_batch* batch);
 
 /* Library version string. */
 const char* usgb_version(void);

@@ -112,6 +112,7 @@ public:
 		}
 		// Per-stage twiddles w_{l p}^{q k}, k < l, q < p.
 		tw_.clear();
+		twInv_.clear();
 		stageOffset_.clear();
 		unsigned l = 1;
 		for (unsigned p : radices_) {
@@ -121,6 +122,7 @@ public:
 					const double a = -2.0 * kPi * static_cast<double>(q) * static_cast<double>(k) /
 							static_cast<double>(l * p);
 					tw_.emplace_back(static_cast<T>(std::cos(a)), static_cast<T>(std::sin(a)));
+					twInv_.emplace_back(static_cast<T>(std::cos(a)), -static_cast<T>(std::sin(a)));
 				}
 			}
 			l *= p;
@@ -141,24 +143,13 @@ public:
 		for (std::size_t s = 0; s < radices_.size(); ++s) {
 			const unsigned p = radices_[s];
 			const unsigned m = n_ / (l * p);
-			const C* tw = tw_.data() + stageOffset_[s];
-			for (unsigned r = 0; r < m; ++r) {
-				for (unsigned k = 0; k < l; ++k) {
-					C v[64];
-					C* vv = v;
-					std::vector<C> big;
-					if (p > 64) { big.resize(p); vv = big.data(); }
-					for (unsigned q = 0; q < p; ++q) {
-						C t = x[k + l * (r + q * m)];
-						C w = tw[k * p + q];
-						if (sign > 0) w = std::conj(w);
-						vv[q] = (q == 0) ? t : t * w;
-					}
-					butterfly(vv, p, sign);
-					for (unsigned q = 0; q < p; ++q) {
-						y[k + l * q + l * p * r] = vv[q];
-					}
-				}
+			const C* tw = (sign > 0 ? twInv_.data() : tw_.data()) + stageOffset_[s];
+			switch (p) {
+			case 2: stage<2>(x, y, tw, l, m, sign); break;
+			case 3: stage<3>(x, y, tw, l, m, sign); break;
+			case 4: stage<4>(x, y, tw, l, m, sign); break;
+			case 5: stage<5>(x, y, tw, l, m, sign); break;
+			default: stage_generic(x, y, tw, p, l, m, sign); break;
 			}
 			std::swap(x, y);
 			l *= p;
@@ -167,6 +158,35 @@ public:
 	}
 
 private:
+	// One Stockham stage of radix P: y[k + l q + l P r] = DFT_P over q of
+	// x[k + l (r + q m)] * w_{lP}^{q k}.
+	template<unsigned P>
+	static void stage(const C* x, C* y, const C* tw, unsigned l, unsigned m, int sign)
+	{
+		for (unsigned r = 0; r < m; ++r) {
+			for (unsigned k = 0; k < l; ++k) {
+				C v[P];
+				v[0] = x[k + l * r];
+				for (unsigned q = 1; q < P; ++q) v[q] = x[k + l * (r + q * m)] * tw[k * P + q];
+				butterfly(v, P, sign);
+				for (unsigned q = 0; q < P; ++q) y[k + l * q + l * P * r] = v[q];
+			}
+		}
+	}
+
+	static void stage_generic(const C* x, C* y, const C* tw, unsigned p, unsigned l, unsigned m, int sign)
+	{
+		std::vector<C> v(p);
+		for (unsigned r = 0; r < m; ++r) {
+			for (unsigned k = 0; k < l; ++k) {
+				v[0] = x[k + l * r];
+				for (unsigned q = 1; q < p; ++q) v[q] = x[k + l * (r + q * m)] * tw[k * p + q];
+				butterfly(v.data(), p, sign);
+				for (unsigned q = 0; q < p; ++q) y[k + l * q + l * p * r] = v[q];
+			}
+		}
+	}
+
 	static void butterfly(C* v, unsigned p, int sign)
 	{
 		const T s = static_cast<T>(sign);
@@ -229,7 +249,7 @@ private:
 	unsigned n_ = 0;
 	std::vector<unsigned> radices_;
 	std::vector<unsigned> stageOffset_;
-	std::vector<C> tw_;
+	std::vector<C> tw_, twInv_;
 	std::vector<C> work_;
 	std::vector<C> bufA_, bufB_;
 };
@@ -358,14 +378,18 @@ void upsample(const T* in, unsigned len, unsigned U, const std::vector<T>& taps,
 	for (long n = 0; n < L; ++n) {
 		const long j = n + off;  // index into the full convolution
 		T acc = 0;
-		// out[n] = sum_m taps[m] * up[j - m], up[i] = in[i / U] if i % U == 0.
-		long mStart = j % U;  // smallest m with (j - m) % U == 0
-		for (long m = mStart; m < ntaps; m += U) {
-			const long src = (j - m) / U;
-			if (src < 0) break;
-			if (src >= static_cast<long>(len)) continue;
-			acc += taps[m] * in[src];
+		// out[n] = sum_m taps[m] * up[j - m], up[i] = in[i / U] if i % U == 0:
+		// m runs over j % U, j % U + U, ... (ascending), source index (j - m) / U.
+		const long m0 = j % U;
+		long src = (j - m0) / U;
+		// Skip taps whose source lies past the end of the input.
+		long m = m0;
+		if (src >= static_cast<long>(len)) {
+			const long skip = src - static_cast<long>(len) + 1;
+			m += skip * U;
+			src -= skip;
 		}
+		for (; m < ntaps && src >= 0; m += U, --src) acc += taps[m] * in[src];
 		out[n] = acc;
 	}
 }
@@ -382,9 +406,9 @@ void remove_dc(T* data, std::size_t size, std::size_t beginOffset)
 	for (std::size_t i = 0; i < size; ++i) data[i] += term;
 }
 
-// Analytic signal by FFT: zero-pad to N, forward FFT, halve bins 0 and N/2,
-// zero bins N/2+1..N-1, backward FFT, scale 2/N, keep the first `len`.
-// Follows src/util/HilbertEnvelope.h:142-197 and :227-251.
+// Analytic signal by FFT: zero-pad to N, forward real FFT, halve bins 0 and
+// N/2, zero bins N/2+1..N-1, backward complex FFT, scale 2/N, keep the first
+// `len`. Follows src/util/HilbertEnvelope.h:142-197 and :227-251.
 template<typename T>
 class Hilbert {
 public:
@@ -393,20 +417,45 @@ public:
 	{
 		if (len == 0 || len > (1U << 20)) throw std::invalid_argument("invalid Hilbert input size");
 		const unsigned N = hilbert_fft_size(len);
-		if (fft_.size() != N) fft_.init(N);
+		const unsigned M = N / 2;
+		if (fft_.size() != N) {
+			fft_.init(N);
+			half_.init(M);
+			wN_.resize(M + 1);
+			for (unsigned k = 0; k <= M; ++k) {
+				const double a = -2.0 * kPi * static_cast<double>(k) / N;
+				wN_[k] = C(static_cast<T>(std::cos(a)), static_cast<T>(std::sin(a)));
+			}
+		}
+		// Forward real FFT of the zero-padded signal (FFTW's r2c computes the
+		// same bins): an M-point complex FFT of z[n] = x[2n] + i x[2n+1] and
+		// X[k] = E[k] + W_N^k O[k], E = (Z[k] + conj Z[M-k]) / 2,
+		// O = (Z[k] - conj Z[M-k]) / 2i, for k = 0..M.
+		z_.assign(M, C(0));
+		for (unsigned i = 0; i < len; ++i) {
+			if (i & 1U) z_[i / 2] = C(z_[i / 2].real(), x[i]);
+			else z_[i / 2] = C(x[i], z_[i / 2].imag());
+		}
+		half_.execute(z_.data(), z_.data(), -1);
 		buf_.assign(N, C(0));
-		for (unsigned i = 0; i < len; ++i) buf_[i] = C(x[i], 0);
-		fft_.execute(buf_.data(), buf_.data(), -1);
+		for (unsigned k = 0; k <= M; ++k) {
+			const C a = z_[k % M];
+			const C b = std::conj(z_[(M - k) % M]);
+			const C e = (a + b) * static_cast<T>(0.5);
+			const C o = (a - b) * C(0, static_cast<T>(-0.5));
+			buf_[k] = e + wN_[k] * o;
+		}
+		// HilbertEnvelope::process: halve bins 0 and N/2, zero the negative
+		// frequencies (already zero), backward FFT, scale 2/N.
 		buf_[0] = C(buf_[0].real() * static_cast<T>(0.5), buf_[0].imag());
-		buf_[N / 2] = C(buf_[N / 2].real() * static_cast<T>(0.5), buf_[N / 2].imag());
-		for (unsigned k = N / 2 + 1; k < N; ++k) buf_[k] = C(0);
+		buf_[M] = C(buf_[M].real() * static_cast<T>(0.5), buf_[M].imag());
 		fft_.execute(buf_.data(), buf_.data(), +1);
 		const T coef = 2 / static_cast<T>(N);
 		for (unsigned i = 0; i < len; ++i) out[i] = C(coef * buf_[i].real(), coef * buf_[i].imag());
 	}
 private:
-	FFT<T> fft_;
-	std::vector<C> buf_;
+	FFT<T> fft_, half_;
+	std::vector<C> buf_, z_, wN_;
 };
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,76 @@
+"""Batched frames: many STA frames of different sizes in two persistent
+launches (preparation over every A-scan of every frame, staged delay-and-sum
+over every grid tile of every frame), optionally replayed from a captured CUDA
+graph. Wraps usgb_batch_* of include/usgb.h."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Sequence
+
+from . import native
+from .engine import StaEngine
+
+
+@dataclass
+class BatchItem:
+    engine: StaEngine   # frame parameters, tables, grid (set_grid_device) and signal tensor
+    rf: object          # torch CUDA tensor (num_tx, num_rx, num_samples) float32
+    value: object       # torch CUDA tensor (ncols, nrows) float32
+    factor: object      # torch CUDA tensor (ncols, nrows) float32
+
+
+class Batch:
+    def __init__(self, max_frames: int, max_elements: int, max_signal_length: int = 0):
+        self._lib = native.load()
+        h = C.c_void_p()
+        rc = self._lib.usgb_batch_create(max_frames, max_elements, max_signal_length, C.byref(h))
+        if rc != 0:
+            self._raise_create(rc)
+        self._h = h
+        self.max_frames = max_frames
+        self._keep = None
+
+    def _raise_create(self, rc):
+        from .errors import from_status
+        raise from_status(rc, self._lib.usgb_batch_last_error(None).decode())
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            from .errors import from_status
+            raise from_status(rc, self._lib.usgb_batch_last_error(self._h).decode())
+
+    def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int) -> None:
+        self._check(self._lib.usgb_batch_set_das_config(self._h, tile_rows, stage_bytes, stages))
+
+    def run(self, items: Sequence[BatchItem], stream, use_graph: bool = True) -> None:
+        """Enqueue the batch on `stream` (torch.cuda.Stream or raw handle)."""
+        arr = (native.BatchItem * len(items))()
+        for i, it in enumerate(items):
+            arr[i].ctx = it.engine._h
+            arr[i].d_rf = it.rf.data_ptr()
+            arr[i].d_value = it.value.data_ptr()
+            arr[i].d_factor = it.factor.data_ptr()
+        self._keep = (arr, list(items))  # tensors stay referenced until the next run
+        ptr = getattr(stream, "cuda_stream", stream)
+        self._check(self._lib.usgb_batch_run(self._h, arr, len(items), C.c_void_p(ptr), int(use_graph)))
+
+    def synchronize(self) -> None:
+        self._check(self._lib.usgb_batch_synchronize(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.usgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -163,6 +163,7 @@ struct usgb_ctx {
 	int dasVariant = 0;
 	unsigned tileRows = 8;
 	unsigned stageBytes = 16384;
+	unsigned stages = 4;
 	std::string err;
 
 	~usgb_ctx()
@@ -172,6 +173,35 @@ struct usgb_ctx {
 		if (h_rf) cudaFreeHost(h_rf);
 		if (h_out) cudaFreeHost(h_out);
 		if (ownStream && stream) cudaStreamDestroy(stream);
+	}
+};
+
+struct usgb_batch {
+	unsigned maxFrames = 0, maxElements = 0, maxSignalLength = 0;
+	unsigned tileRows = 8, stageBytes = 16384, stages = 0;
+	unsigned numSMs = 0;
+	size_t descBytes = 0;
+	unsigned char* h_desc = nullptr;   // pinned: header, prep frames, DAS frames
+	unsigned char* d_desc = nullptr;
+	unsigned* d_err = nullptr;
+	cudaEvent_t done = nullptr;
+	bool pending = false;
+	// Captured graph and the launch shape it was captured for.
+	cudaGraphExec_t graph = nullptr;
+	size_t graphPrepSmem = 0;
+	unsigned graphPrepBlocks = 0, graphDasBlocks = 0;
+	int graphStorage = -1;
+	bool graphAnalytic = true;
+	cudaStream_t graphStream = nullptr;
+	std::string err;
+
+	~usgb_batch()
+	{
+		if (graph) cudaGraphExecDestroy(graph);
+		if (done) cudaEventDestroy(done);
+		if (d_desc) cudaFree(d_desc);
+		if (d_err) cudaFree(d_err);
+		if (h_desc) cudaFreeHost(h_desc);
 	}
 };
 
@@ -408,6 +438,7 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.errWord = c->d_err;
 	dp.tileRows = c->tileRows;
 	dp.stageBytes = c->stageBytes;
+	dp.stages = c->stages;
 	return dp;
 }
 
@@ -430,6 +461,33 @@ void ensure_grid(usgb_ctx* c, uint32_t ncols, uint32_t nrows)
 	c->ncols = ncols;
 	c->nrows = nrows;
 	c->npix = static_cast<unsigned>(npix);
+}
+
+size_t max_smem()
+{
+	int dev = 0, v = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+	if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+	return static_cast<size_t>(v);
+}
+
+// Default delay-and-sum kernel: the staged kernel with 32 x 8 tiles, 16 KiB
+// stages and the deepest pipeline that fits in shared memory (then 32 x 4
+// tiles), else the plain kernel.
+void choose_default_das(usgb_ctx* c)
+{
+	for (unsigned rows : {8u, 4u}) {
+		for (unsigned nst : {8u, 6u, 4u, 2u}) {
+			if (usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, 16384u, nst) <= max_smem()) {
+				c->dasVariant = 1;
+				c->tileRows = rows;
+				c->stageBytes = 16384u;
+				c->stages = nst;
+				return;
+			}
+		}
+	}
+	c->dasVariant = 0;
 }
 
 void check_prep_fits(const usgb_ctx* c)
@@ -498,6 +556,7 @@ int usgb_create(const usgb_sta_params* params, usgb_ctx** out)
 		check_and_derive(c, params);
 		build_tables(c);
 		check_prep_fits(c);
+		choose_default_das(c);
 		alloc_frame(c);
 		USGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
 		c->ownStream = true;
@@ -647,29 +706,106 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 	return USGB_OK;
 }
 
-int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes)
+int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return guarded(c, [&] {
 		if (variant != 0 && variant != 1) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
 		const unsigned rows = tile_rows ? tile_rows : c->tileRows;
 		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
+		const unsigned nst = stages ? stages : c->stages;
 		if (variant == 1) {
 			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
 			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
 				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 			}
-			int dev = 0, maxSmem = 0;
-			USGB_CUDA(cudaGetDevice(&dev));
-			USGB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-			const size_t need = usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap);
-			if (need > static_cast<size_t>(maxSmem)) {
+			if (nst < 2 || nst > 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage count must be in [2, 16].");
+			const size_t need = usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst);
+			if (need > max_smem()) {
 				USGB_FAIL(USGB_ERR_UNSUPPORTED, "Staged delay-and-sum needs " << need << " bytes of shared memory (device: "
-						<< maxSmem << "); use fewer tile rows or smaller stages.");
+						<< max_smem() << "); use fewer tile rows, stages or smaller stages.");
 			}
 		}
 		c->dasVariant = variant;
 		c->tileRows = rows;
 		c->stageBytes = cap;
+		c->stages = nst;
+	});
+}
+
+int usgb_get_das_config(const usgb_ctx* c, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes, uint32_t* stages)
+{
+	if (!c) return USGB_ERR_INVALID_PARAMETER;
+	if (variant) *variant = c->dasVariant;
+	if (tile_rows) *tile_rows = c->tileRows;
+	if (stage_bytes) *stage_bytes = c->stageBytes;
+	if (stages) *stages = c->stages;
+	return USGB_OK;
+}
+
+int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float* d_factor, uint32_t iterations,
+		float* best_ms)
+{
+	return guarded(c, [&] {
+		if (!d_signals || !d_value || !d_factor) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
+		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+		if (reinterpret_cast<uintptr_t>(d_signals) % 16 != 0) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The signal tensor must be 16-byte aligned.");
+		}
+		const unsigned iters = iterations ? iterations : 3;
+		struct Cand { int variant; unsigned rows, cap, stages; };
+		std::vector<Cand> cands;
+		for (unsigned rows : {4u, 8u, 16u})
+			for (unsigned cap : {8192u, 16384u, 32768u})
+				for (unsigned nst : {2u, 4u, 6u, 8u, 12u, 16u})
+					if (usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst) <= max_smem())
+						cands.push_back({1, rows, cap, nst});
+		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});
+		cudaEvent_t e0, e1;
+		USGB_CUDA(cudaEventCreate(&e0));
+		USGB_CUDA(cudaEventCreate(&e1));
+		float best = 1e30f;
+		Cand bestC = cands.back();
+		const Cand saved{c->dasVariant, c->tileRows, c->stageBytes, c->stages};
+		for (const Cand& k : cands) {
+			c->dasVariant = k.variant;
+			c->tileRows = k.rows;
+			c->stageBytes = k.cap;
+			c->stages = k.stages;
+			const usgb::DasParams dp = das_params(c, d_signals, d_value, d_factor);
+			USGB_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+			USGB_CUDA(usgb::launch_das(dp, static_cast<int>(c->prm.storage), static_cast<int>(c->prm.coherence),
+					c->analytic, k.variant, c->stream));  // warm-up
+			USGB_CUDA(cudaEventRecord(e0, c->stream));
+			for (unsigned i = 0; i < iters; ++i) {
+				USGB_CUDA(usgb::launch_das(dp, static_cast<int>(c->prm.storage), static_cast<int>(c->prm.coherence),
+						c->analytic, k.variant, c->stream));
+			}
+			USGB_CUDA(cudaEventRecord(e1, c->stream));
+			USGB_CUDA(cudaEventSynchronize(e1));
+			unsigned errWord = 0;
+			USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+			float ms = 0;
+			USGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			ms /= static_cast<float>(iters);
+			if (!errWord && ms < best) {
+				best = ms;
+				bestC = k;
+			}
+		}
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		if (best >= 1e30f) {
+			c->dasVariant = saved.variant;
+			c->tileRows = saved.rows;
+			c->stageBytes = saved.cap;
+			c->stages = saved.stages;
+			USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "no delay-and-sum configuration completed");
+		}
+		c->dasVariant = bestC.variant;
+		c->tileRows = bestC.rows;
+		c->stageBytes = bestC.cap;
+		c->stages = bestC.stages;
+		if (best_ms) *best_ms = best;
 	});
 }
 
@@ -680,6 +816,259 @@ int usgb_synchronize(usgb_ctx* c)
 		unsigned errWord = 0;
 		USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
 		if (errWord) USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+	});
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched frames
+// ===========================================================================
+namespace {
+
+size_t batch_desc_bytes(unsigned maxFrames)
+{
+	return sizeof(usgb::BatchHeader) + maxFrames * (sizeof(usgb::BatchPrepFrame) + sizeof(usgb::BatchDasFrame));
+}
+
+// Largest prep shared memory over the batch's frames.
+size_t batch_prep_smem(const usgb_batch_item* items, uint32_t count)
+{
+	size_t m = 0;
+	for (uint32_t i = 0; i < count; ++i) {
+		const usgb::PrepParams pp = prep_params(items[i].ctx, nullptr, nullptr);
+		m = std::max(m, usgb::prep_smem_bytes(pp, items[i].ctx->analytic));
+	}
+	return m;
+}
+
+template<typename F>
+int batch_guarded(usgb_batch* b, F&& f)
+{
+	if (!b) return USGB_ERR_INVALID_PARAMETER;
+	try {
+		f();
+		return USGB_OK;
+	} catch (const Failure& e) {
+		b->err = e.msg;
+		return e.code;
+	} catch (const std::exception& e) {
+		b->err = e.what();
+		return USGB_ERR_INVALID_STATE;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+
+int usgb_batch_create(uint32_t max_frames, uint32_t max_elements, uint32_t max_signal_length, usgb_batch** out)
+{
+	if (!out) return USGB_ERR_INVALID_PARAMETER;
+	*out = nullptr;
+	usgb_batch* b = nullptr;
+	try {
+		if (max_frames == 0 || max_frames > 4096) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "max_frames must be in [1, 4096].");
+		if (max_elements == 0 || max_elements > 1024) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "max_elements must be in [1, 1024].");
+		b = new usgb_batch();
+		b->maxFrames = max_frames;
+		b->maxElements = max_elements;
+		b->maxSignalLength = max_signal_length;
+		int dev = 0, sms = 0;
+		USGB_CUDA(cudaGetDevice(&dev));
+		USGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		b->numSMs = static_cast<unsigned>(sms);
+		for (unsigned nst : {8u, 6u, 4u, 2u}) {
+			if (usgb::das_staged_smem_bytes(max_elements, max_elements, b->tileRows, b->stageBytes, nst) <= max_smem()) {
+				b->stages = nst;
+				break;
+			}
+		}
+		if (!b->stages) {
+			b->tileRows = 4;
+			b->stages = 2;
+			if (usgb::das_staged_smem_bytes(max_elements, max_elements, 4, b->stageBytes, 2) > max_smem()) {
+				USGB_FAIL(USGB_ERR_UNSUPPORTED, "max_elements too large for the batched delay-and-sum.");
+			}
+		}
+		b->descBytes = batch_desc_bytes(max_frames);
+		USGB_CUDA(cudaMallocHost(&b->h_desc, b->descBytes));
+		USGB_CUDA(cudaMalloc(&b->d_desc, b->descBytes));
+		USGB_CUDA(cudaMalloc(&b->d_err, sizeof(unsigned)));
+		USGB_CUDA(cudaMemset(b->d_err, 0, sizeof(unsigned)));
+		USGB_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+		*out = b;
+		return USGB_OK;
+	} catch (const Failure& e) {
+		g_createError = e.msg;
+		delete b;
+		return e.code;
+	}
+}
+
+void usgb_batch_destroy(usgb_batch* b)
+{
+	if (!b) return;
+	if (b->pending) cudaEventSynchronize(b->done);
+	delete b;
+}
+
+const char* usgb_batch_last_error(const usgb_batch* b)
+{
+	return b ? b->err.c_str() : g_createError.c_str();
+}
+
+int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
+{
+	return batch_guarded(b, [&] {
+		if (tile_rows != 4 && tile_rows != 8 && tile_rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+		if (stage_bytes < 1024 || stage_bytes % 128 != 0 || stage_bytes > (1u << 20)) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
+		}
+		if (stages < 2 || stages > 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage count must be in [2, 16].");
+		if (usgb::das_staged_smem_bytes(b->maxElements, b->maxElements, tile_rows, stage_bytes, stages) > max_smem()) {
+			USGB_FAIL(USGB_ERR_UNSUPPORTED, "configuration does not fit in shared memory for max_elements "
+					<< b->maxElements << '.');
+		}
+		b->tileRows = tile_rows;
+		b->stageBytes = stage_bytes;
+		b->stages = stages;
+		if (b->graph) {
+			cudaGraphExecDestroy(b->graph);
+			b->graph = nullptr;
+		}
+	});
+}
+
+int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph)
+{
+	return batch_guarded(b, [&] {
+		if (!items || count == 0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "empty batch");
+		if (count > b->maxFrames) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batch of " << count << " frames exceeds max_frames "
+				<< b->maxFrames << '.');
+		cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+		const usgb_ctx* c0 = items[0].ctx;
+		if (!c0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null context in batch");
+		for (uint32_t i = 0; i < count; ++i) {
+			const usgb_ctx* c = items[i].ctx;
+			if (!c || !items[i].d_rf || !items[i].d_value || !items[i].d_factor) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null pointer in batch item " << i << '.');
+			}
+			if (c->prm.storage != c0->prm.storage || c->analytic != c0->analytic) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "All frames of a batch share the storage type and signal path.");
+			}
+			if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid of batch item " << i << " has not been set.");
+			if (c->prm.num_tx > b->maxElements || c->prm.num_rx > b->maxElements) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batch item " << i << " has more elements than max_elements.");
+			}
+			if (b->maxSignalLength && c->L > b->maxSignalLength) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batch item " << i << " exceeds max_signal_length.");
+			}
+		}
+		// The descriptor buffer of the previous run must have been consumed.
+		if (b->pending) {
+			USGB_CUDA(cudaEventSynchronize(b->done));
+			b->pending = false;
+		}
+		auto* hdr = reinterpret_cast<usgb::BatchHeader*>(b->h_desc);
+		auto* prepF = reinterpret_cast<usgb::BatchPrepFrame*>(b->h_desc + sizeof(usgb::BatchHeader));
+		auto* dasF = reinterpret_cast<usgb::BatchDasFrame*>(b->h_desc + sizeof(usgb::BatchHeader)
+				+ b->maxFrames * sizeof(usgb::BatchPrepFrame));
+		unsigned sigBegin = 0, tileBegin = 0;
+		for (uint32_t i = 0; i < count; ++i) {
+			usgb_ctx* c = items[i].ctx;
+			prepF[i].prep = prep_params(c, items[i].d_rf, c->d_sig);
+			prepF[i].signalBegin = sigBegin;
+			sigBegin += c->numSignals;
+			usgb::DasParams dp = das_params(c, c->d_sig, items[i].d_value, items[i].d_factor);
+			dp.errWord = b->d_err;
+			dp.tileRows = b->tileRows;
+			dp.stageBytes = b->stageBytes;
+			dp.stages = b->stages;
+			dasF[i].das = dp;
+			dasF[i].tileBegin = tileBegin;
+			dasF[i].tilesX = (c->ncols + 31) / 32;
+			dasF[i].cf = static_cast<int>(c->prm.coherence);
+			tileBegin += dasF[i].tilesX * ((c->nrows + b->tileRows - 1) / b->tileRows);
+		}
+		hdr->count = count;
+		hdr->totalSignals = sigBegin;
+		hdr->totalTiles = tileBegin;
+		const auto* dHdr = reinterpret_cast<const usgb::BatchHeader*>(b->d_desc);
+		const auto* dPrep = reinterpret_cast<const usgb::BatchPrepFrame*>(b->d_desc + sizeof(usgb::BatchHeader));
+		const auto* dDas = reinterpret_cast<const usgb::BatchDasFrame*>(b->d_desc + sizeof(usgb::BatchHeader)
+				+ b->maxFrames * sizeof(usgb::BatchPrepFrame));
+		const size_t prepSmem = batch_prep_smem(items, count);
+		if (prepSmem > max_smem()) USGB_FAIL(USGB_ERR_UNSUPPORTED, "An A-scan of the batch is too long for on-chip preparation.");
+		const unsigned prepPerSM = std::max<unsigned>(1, static_cast<unsigned>((228u * 1024u) / (prepSmem + 1024u)));
+		const unsigned prepBlocks = b->numSMs * std::min(prepPerSM, 4u);
+		usgb::BatchDasConfig dc{};
+		dc.maxTx = dc.maxRx = b->maxElements;
+		dc.tileRows = b->tileRows;
+		dc.stageBytes = b->stageBytes;
+		dc.stages = b->stages;
+		const size_t dasSmem = usgb::das_staged_smem_bytes(dc.maxTx, dc.maxRx, dc.tileRows, dc.stageBytes, dc.stages);
+		const unsigned dasPerSM = std::max<unsigned>(1, static_cast<unsigned>((228u * 1024u) / (dasSmem + 1024u)));
+		dc.blocks = b->numSMs * std::min(dasPerSM, 4u);
+		const int storage = static_cast<int>(c0->prm.storage);
+		const bool analytic = c0->analytic;
+
+		auto enqueue = [&](cudaStream_t st) {
+			USGB_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc, b->descBytes, cudaMemcpyHostToDevice, st));
+			USGB_CUDA(usgb::launch_prep_batch(dPrep, dHdr, prepSmem, prepBlocks, storage, analytic, st));
+			USGB_CUDA(usgb::launch_das_staged_batch(dDas, dHdr, dc, storage, analytic, st));
+		};
+		if (use_graph) {
+			// Re-capture when the launch shape changed (the kernels read the
+			// frames from the descriptor buffer, so the graph is frame-agnostic).
+			if (!b->graph || b->graphPrepSmem < prepSmem || b->graphStorage != storage || b->graphAnalytic != analytic) {
+				if (b->graph) {
+					cudaGraphExecDestroy(b->graph);
+					b->graph = nullptr;
+				}
+				cudaStream_t cap;
+				USGB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+				cudaGraph_t g = nullptr;
+				USGB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+				try {
+					enqueue(cap);
+				} catch (...) {
+					cudaStreamEndCapture(cap, &g);
+					if (g) cudaGraphDestroy(g);
+					cudaStreamDestroy(cap);
+					throw;
+				}
+				USGB_CUDA(cudaStreamEndCapture(cap, &g));
+				const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+				cudaGraphDestroy(g);
+				cudaStreamDestroy(cap);
+				USGB_CUDA(ie);
+				b->graphPrepSmem = prepSmem;
+				b->graphStorage = storage;
+				b->graphAnalytic = analytic;
+			}
+			USGB_CUDA(cudaGraphLaunch(b->graph, stream));
+		} else {
+			enqueue(stream);
+		}
+		USGB_CUDA(cudaEventRecord(b->done, stream));
+		b->pending = true;
+	});
+}
+
+int usgb_batch_synchronize(usgb_batch* b)
+{
+	return batch_guarded(b, [&] {
+		if (b->pending) {
+			USGB_CUDA(cudaEventSynchronize(b->done));
+			b->pending = false;
+		}
+		unsigned errWord = 0;
+		USGB_CUDA(cudaMemcpy(&errWord, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+		if (errWord) {
+			USGB_CUDA(cudaMemset(b->d_err, 0, sizeof(unsigned)));
+			USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+		}
 	});
 }
 

@@ -66,39 +66,36 @@ das_direct_kernel(DasParams p)
 	CFState<CF> cf;
 	for (unsigned r = 0; r < p.numRx; ++r) {
 		const float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
-		float2 acc = make_float2(0.f, 0.f);
-		if (ANALYTIC) {
-			using CT = typename Complex<S>::T;
-			const CT* base = reinterpret_cast<const CT*>(p.sig) + static_cast<size_t>(r) * p.sigStride;
-			for (unsigned t = 0; t < p.numTx; ++t) {
-				const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
-				float k;
-				const int i = split_delay(d, k);
-				if (static_cast<unsigned>(i) <= lastIdx) {
-					const CT* s = base + t * txStride + i;
+		// Per-transmitter terms go to an even and an odd accumulator (the
+		// order every delay-and-sum kernel of the library uses).
+		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+		for (unsigned t = 0; t < p.numTx; ++t) {
+			const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
+			float k;
+			const int i = split_delay(d, k);
+			float2 v = make_float2(0.f, 0.f);
+			if (static_cast<unsigned>(i) <= lastIdx) {
+				if (ANALYTIC) {
+					using CT = typename Complex<S>::T;
+					const CT* s = reinterpret_cast<const CT*>(p.sig) + static_cast<size_t>(r) * p.sigStride + t * txStride + i;
 					const float2 s0 = Complex<S>::load(s);
 					const float2 s1 = Complex<S>::load(s + 1);
 					const float w0 = 1.0f - k;
-					acc.x = fmaf(w0, s0.x, acc.x);
-					acc.y = fmaf(w0, s0.y, acc.y);
-					acc.x = fmaf(k, s1.x, acc.x);
-					acc.y = fmaf(k, s1.y, acc.y);
+					v.x = fmaf(w0, s0.x, v.x);
+					v.y = fmaf(w0, s0.y, v.y);
+					v.x = fmaf(k, s1.x, v.x);
+					v.y = fmaf(k, s1.y, v.y);
+				} else {
+					using RT = typename Real<S>::T;
+					const RT* s = reinterpret_cast<const RT*>(p.sig) + static_cast<size_t>(r) * p.sigStride + t * txStride + i;
+					v.x = fmaf(1.0f - k, Real<S>::load(s), v.x);
+					v.x = fmaf(k, Real<S>::load(s + 1), v.x);
 				}
 			}
-		} else {
-			using RT = typename Real<S>::T;
-			const RT* base = reinterpret_cast<const RT*>(p.sig) + static_cast<size_t>(r) * p.sigStride;
-			for (unsigned t = 0; t < p.numTx; ++t) {
-				const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
-				float k;
-				const int i = split_delay(d, k);
-				if (static_cast<unsigned>(i) <= lastIdx) {
-					const RT* s = base + t * txStride + i;
-					acc.x = fmaf(1.0f - k, Real<S>::load(s), acc.x);
-					acc.x = fmaf(k, Real<S>::load(s + 1), acc.x);
-				}
-			}
+			if (t & 1) { accOdd.x += v.x; accOdd.y += v.y; }
+			else { accEven.x += v.x; accEven.y += v.y; }
 		}
+		const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
 		const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
 		total.x += rs.x;
 		total.y += rs.y;
@@ -139,7 +136,7 @@ cudaError_t dispatch_cf(const DasParams& p, int cf, bool analytic, cudaStream_t 
 
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream)
 {
-	if (variant == 1) return launch_das_staged(p, storage, cf, analytic, p.stageBytes, stream);
+	if (variant == 1) return launch_das_staged(p, storage, cf, analytic, stream);
 	switch (storage) {
 	case STORE_F16: return dispatch_cf<STORE_F16>(p, cf, analytic, stream);
 	case STORE_BF16: return dispatch_cf<STORE_BF16>(p, cf, analytic, stream);

@@ -1,9 +1,9 @@
-// Staged delay-and-sum kernel: one thread block per tile of 32 columns x
-// TROWS rows of grid points; per (tx, rx) pair, the window of the A-scan that
-// the tile's delays can reach is copied into shared memory by a producer warp
-// with bulk copies (cp.async.bulk, completion on an mbarrier), several
-// windows per pipeline stage, and the consumer warps gather both
-// interpolation taps from shared memory.
+// Staged delay-and-sum: one thread block per tile of 32 columns x TROWS rows
+// of grid points; per (tx, rx) pair, the window of the A-scan that the tile's
+// delays can reach is copied into shared memory by a producer warp with bulk
+// copies (cp.async.bulk, completion on an mbarrier), several windows per
+// pipeline stage, and the consumer warps gather both interpolation taps from
+// shared memory.
 //
 // Arithmetic follows the plain kernel (usgb_das.cu) exactly: same delay
 // rounding, same receiver-major accumulation, same coherence factors.
@@ -18,6 +18,11 @@
 // Warp layout: lane = column, warp = row; neighbouring columns have close
 // delays, so the shared-memory gathers of a warp mostly hit the same or
 // consecutive words.
+//
+// The per-tile body is a device function that keeps the pipeline's stage
+// counter across calls, so one persistent block can run tiles of many frames
+// back to back (batched kernel): the barriers are initialised once and their
+// phases simply continue.
 #include <cuda_runtime.h>
 
 #include "usgb_common.cuh"
@@ -28,7 +33,6 @@ namespace usgb {
 
 namespace {
 
-constexpr int kStages = 4;          // pipeline depth
 constexpr int kMaxWindows = 32;     // windows per stage (one per producer lane)
 constexpr int kGlobalWindow = -1;   // window too large for a stage: gather from global memory
 constexpr int kEmptyWindow = -2;    // no valid sample can be reached
@@ -41,25 +45,63 @@ struct StageMeta {
 	int4 win[kMaxWindows];  // (tx, lo, off, 0) per window
 };
 
-// Shared-memory layout (byte offsets), computed identically on host and device.
+// Shared-memory layout (byte offsets), computed identically on host and
+// device, for at most maxTx / maxRx elements.
 struct StagedLayout {
 	unsigned bars, meta, minmax, partial, txd, stage, total;
-	unsigned capBytes;
-	__host__ __device__ StagedLayout(unsigned numTx, unsigned numRx, unsigned trows, unsigned capBytes_)
+	__host__ __device__ StagedLayout(unsigned maxTx, unsigned maxRx, unsigned trows, unsigned capBytes, unsigned stages)
 	{
-		capBytes = capBytes_;
 		bars = 0;
-		meta = 2 * kStages * 8;
-		minmax = meta + kStages * static_cast<unsigned>(sizeof(StageMeta));
+		meta = (2 * stages * 8 + 15) & ~15u;
+		minmax = meta + stages * static_cast<unsigned>(sizeof(StageMeta));
 		minmax = (minmax + 15) & ~15u;
-		partial = minmax + 2 * (numTx + numRx) * 4;
-		txd = partial + 2 * trows * (numTx + numRx) * 4;
+		partial = minmax + 2 * (maxTx + maxRx) * 4;
+		txd = partial + 2 * trows * (maxTx + maxRx) * 4;
 		txd = (txd + 15) & ~15u;
-		stage = txd + numTx * 32 * trows * 4;
+		stage = txd + maxTx * 32 * trows * 4;
 		stage = (stage + 127) & ~127u;
-		total = stage + kStages * capBytes;
+		total = stage + stages * capBytes;
 	}
 };
+
+// Pointers into the block's shared memory.
+struct Smem {
+	uint64_t* full;
+	uint64_t* empty;
+	StageMeta* meta;
+	float* minT;     // [maxTx]
+	float* maxT;     // [maxTx]
+	float* minR;     // [maxRx]
+	float* maxR;     // [maxRx]
+	float* partMin;  // [TROWS][maxTx + maxRx]
+	float* partMax;
+	float* txd;      // [maxTx][P]
+	unsigned char* stageBuf;
+	unsigned nst;
+	unsigned capBytes;
+	unsigned maxE;   // maxTx + maxRx (row stride of the partial arrays)
+};
+
+__device__ __forceinline__ Smem carve(unsigned char* smem, const StagedLayout& lay, unsigned maxTx, unsigned maxRx,
+		unsigned trows, unsigned nst, unsigned capBytes)
+{
+	Smem s;
+	s.full = reinterpret_cast<uint64_t*>(smem + lay.bars);
+	s.empty = s.full + nst;
+	s.meta = reinterpret_cast<StageMeta*>(smem + lay.meta);
+	s.minT = reinterpret_cast<float*>(smem + lay.minmax);
+	s.maxT = s.minT + maxTx;
+	s.minR = s.maxT + maxTx;
+	s.maxR = s.minR + maxRx;
+	s.partMin = reinterpret_cast<float*>(smem + lay.partial);
+	s.partMax = s.partMin + trows * (maxTx + maxRx);
+	s.txd = reinterpret_cast<float*>(smem + lay.txd);
+	s.stageBuf = smem + lay.stage;
+	s.nst = nst;
+	s.capBytes = capBytes;
+	s.maxE = maxTx + maxRx;
+	return s;
+}
 
 template<bool ANALYTIC, int S> struct Sample;
 template<int S> struct Sample<true, S> {
@@ -86,37 +128,54 @@ template<int S> struct Sample<false, S> {
 	}
 };
 
-__device__ __forceinline__ int floor_to_int(float v)
+// Contribution of one window to one grid point: delay d = txd + rxd,
+// idx = floor(d), k = d - idx; both taps from the stage buffer (or from
+// global memory for a window that did not fit a stage), (1-k) s0 + k s1.
+template<typename SP>
+__device__ __forceinline__ void gather_window(int4 wm, const typename SP::T* buf, const typename SP::T* sig,
+		size_t txStride, unsigned r, size_t sigStride, float txdv, float rxd, bool active, unsigned lastIdx, float2& v)
 {
-	return static_cast<int>(floorf(v));
+	const float d = fmaxf(__fadd_rn(txdv, rxd), -1.0f);
+	const float t0 = __fadd_rd(d, 8388608.0f);
+	const float k = d - (t0 - 8388608.0f);
+	const int i = __float_as_int(t0) - 0x4B000000;
+	if (active && static_cast<unsigned>(i) <= lastIdx) {
+		if (wm.z >= 0) {
+			SP::accumulate(buf + (i - wm.y + wm.z), k, v);
+		} else if (wm.z == kGlobalWindow) {
+			SP::accumulate(sig + wm.x * txStride + static_cast<size_t>(r) * sigStride + i, k, v);
+		}
+	}
 }
 
+__device__ __forceinline__ void init_barriers(const Smem& sm, int trows)
+{
+	if (threadIdx.x == 0) {
+		for (unsigned s = 0; s < sm.nst; ++s) {
+			mbar_init(&sm.full[s], 1);
+			mbar_init(&sm.empty[s], trows);
+		}
+		fence_barrier_init();
+	}
+	__syncthreads();
+}
+
+// One tile (bx, by) of one frame. `it` is the block's running stage counter
+// (the same value in every thread on entry and on exit). Returns false after a
+// wait gave up (the error is recorded in p.errWord).
 template<int S, int CF, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32, 1)
-das_staged_kernel(DasParams p, unsigned capBytes)
+__device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, unsigned by, int& it)
 {
 	using SP = Sample<ANALYTIC, S>;
 	using T = typename SP::T;
 	constexpr int P = 32 * TROWS;
-	extern __shared__ __align__(128) unsigned char smem[];
-	const StagedLayout lay(p.numTx, p.numRx, TROWS, capBytes);
-	uint64_t* full = reinterpret_cast<uint64_t*>(smem + lay.bars);
-	uint64_t* empty = full + kStages;
-	StageMeta* meta = reinterpret_cast<StageMeta*>(smem + lay.meta);
-	float* minT = reinterpret_cast<float*>(smem + lay.minmax);
-	float* maxT = minT + p.numTx;
-	float* minR = maxT + p.numTx;
-	float* maxR = minR + p.numRx;
-	float* partMin = reinterpret_cast<float*>(smem + lay.partial);          // [TROWS][numTx + numRx]
-	float* partMax = partMin + TROWS * (p.numTx + p.numRx);
-	float* txd = reinterpret_cast<float*>(smem + lay.txd);                  // [numTx][P]
-	unsigned char* stageBuf = smem + lay.stage;
-
+	const int nst = static_cast<int>(sm.nst);
+	const unsigned capBytes = sm.capBytes;
 	const int warp = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
 	const bool producer = warp == TROWS;
-	const unsigned col = blockIdx.x * 32 + lane;
-	const unsigned row = blockIdx.y * TROWS + warp;
+	const unsigned col = bx * 32 + lane;
+	const unsigned row = by * TROWS + warp;
 	const bool active = !producer && col < p.ncols && row < p.nrows;
 	const unsigned pix = col * p.nrows + row;
 	const int slot = warp * 32 + lane;
@@ -135,7 +194,7 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 			if (e < p.numTx) {
 				const float dist = distance3d_z0(__ldg(&p.txXY[2 * e]), __ldg(&p.txXY[2 * e + 1]), px, py, pz);
 				v = __fadd_rn(p.signalOffset, __fmul_rn(dist, p.invCT));
-				txd[e * P + slot] = v;
+				sm.txd[e * P + slot] = v;
 			} else {
 				const unsigned r = e - p.numTx;
 				v = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
@@ -147,33 +206,27 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 				mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
 			}
 			if (lane == 0) {
-				partMin[warp * nE + e] = mn;
-				partMax[warp * nE + e] = mx;
+				sm.partMin[warp * sm.maxE + e] = mn;
+				sm.partMax[warp * sm.maxE + e] = mx;
 			}
 		}
 	}
-	if (threadIdx.x == 0) {
-		for (int s = 0; s < kStages; ++s) {
-			mbar_init(&full[s], 1);
-			mbar_init(&empty[s], TROWS);
-		}
-		fence_barrier_init();
-	}
 	__syncthreads();
 	for (unsigned e = threadIdx.x; e < nE; e += blockDim.x) {
-		float mn = partMin[e], mx = partMax[e];
+		float mn = sm.partMin[e], mx = sm.partMax[e];
 		for (int w = 1; w < TROWS; ++w) {
-			mn = fminf(mn, partMin[w * nE + e]);
-			mx = fmaxf(mx, partMax[w * nE + e]);
+			mn = fminf(mn, sm.partMin[w * sm.maxE + e]);
+			mx = fmaxf(mx, sm.partMax[w * sm.maxE + e]);
 		}
-		if (e < p.numTx) { minT[e] = mn; maxT[e] = mx; }
-		else { minR[e - p.numTx] = mn; maxR[e - p.numTx] = mx; }
+		if (e < p.numTx) { sm.minT[e] = mn; sm.maxT[e] = mx; }
+		else { sm.minR[e - p.numTx] = mn; sm.maxR[e - p.numTx] = mx; }
 	}
 	__syncthreads();
 
 	const int L = static_cast<int>(p.L);
 	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
 	const T* sig = reinterpret_cast<const T*>(p.sig);
+	bool ok = true;
 
 	if (producer) {
 		// -------------------------------------------------------------- producer
@@ -181,15 +234,14 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 		// receiver at once; a prefix sum packs as many as fit into the stage,
 		// lane 0 arms the stage's barrier with the total byte count and every
 		// lane issues its own bulk copy.
-		int it = 0;
-		bool ok = true;
+		const int itStart = it;
 		for (unsigned r = 0; r < p.numRx && ok; ++r) {
 			unsigned t0 = 0;
 			while (t0 < p.numTx) {
-				const int s = it % kStages;
-				if (it >= kStages) {
+				const int s = it % nst;
+				if (it >= nst) {
 					bool w = true;
-					if (lane == 0) w = mbar_wait_bounded(&empty[s], ((it / kStages) - 1) & 1, kWaitLimitNs);
+					if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], ((it / nst) - 1) & 1, kWaitLimitNs);
 					w = __shfl_sync(0xffffffffu, w, 0);
 					if (!w) {
 						if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
@@ -201,8 +253,8 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 				int lo = 0, kind = kEmptyWindow;
 				unsigned wb = 0;
 				if (t < p.numTx) {
-					const float a = __fadd_rn(minT[t], minR[r]);
-					const float b = __fadd_rn(maxT[t], maxR[r]);
+					const float a = __fadd_rn(sm.minT[t], sm.minR[r]);
+					const float b = __fadd_rn(sm.maxT[t], sm.maxR[r]);
 					// Window [lo, hi] of sample indices (a valid gather reads idx and idx + 1).
 					const float lof = fmaxf(floorf(a), 0.0f);
 					const float hif = fminf(floorf(b) + 1.0f, static_cast<float>(L - 1));
@@ -229,7 +281,7 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 				const int n = __popc(__ballot_sync(0xffffffffu, fits));
 				const unsigned total = __shfl_sync(0xffffffffu, incl, n - 1);
 				const unsigned excl = incl - wb;
-				StageMeta& m = meta[s];
+				StageMeta& m = sm.meta[s];
 				if (lane < n) {
 					const int off = (kind == 0) ? static_cast<int>(excl / sizeof(T)) : kind;
 					m.win[lane] = make_int4(static_cast<int>(t), lo, off, 0);
@@ -240,137 +292,245 @@ das_staged_kernel(DasParams p, unsigned capBytes)
 				}
 				__threadfence_block();
 				__syncwarp();
-				if (lane == 0) mbar_arrive_expect_tx(&full[s], total);
+				if (lane == 0) mbar_arrive_expect_tx(&sm.full[s], total);
 				__syncwarp();
 				if (lane < n && wb > 0) {
 					const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
-					bulk_copy_g2s(stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &full[s]);
+					bulk_copy_g2s(sm.stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &sm.full[s]);
 				}
 				t0 += static_cast<unsigned>(n);
 				++it;
 			}
 		}
-		// Let every issued copy land before the block can exit.
+		// Let this tile's last copies land before the block moves on or exits.
 		if (lane == 0) {
-			for (int j = (it > kStages ? it - kStages : 0); j < it; ++j) {
-				if (!mbar_wait_bounded(&full[j % kStages], (j / kStages) & 1, kWaitLimitNs)) {
+			const int from = (it - nst > itStart) ? it - nst : itStart;
+			for (int j = from; j < it; ++j) {
+				if (!mbar_wait_bounded(&sm.full[j % nst], (j / nst) & 1, kWaitLimitNs)) {
 					atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+					ok = false;
 					break;
 				}
 			}
 		}
-		return;
-	}
-
-	// ------------------------------------------------------------------ consumers
-	const unsigned lastIdx = static_cast<unsigned>(L - 2);
-	float2 total = make_float2(0.f, 0.f);
-	CFState<CF> cf;
-	float2 acc = make_float2(0.f, 0.f);
-	unsigned r = 0;
-	float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[0]), __ldg(&p.rxXY[1]), px, py, pz), p.invCT);
-	int it = 0;
-	bool ok = true;
-	while (r < p.numRx) {
-		const int s = it % kStages;
-		if (!mbar_wait_bounded(&full[s], (it / kStages) & 1, kWaitLimitNs)) {
-			atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-			ok = false;
-			break;
-		}
-		const StageMeta& m = meta[s];
-		const T* buf = reinterpret_cast<const T*>(stageBuf + static_cast<size_t>(s) * capBytes);
-		const int n = m.count;
-		for (int w = 0; w < n; ++w) {
-			const int4 wm = m.win[w];
-			const int t = wm.x;
-			const int off = wm.z;
-			const float d = fmaxf(__fadd_rn(txd[t * P + slot], rxd), -1.0f);
-			const float t0 = __fadd_rd(d, 8388608.0f);
-			const float k = d - (t0 - 8388608.0f);
-			const int i = __float_as_int(t0) - 0x4B000000;
-			if (active && static_cast<unsigned>(i) <= lastIdx) {
-				if (off >= 0) {
-					SP::accumulate(buf + (i - wm.y + off), k, acc);
-				} else if (off == kGlobalWindow) {
-					SP::accumulate(sig + t * txStride + static_cast<size_t>(r) * p.sigStride + i, k, acc);
+	} else {
+		// ------------------------------------------------------------ consumers
+		const unsigned lastIdx = static_cast<unsigned>(L - 2);
+		float2 total = make_float2(0.f, 0.f);
+		CFState<CF> cf;
+		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+		unsigned r = 0;
+		float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[0]), __ldg(&p.rxXY[1]), px, py, pz), p.invCT);
+		while (r < p.numRx) {
+			const int s = it % nst;
+			if (!mbar_wait_bounded(&sm.full[s], (it / nst) & 1, kWaitLimitNs)) {
+				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+				ok = false;
+				break;
+			}
+			const StageMeta& m = sm.meta[s];
+			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
+			const int n = m.count;
+			// Windows of a stage are consecutive transmitters of receiver r, so
+			// a pair (w, w + 1) holds one even and one odd transmitter; their
+			// gathers are independent and go to the even / odd accumulators.
+			int w = 0;
+			for (; w + 1 < n; w += 2) {
+				const int4 wa = m.win[w];
+				const int4 wb = m.win[w + 1];
+				float2 va = make_float2(0.f, 0.f), vb = make_float2(0.f, 0.f);
+				gather_window<SP>(wa, buf, sig, txStride, r, p.sigStride, sm.txd[wa.x * P + slot], rxd, active, lastIdx, va);
+				gather_window<SP>(wb, buf, sig, txStride, r, p.sigStride, sm.txd[wb.x * P + slot], rxd, active, lastIdx, vb);
+				if (wa.x & 1) {
+					accOdd.x += va.x; accOdd.y += va.y;
+					accEven.x += vb.x; accEven.y += vb.y;
+				} else {
+					accEven.x += va.x; accEven.y += va.y;
+					accOdd.x += vb.x; accOdd.y += vb.y;
+				}
+			}
+			if (w < n) {
+				const int4 wa = m.win[w];
+				float2 va = make_float2(0.f, 0.f);
+				gather_window<SP>(wa, buf, sig, txStride, r, p.sigStride, sm.txd[wa.x * P + slot], rxd, active, lastIdx, va);
+				if (wa.x & 1) { accOdd.x += va.x; accOdd.y += va.y; }
+				else { accEven.x += va.x; accEven.y += va.y; }
+			}
+			const int last = m.lastOfRx;
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&sm.empty[s]);
+			++it;
+			if (last) {
+				const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
+				const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
+				total.x += rs.x;
+				total.y += rs.y;
+				cf.add(rs);
+				accEven = make_float2(0.f, 0.f);
+				accOdd = make_float2(0.f, 0.f);
+				++r;
+				if (r < p.numRx) {
+					rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
 				}
 			}
 		}
-		const int last = m.lastOfRx;
-		__syncwarp();
-		if (lane == 0) mbar_arrive(&empty[s]);
-		++it;
-		if (last) {
-			const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
-			total.x += rs.x;
-			total.y += rs.y;
-			cf.add(rs);
-			acc = make_float2(0.f, 0.f);
-			++r;
-			if (r < p.numRx) {
-				rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
-			}
+		if (ok && active) {
+			const float v = ANALYTIC ? magnitude(total) : total.x;
+			p.value[pix] = v * p.valueCoef;
+			p.factor[pix] = cf.result(p.numRx, p, total);
 		}
 	}
-	if (ok && active) {
-		const float v = ANALYTIC ? magnitude(total) : total.x;
-		p.value[pix] = v * p.valueCoef;
-		p.factor[pix] = cf.result(p.numRx, p, total);
+	return ok;
+}
+
+// Single frame: one block per tile.
+template<int S, int CF, bool ANALYTIC, int TROWS>
+__global__ void __launch_bounds__((TROWS + 1) * 32, 1)
+das_staged_kernel(DasParams p)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	const StagedLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
+	const Smem sm = carve(smem, lay, p.numTx, p.numRx, TROWS, p.stages, p.stageBytes);
+	init_barriers(sm, TROWS);
+	int it = 0;
+	staged_tile<S, CF, ANALYTIC, TROWS>(p, sm, blockIdx.x, blockIdx.y, it);
+}
+
+template<int S, bool ANALYTIC, int TROWS>
+__device__ __forceinline__ bool tile_any_cf(const DasParams& p, int cf, const Smem& sm, unsigned bx, unsigned by, int& it)
+{
+	if (!ANALYTIC) {
+		return (cf == CF_SCF) ? staged_tile<S, CF_SCF, false, TROWS>(p, sm, bx, by, it)
+		                      : staged_tile<S, CF_NONE, false, TROWS>(p, sm, bx, by, it);
+	}
+	switch (cf) {
+	case CF_PCF: return staged_tile<S, CF_PCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_SCF: return staged_tile<S, CF_SCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_MF: return staged_tile<S, CF_MF, true, TROWS>(p, sm, bx, by, it);
+	default: return staged_tile<S, CF_NONE, true, TROWS>(p, sm, bx, by, it);
+	}
+}
+
+// Many frames: persistent blocks walk the tiles of every frame in the batch
+// (frames of different sizes and coherence factors; same storage type).
+template<int S, bool ANALYTIC, int TROWS>
+__global__ void __launch_bounds__((TROWS + 1) * 32, 1)
+das_staged_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
+		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	__shared__ DasParams sp;
+	__shared__ int sAbort;
+	const StagedLayout lay(maxTx, maxRx, TROWS, capBytes, stages);
+	const Smem sm = carve(smem, lay, maxTx, maxRx, TROWS, stages, capBytes);
+	if (threadIdx.x == 0) sAbort = 0;
+	init_barriers(sm, TROWS);
+	const unsigned count = hdr->count;
+	const unsigned totalTiles = hdr->totalTiles;
+	int it = 0;
+	unsigned f = 0;
+	for (unsigned w = blockIdx.x; w < totalTiles; w += gridDim.x) {
+		while (f + 1 < count && frames[f + 1].tileBegin <= w) ++f;  // work items are visited in increasing order
+		__syncthreads();  // the previous tile is done with sp and the shared tables
+		if (threadIdx.x == 0) sp = frames[f].das;
+		__syncthreads();
+		if (sAbort) break;
+		const unsigned local = w - frames[f].tileBegin;
+		const unsigned tilesX = frames[f].tilesX;
+		const bool ok = tile_any_cf<S, ANALYTIC, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
+		if (!ok) sAbort = 1;
 	}
 }
 
 template<int S, int CF, bool ANALYTIC, int TROWS>
-cudaError_t launch_one(const DasParams& p, unsigned capBytes, cudaStream_t stream)
+cudaError_t launch_one(const DasParams& p, cudaStream_t stream)
 {
-	const StagedLayout lay(p.numTx, p.numRx, TROWS, capBytes);
+	const StagedLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
 	cudaError_t e = cudaFuncSetAttribute(das_staged_kernel<S, CF, ANALYTIC, TROWS>,
 			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
 	const dim3 grid((p.ncols + 31) / 32, (p.nrows + TROWS - 1) / TROWS);
-	das_staged_kernel<S, CF, ANALYTIC, TROWS><<<grid, (TROWS + 1) * 32, lay.total, stream>>>(p, capBytes);
+	das_staged_kernel<S, CF, ANALYTIC, TROWS><<<grid, (TROWS + 1) * 32, lay.total, stream>>>(p);
 	return cudaGetLastError();
 }
 
 template<int S, int CF, bool ANALYTIC>
-cudaError_t launch_rows(const DasParams& p, unsigned capBytes, cudaStream_t stream)
+cudaError_t launch_rows(const DasParams& p, cudaStream_t stream)
 {
 	switch (p.tileRows) {
-	case 4: return launch_one<S, CF, ANALYTIC, 4>(p, capBytes, stream);
-	case 16: return launch_one<S, CF, ANALYTIC, 16>(p, capBytes, stream);
-	default: return launch_one<S, CF, ANALYTIC, 8>(p, capBytes, stream);
+	case 4: return launch_one<S, CF, ANALYTIC, 4>(p, stream);
+	case 16: return launch_one<S, CF, ANALYTIC, 16>(p, stream);
+	default: return launch_one<S, CF, ANALYTIC, 8>(p, stream);
 	}
 }
 
 template<int S>
-cudaError_t dispatch(const DasParams& p, int cf, bool analytic, unsigned capBytes, cudaStream_t stream)
+cudaError_t dispatch(const DasParams& p, int cf, bool analytic, cudaStream_t stream)
 {
 	if (!analytic) {
-		return (cf == CF_SCF) ? launch_rows<S, CF_SCF, false>(p, capBytes, stream)
-		                      : launch_rows<S, CF_NONE, false>(p, capBytes, stream);
+		return (cf == CF_SCF) ? launch_rows<S, CF_SCF, false>(p, stream) : launch_rows<S, CF_NONE, false>(p, stream);
 	}
 	switch (cf) {
-	case CF_PCF: return launch_rows<S, CF_PCF, true>(p, capBytes, stream);
-	case CF_SCF: return launch_rows<S, CF_SCF, true>(p, capBytes, stream);
-	case CF_MF: return launch_rows<S, CF_MF, true>(p, capBytes, stream);
-	default: return launch_rows<S, CF_NONE, true>(p, capBytes, stream);
+	case CF_PCF: return launch_rows<S, CF_PCF, true>(p, stream);
+	case CF_SCF: return launch_rows<S, CF_SCF, true>(p, stream);
+	case CF_MF: return launch_rows<S, CF_MF, true>(p, stream);
+	default: return launch_rows<S, CF_NONE, true>(p, stream);
+	}
+}
+
+template<int S, bool ANALYTIC, int TROWS>
+cudaError_t launch_batch_one(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		cudaStream_t stream)
+{
+	const StagedLayout lay(c.maxTx, c.maxRx, TROWS, c.stageBytes, c.stages);
+	cudaError_t e = cudaFuncSetAttribute(das_staged_batch_kernel<S, ANALYTIC, TROWS>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
+	if (e != cudaSuccess) return e;
+	das_staged_batch_kernel<S, ANALYTIC, TROWS><<<c.blocks, (TROWS + 1) * 32, lay.total, stream>>>(
+			frames, hdr, c.maxTx, c.maxRx, c.stageBytes, c.stages);
+	return cudaGetLastError();
+}
+
+template<int S, bool ANALYTIC>
+cudaError_t batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c, cudaStream_t stream)
+{
+	switch (c.tileRows) {
+	case 4: return launch_batch_one<S, ANALYTIC, 4>(frames, hdr, c, stream);
+	case 16: return launch_batch_one<S, ANALYTIC, 16>(frames, hdr, c, stream);
+	default: return launch_batch_one<S, ANALYTIC, 8>(frames, hdr, c, stream);
 	}
 }
 
 }  // namespace
 
-size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes)
+size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages)
 {
-	return StagedLayout(numTx, numRx, tileRows, capBytes).total;
+	return StagedLayout(numTx, numRx, tileRows, capBytes, stages).total;
 }
 
-cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, unsigned capBytes,
-		cudaStream_t stream)
+cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream)
 {
 	switch (storage) {
-	case STORE_F16: return dispatch<STORE_F16>(p, cf, analytic, capBytes, stream);
-	case STORE_BF16: return dispatch<STORE_BF16>(p, cf, analytic, capBytes, stream);
-	default: return dispatch<STORE_F32>(p, cf, analytic, capBytes, stream);
+	case STORE_F16: return dispatch<STORE_F16>(p, cf, analytic, stream);
+	case STORE_BF16: return dispatch<STORE_BF16>(p, cf, analytic, stream);
+	default: return dispatch<STORE_F32>(p, cf, analytic, stream);
+	}
+}
+
+cudaError_t launch_das_staged_batch(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		int storage, bool analytic, cudaStream_t stream)
+{
+	if (analytic) {
+		switch (storage) {
+		case STORE_F16: return batch_rows<STORE_F16, true>(frames, hdr, c, stream);
+		case STORE_BF16: return batch_rows<STORE_BF16, true>(frames, hdr, c, stream);
+		default: return batch_rows<STORE_F32, true>(frames, hdr, c, stream);
+		}
+	}
+	switch (storage) {
+	case STORE_F16: return batch_rows<STORE_F16, false>(frames, hdr, c, stream);
+	case STORE_BF16: return batch_rows<STORE_BF16, false>(frames, hdr, c, stream);
+	default: return batch_rows<STORE_F32, false>(frames, hdr, c, stream);
 	}
 }
 

@@ -60,15 +60,53 @@ struct DasParams {
 	float* value;
 	float* factor;
 	unsigned* errWord;
-	// Staged kernel: rows of the 32-column pixel tile, bytes per pipeline stage.
+	// Staged kernel: rows of the 32-column pixel tile, bytes per pipeline
+	// stage, number of stages (2..16).
 	unsigned tileRows;
 	unsigned stageBytes;
+	unsigned stages;
 };
 
 // variant 0: plain kernel; 1: staged kernel.
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
-cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, unsigned capBytes,
-		cudaStream_t stream);
-size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes);
+cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// Batched (multi-frame) launches: persistent blocks walk the work items of
+// every frame; descriptors live in device memory so a captured graph can be
+// replayed with new frames.
+// ---------------------------------------------------------------------------
+struct BatchHeader {
+	unsigned count;          // frames in the batch
+	unsigned totalSignals;   // sum of A-scans (prep work items)
+	unsigned totalTiles;     // sum of DAS tiles
+	unsigned pad;
+};
+
+struct BatchPrepFrame {
+	PrepParams prep;
+	unsigned signalBegin;    // first global A-scan index of the frame
+	unsigned pad[3];
+};
+
+struct BatchDasFrame {
+	DasParams das;
+	unsigned tileBegin;      // first global tile index of the frame
+	unsigned tilesX;         // tiles per row of tiles (32-column tiles)
+	int cf;
+	unsigned pad;
+};
+
+struct BatchDasConfig {
+	unsigned maxTx, maxRx;   // layout limits of the shared memory
+	unsigned tileRows, stageBytes, stages;
+	unsigned blocks;         // persistent grid size
+};
+
+cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
+		int storage, bool analytic, cudaStream_t stream);
+cudaError_t launch_das_staged_batch(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		int storage, bool analytic, cudaStream_t stream);
+size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages);
 
 }  // namespace usgb

@@ -328,8 +328,9 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	dp.errWord = reinterpret_cast<unsigned*>(base + lay.err);
 	dp.tileRows = 8;
 	dp.stageBytes = 16384;
+	dp.stages = 4;
 	// The staged kernel when its shared memory fits, the plain one otherwise.
-	const bool staged = usgb::das_staged_smem_bytes(p->num_tx, p->num_rx, dp.tileRows, dp.stageBytes)
+	const bool staged = usgb::das_staged_smem_bytes(p->num_tx, p->num_rx, dp.tileRows, dp.stageBytes, dp.stages)
 			<= static_cast<size_t>(maxSmem);
 	if (!staged && static_cast<size_t>(p->num_tx) * 128 * sizeof(float) > static_cast<size_t>(maxSmem)) {
 		NA_FAIL(USGB_ERR_UNSUPPORTED, "Too many transmit elements for the delay table: " << p->num_tx << '.');

@@ -384,14 +384,12 @@ __device__ void store_pass(const PrepParams& p, const float* rfs, const float* t
 	}
 }
 
-// NT = 0 selects the generic FIR loop.
+// Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
+// the generic FIR loop.
 template<int S, int NT, int U>
-__global__ void __launch_bounds__(kPrepThreads, 1)
-prep_analytic_kernel(PrepParams p)
+__device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 {
-	extern __shared__ __align__(16) float sm[];
 	const PrepLayout lay(p, true);
-	const unsigned a = blockIdx.x;
 	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, true);
 	float2* data = reinterpret_cast<float2*>(sm + lay.data);
 	float* xs = sm + lay.data;  // the packed complex buffer read as floats: x[n] at n
@@ -441,20 +439,78 @@ prep_analytic_kernel(PrepParams p)
 
 	// 6. Store (x[n] - mean, y[n]) for n < L; x is recomputed from the A-scan.
 	store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);
+	__syncthreads();  // shared memory is reused by the next A-scan of a batch
 }
 
 // Real-RF path: upsampling (fixed 4x FIR) and DC removal only.
+template<int S, int NT, int U>
+__device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
+{
+	const PrepLayout lay(p, false);
+	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
+	const float part = fir_pass<NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr);
+	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
+	store_pass<S, false, NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr, mean, a);
+	__syncthreads();
+}
+
+template<int S, int NT, int U>
+__global__ void __launch_bounds__(kPrepThreads, 1)
+prep_analytic_kernel(PrepParams p)
+{
+	extern __shared__ __align__(16) float sm[];
+	prep_analytic_body<S, NT, U>(p, blockIdx.x, sm);
+}
+
 template<int S, int NT, int U>
 __global__ void __launch_bounds__(kPrepThreads, 1)
 prep_real_kernel(PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
-	const PrepLayout lay(p, false);
-	const unsigned a = blockIdx.x;
-	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
-	const float part = fir_pass<NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr);
-	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
-	store_pass<S, false, NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr, mean, a);
+	prep_real_body<S, NT, U>(p, blockIdx.x, sm);
+}
+
+// FIR shapes with specialised code: the processors' Kaiser-sinc FIR (half
+// transition 0.2) has 2K + 1 = 27 taps per phase for every factor; the fixed
+// 4x FIR of the real path has 21; no upsampling is 1 tap; 0 = generic.
+__host__ __device__ inline int fir_shape(unsigned tapsPerPhase, unsigned U)
+{
+	if (tapsPerPhase == 27 && U == 8) return 1;
+	if (tapsPerPhase == 27 && U == 4) return 2;
+	if (tapsPerPhase == 21 && U == 4) return 3;
+	if (tapsPerPhase == 1 && U == 1) return 4;
+	return 0;
+}
+
+// Many frames: persistent blocks walk the A-scans of every frame of the batch.
+template<int S, bool ANALYTIC>
+__global__ void __launch_bounds__(kPrepThreads, 1)
+prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr)
+{
+	extern __shared__ __align__(16) float sm[];
+	__shared__ PrepParams sp;
+	const unsigned count = hdr->count;
+	const unsigned total = hdr->totalSignals;
+	unsigned f = 0;
+	for (unsigned g = blockIdx.x; g < total; g += gridDim.x) {
+		while (f + 1 < count && frames[f + 1].signalBegin <= g) ++f;
+		__syncthreads();
+		if (threadIdx.x == 0) sp = frames[f].prep;
+		__syncthreads();
+		const unsigned a = g - frames[f].signalBegin;
+		const int shape = fir_shape(sp.tapsPerPhase, sp.U);
+		if (ANALYTIC) {
+			switch (shape) {
+			case 1: prep_analytic_body<S, 27, 8>(sp, a, sm); break;
+			case 2: prep_analytic_body<S, 27, 4>(sp, a, sm); break;
+			case 4: prep_analytic_body<S, 1, 1>(sp, a, sm); break;
+			default: prep_analytic_body<S, 0, 1>(sp, a, sm); break;
+			}
+		} else {
+			if (shape == 3) prep_real_body<S, 21, 4>(sp, a, sm);
+			else prep_real_body<S, 0, 1>(sp, a, sm);
+		}
+	}
 }
 
 template<int S, int NT, int U>
@@ -477,14 +533,24 @@ cudaError_t launch_kernel(const PrepParams& p, bool analytic, size_t smem, cudaS
 template<int S>
 cudaError_t dispatch_fir(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
 {
-	// Specialised FIR shapes: the processors' Kaiser-sinc FIR (half transition
-	// 0.2) has 2K + 1 = 27 taps per phase for every factor; the fixed 4x FIR
-	// of the real path has 21; no upsampling is 1 tap.
-	if (p.tapsPerPhase == 27 && p.U == 8) return launch_kernel<S, 27, 8>(p, analytic, smem, stream);
-	if (p.tapsPerPhase == 27 && p.U == 4) return launch_kernel<S, 27, 4>(p, analytic, smem, stream);
-	if (p.tapsPerPhase == 21 && p.U == 4) return launch_kernel<S, 21, 4>(p, analytic, smem, stream);
-	if (p.tapsPerPhase == 1 && p.U == 1) return launch_kernel<S, 1, 1>(p, analytic, smem, stream);
-	return launch_kernel<S, 0, 1>(p, analytic, smem, stream);
+	switch (fir_shape(p.tapsPerPhase, p.U)) {
+	case 1: return launch_kernel<S, 27, 8>(p, analytic, smem, stream);
+	case 2: return launch_kernel<S, 27, 4>(p, analytic, smem, stream);
+	case 3: return launch_kernel<S, 21, 4>(p, analytic, smem, stream);
+	case 4: return launch_kernel<S, 1, 1>(p, analytic, smem, stream);
+	default: return launch_kernel<S, 0, 1>(p, analytic, smem, stream);
+	}
+}
+
+template<int S, bool ANALYTIC>
+cudaError_t launch_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
+		cudaStream_t stream)
+{
+	cudaError_t e = cudaFuncSetAttribute(prep_batch_kernel<S, ANALYTIC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	prep_batch_kernel<S, ANALYTIC><<<blocks, kPrepThreads, smem, stream>>>(frames, hdr);
+	return cudaGetLastError();
 }
 
 }  // namespace
@@ -492,6 +558,23 @@ cudaError_t dispatch_fir(const PrepParams& p, bool analytic, size_t smem, cudaSt
 size_t prep_smem_bytes(const PrepParams& p, bool analytic)
 {
 	return static_cast<size_t>(PrepLayout(p, analytic).total) * sizeof(float);
+}
+
+cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
+		int storage, bool analytic, cudaStream_t stream)
+{
+	if (analytic) {
+		switch (storage) {
+		case STORE_F16: return launch_batch<STORE_F16, true>(frames, hdr, smem, blocks, stream);
+		case STORE_BF16: return launch_batch<STORE_BF16, true>(frames, hdr, smem, blocks, stream);
+		default: return launch_batch<STORE_F32, true>(frames, hdr, smem, blocks, stream);
+		}
+	}
+	switch (storage) {
+	case STORE_F16: return launch_batch<STORE_F16, false>(frames, hdr, smem, blocks, stream);
+	case STORE_BF16: return launch_batch<STORE_BF16, false>(frames, hdr, smem, blocks, stream);
+	default: return launch_batch<STORE_F32, false>(frames, hdr, smem, blocks, stream);
+	}
 }
 
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream)

@@ -111,9 +111,22 @@ class StaEngine:
         return {"signal_length": L.value, "fft_size": N.value, "signal_stride": stride.value,
                 "signal_bytes": nbytes.value}
 
-    def set_das_variant(self, variant: int, tile_rows: int = 0, stage_bytes: int = 0) -> None:
-        """0: plain kernel; 1: staged kernel (tile_rows in {4, 8, 16})."""
-        self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, stage_bytes))
+    def set_das_variant(self, variant: int, tile_rows: int = 0, stage_bytes: int = 0, stages: int = 0) -> None:
+        """0: plain kernel; 1: staged kernel (tile_rows in {4, 8, 16}, stages in [2, 16])."""
+        self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, stage_bytes, stages))
+
+    def das_config(self):
+        v, r, b, n = C.c_int(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._check(self._lib.usgb_get_das_config(self._h, C.byref(v), C.byref(r), C.byref(b), C.byref(n)))
+        return {"variant": v.value, "tile_rows": r.value, "stage_bytes": b.value, "stages": n.value}
+
+    def autotune_das(self, signals, value, factor, iterations: int = 3) -> float:
+        """Times the delay-and-sum configurations on these prepared signals and
+        keeps the fastest; returns its time in ms."""
+        ms = C.c_float()
+        self._check(self._lib.usgb_autotune_das(self._h, C.c_void_p(signals.data_ptr()), C.c_void_p(value.data_ptr()),
+                                                C.c_void_p(factor.data_ptr()), iterations, C.byref(ms)))
+        return ms.value
 
     # -- host path (reference data flow) -----------------------------------
     def set_grid(self, xyz: np.ndarray) -> None:

@@ -34,6 +34,11 @@ class StaParams(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    """Mirror of ``usgb_batch_item``."""
+    _fields_ = [("ctx", C.c_void_p), ("d_rf", C.c_void_p), ("d_value", C.c_void_p), ("d_factor", C.c_void_p)]
+
+
 # Every symbol include/usgb.h declares, with (restype, argtypes).
 SIGNATURES = {
     "usgb_create": (C.c_int, [C.POINTER(StaParams), C.POINTER(C.c_void_p)]),
@@ -49,9 +54,19 @@ SIGNATURES = {
     "usgb_delay_and_sum_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "usgb_signal_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                    C.POINTER(C.c_uint32), C.POINTER(C.c_size_t)]),
-    "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32]),
+    "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "usgb_get_das_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
+    "usgb_autotune_das": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.POINTER(C.c_float)]),
     "usgb_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_version": (C.c_char_p, []),
+    "usgb_batch_create": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "usgb_batch_destroy": (None, [C.c_void_p]),
+    "usgb_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "usgb_batch_set_das_config": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "usgb_batch_run": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_uint32, C.c_void_p, C.c_int]),
+    "usgb_batch_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_process_frame_noalloc": (C.c_int, [C.POINTER(StaParams), C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
 }
