@@ -319,6 +319,13 @@ def run_gpu(args):
         cpu = cpu_baseline(frame, os.cpu_count() or 1)
         cpu.pop("sec_per_frame", None)
 
+    mixed = None
+    if world == 1 and not args.no_mixed:
+        eng.close()
+        del rfs, rf0, value, factor, grid, sig
+        torch.cuda.empty_cache()
+        mixed = run_mixed(dev)
+
     if rank == 0:
         fps = world * args.steps / (total_ms * 1e-3)
         line = {
@@ -339,11 +346,135 @@ def run_gpu(args):
                          "algorithmic_bytes": top[2]},
             "das_gathers_per_s": gathers / (das_ms * 1e-3),
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
+            "mixed": mixed,
         }
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _db(err: float, peak: float) -> float:
+    return float(20.0 * np.log10(max(err, 1e-30) / max(peak, 1e-30)))
+
+
+def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
+    """The mixed-size workload: `num_frames` frames (elements {32, 64, 96,
+    128}, samples {1024, 2048, 4096} at 40 MHz, grids {128x128, 256x256,
+    512x1024}, PCF on or off, 4x upsampling), every frame's RF resident.
+
+    plain_f32   frames/s of the plain FP32 form: one frame at a time, the
+                direct delay-and-sum kernel;
+    batched_*   frames/s of all frames in one persistent preparation launch +
+                one persistent staged delay-and-sum launch, replayed from a
+                CUDA graph, tile shape autotuned on the batch;
+    serving_f16 the continuous-batching loop over the same frames arriving as
+                a Poisson stream (host RF in, host image out): frames/s,
+                p50/p99 latency from arrival to image in host memory;
+    err_db      peak-relative error of each form's image against the FP64
+                oracle on the `oracle_frames` smallest frames (worst case)."""
+    import torch
+    from dataclasses import replace
+    import oracle
+    from us_lab4a_gb300 import StaEngine, workloads
+    from us_lab4a_gb300.batch import Batch, BatchItem
+    from us_lab4a_gb300.serving import Request, ServingLoop, poisson_arrivals
+    s = torch.cuda.Stream(device=dev)
+    frames = workloads.mixed(num_frames, storage="f16")
+    with torch.cuda.stream(s):
+        rfs = [fr.make_rf_torch(dev) for fr in frames]
+        grids = [torch.as_tensor(fr.grid_xyz, device=dev) for fr in frames]
+    s.synchronize()
+    gathers = sum(fr.npix * fr.spec.num_tx * fr.spec.num_rx for fr in frames)
+
+    def items_for(storage, plain):
+        items = []
+        for fr, rf, g in zip(frames, rfs, grids):
+            e = StaEngine(replace(fr.spec, storage=storage))
+            e.set_stream(s)
+            if plain:
+                e.set_das_variant(0)
+            e.set_grid_device(g)
+            v = torch.empty(fr.grid_xyz.shape[:2], device=dev)
+            items.append(BatchItem(e, rf, v, torch.empty_like(v)))
+        return items
+
+    def timed(fn):
+        fn()
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    small = sorted(range(num_frames), key=lambda i: frames[i].npix * frames[i].spec.num_tx ** 2)[:oracle_frames]
+    refs = {}
+    for i in small:
+        fr = frames[i]
+        sp = fr.spec
+        ospec = oracle.OracleSpec(tx_xy=sp.tx_xy, rx_xy=sp.rx_xy, num_samples=sp.num_samples,
+                                  upsampling=sp.upsampling, sampling_frequency=sp.sampling_frequency,
+                                  propagation_speed=sp.propagation_speed, center_frequency=sp.center_frequency,
+                                  rx_apod=sp.rx_apod, cf={"none": 0, "pcf": 1, "scf": 2, "mf": 3}[sp.coherence])
+        refs[i] = oracle.process(ospec, rfs[i].cpu().numpy().astype(np.float64), fr.grid_xyz, dtype=np.float64)[0]
+
+    def err_db(items):
+        worst = -1e9
+        for i in small:
+            v = items[i].value.cpu().numpy().astype(np.float64)
+            worst = max(worst, _db(float(np.abs(v - refs[i]).max()), float(np.abs(refs[i]).max())))
+        return worst
+
+    out = {"workload": f"{num_frames} mixed-size frames (elements 32-128, 1024-4096 samples @40 MHz, 4x, "
+                       f"grids 128x128 / 256x256 / 512x1024, PCF on/off), RF resident",
+           "gathers": gathers}
+    plain = items_for("f32", plain=True)
+    ms = timed(lambda: [it.engine.process_device(it.rf, it.value, it.factor) for it in plain])
+    out["plain_f32"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms, "err_db": err_db(plain)}
+    for it in plain:
+        it.engine.close()
+    del plain
+    best_f16 = None
+    for storage in ("f32", "f16"):
+        items = items_for(storage, plain=False)
+        with Batch(num_frames, 128) as b:
+            cfg, _ = b.autotune(items, s)
+            ms = timed(lambda: b.run(items, s, use_graph=True))
+            out[f"batched_{storage}"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms,
+                                         "das_config": list(cfg), "err_db": err_db(items)}
+        for it in items:
+            it.engine.close()
+        if storage == "f16":
+            best_f16 = cfg
+    torch.cuda.synchronize(dev)
+    # Serving: the same frames as requests (pinned host RF), saturating Poisson arrivals.
+    arrivals = poisson_arrivals(num_frames, rate=2000.0, seed=11)
+    reqs = [Request(i, fr.spec, fr.grid_xyz, rfs[i].cpu().pin_memory(), float(t))
+            for i, (fr, t) in enumerate(zip(frames, arrivals))]
+    loop = ServingLoop(hbm_budget_bytes=150 << 30, max_batch=num_frames, max_elements=128, das_config=best_f16,
+                       device=dev)
+    loop.run(reqs, keep_images=False)  # creates the resident slots
+    for r in reqs:
+        r.done = None
+    st = loop.run(reqs, keep_images=True)
+    loop.close()
+    worst = -1e9
+    for i in small:
+        worst = max(worst, _db(float(np.abs(reqs[i].value.astype(np.float64) - refs[i]).max()),
+                               float(np.abs(refs[i]).max())))
+    out["serving_f16"] = {"frames_per_s": st["frames_per_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                          "arrival_rate": 2000.0, "batches": st["batches"], "mean_batch": st["mean_batch"],
+                          "hbm_budget_gb": 150, "peak_resident_gb": st["peak_resident_bytes"] / 1e9,
+                          "err_db": worst}
+    base = out["plain_f32"]["frames_per_s"]
+    out["speedup_vs_plain_f32"] = {"batched_f16": out["batched_f16"]["frames_per_s"] / base,
+                                   "serving_f16": st["frames_per_s"] / base}
+    out["err_db_oracle_frames"] = len(small)
+    return out
 
 
 def main():
@@ -361,6 +492,7 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the 48-frame mixed-size / serving section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

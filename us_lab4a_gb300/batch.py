@@ -29,6 +29,7 @@ class Batch:
             self._raise_create(rc)
         self._h = h
         self.max_frames = max_frames
+        self.das_config = None  # library default until set
         self._keep = None
 
     def _raise_create(self, rc):
@@ -40,8 +41,38 @@ class Batch:
             from .errors import from_status
             raise from_status(rc, self._lib.usgb_batch_last_error(self._h).decode())
 
+    # (tile rows, stage bytes, stages) tried by autotune(), most likely first.
+    CANDIDATES = ((4, 16384, 2), (4, 8192, 2), (8, 16384, 2), (4, 16384, 4), (8, 32768, 2), (16, 32768, 2))
+
     def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int) -> None:
         self._check(self._lib.usgb_batch_set_das_config(self._h, tile_rows, stage_bytes, stages))
+        self.das_config = (tile_rows, stage_bytes, stages)
+
+    def autotune(self, items: Sequence[BatchItem], stream, candidates=None, repeats: int = 1):
+        """Time the whole batch (graph replay) under each staged-kernel shape
+        that fits and keep the fastest. Returns ((rows, stage_bytes, stages), ms)."""
+        import torch
+        best = None
+        for cfg in candidates or self.CANDIDATES:
+            try:
+                self.set_das_config(*cfg)
+            except Exception:
+                continue  # does not fit in shared memory for max_elements
+            self.run(items, stream, use_graph=True)  # capture
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(repeats):
+                self.run(items, stream, use_graph=True)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / repeats
+            if best is None or ms < best[1]:
+                best = (cfg, ms)
+        if best is None:
+            raise RuntimeError("no staged delay-and-sum shape fits this batch")
+        self.set_das_config(*best[0])
+        return best
 
     def run(self, items: Sequence[BatchItem], stream, use_graph: bool = True) -> None:
         """Enqueue the batch on `stream` (torch.cuda.Stream or raw handle)."""

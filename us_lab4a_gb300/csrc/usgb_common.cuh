@@ -111,15 +111,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 	return ok != 0;
 }
 
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or about `hint_ns` nanoseconds pass, instead of spinning.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t hint_ns)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns) : "memory");
+	return ok != 0;
+}
+
 // Bounded wait for the phase of `parity` to complete. Gives up after
 // `limit_ns` nanoseconds and returns false; the caller records the error and
-// winds down instead of spinning forever.
+// winds down instead of waiting forever.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
 {
 	if (mbar_try_wait(bar, parity)) return true;
 	const uint64_t t0 = global_timer_ns();
 	for (;;) {
-		if (mbar_try_wait(bar, parity)) return true;
+		if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
 		if (global_timer_ns() - t0 > limit_ns) return false;
 	}
 }

@@ -26,15 +26,43 @@ namespace {
 
 constexpr int kDirectThreads = 128;
 
-// floor(d) and d - floor(d) for d >= -1 (and d < 2^23): one add with
-// rounding toward -inf against 2^23 puts floor(d) in the mantissa. For
-// -1 <= d < 0 the returned index is negative (-1 or -2), so the unsigned
-// range test below rejects it.
+// floor(d) and d - floor(d) for 0 <= d < 2^23: one add with rounding toward
+// -inf against 2^23 puts floor(d) in the mantissa. Every other d lands
+// outside [0, 2^23) as an unsigned index, so the range test below rejects it:
+// -2^23 <= d < 0 gives a sum in [0, 2^23) (index -2^23..-1), a negative sum
+// (d < -2^23, -inf) has its sign bit set (index >= 0xB5000000 after the
+// wrap), d >= 2^23, +inf and NaN give indices >= 2^23.
 __device__ __forceinline__ int split_delay(float d, float& frac)
 {
 	const float t = __fadd_rd(d, 8388608.0f);
 	frac = d - (t - 8388608.0f);
-	return __float_as_int(t) - 0x4B000000;
+	return static_cast<int>(__float_as_uint(t) - 0x4B000000u);  // wraps, never overflows
+}
+
+template<int S, bool ANALYTIC>
+__device__ __forceinline__ constexpr size_t sample_bytes()
+{
+	return ANALYTIC ? sizeof(typename Complex<S>::T) : sizeof(typename Real<S>::T);
+}
+
+// acc += (1-k) s[0] + k s[1] (complex or real taps at `s`).
+template<int S, bool ANALYTIC>
+__device__ __forceinline__ void gather(const char* s, float k, float2& acc)
+{
+	const float w0 = 1.0f - k;
+	if constexpr (ANALYTIC) {
+		using CT = typename Complex<S>::T;
+		const float2 s0 = Complex<S>::load(reinterpret_cast<const CT*>(s));
+		const float2 s1 = Complex<S>::load(reinterpret_cast<const CT*>(s) + 1);
+		acc.x = fmaf(w0, s0.x, acc.x);
+		acc.y = fmaf(w0, s0.y, acc.y);
+		acc.x = fmaf(k, s1.x, acc.x);
+		acc.y = fmaf(k, s1.y, acc.y);
+	} else {
+		using RT = typename Real<S>::T;
+		acc.x = fmaf(w0, Real<S>::load(reinterpret_cast<const RT*>(s)), acc.x);
+		acc.x = fmaf(k, Real<S>::load(reinterpret_cast<const RT*>(s) + 1), acc.x);
+	}
 }
 
 // Plain form: one thread per grid point, gathers straight from global
@@ -66,34 +94,18 @@ das_direct_kernel(DasParams p)
 	CFState<CF> cf;
 	for (unsigned r = 0; r < p.numRx; ++r) {
 		const float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
-		// Per-transmitter terms go to an even and an odd accumulator (the
-		// order every delay-and-sum kernel of the library uses).
+		// Per-transmitter terms go straight into an even and an odd
+		// accumulator (the order every delay-and-sum kernel of the library uses).
 		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+		const char* rsig = static_cast<const char*>(p.sig) + (static_cast<size_t>(r) * p.sigStride) * sample_bytes<S, ANALYTIC>();
 		for (unsigned t = 0; t < p.numTx; ++t) {
-			const float d = fmaxf(__fadd_rn(txd[t * blockDim.x + tid], rxd), -1.0f);
 			float k;
-			const int i = split_delay(d, k);
-			float2 v = make_float2(0.f, 0.f);
+			const int i = split_delay(__fadd_rn(txd[t * blockDim.x + tid], rxd), k);
 			if (static_cast<unsigned>(i) <= lastIdx) {
-				if (ANALYTIC) {
-					using CT = typename Complex<S>::T;
-					const CT* s = reinterpret_cast<const CT*>(p.sig) + static_cast<size_t>(r) * p.sigStride + t * txStride + i;
-					const float2 s0 = Complex<S>::load(s);
-					const float2 s1 = Complex<S>::load(s + 1);
-					const float w0 = 1.0f - k;
-					v.x = fmaf(w0, s0.x, v.x);
-					v.y = fmaf(w0, s0.y, v.y);
-					v.x = fmaf(k, s1.x, v.x);
-					v.y = fmaf(k, s1.y, v.y);
-				} else {
-					using RT = typename Real<S>::T;
-					const RT* s = reinterpret_cast<const RT*>(p.sig) + static_cast<size_t>(r) * p.sigStride + t * txStride + i;
-					v.x = fmaf(1.0f - k, Real<S>::load(s), v.x);
-					v.x = fmaf(k, Real<S>::load(s + 1), v.x);
-				}
+				const char* s = rsig + (t * txStride + i) * sample_bytes<S, ANALYTIC>();
+				if (t & 1) gather<S, ANALYTIC>(s, k, accOdd);
+				else gather<S, ANALYTIC>(s, k, accEven);
 			}
-			if (t & 1) { accOdd.x += v.x; accOdd.y += v.y; }
-			else { accEven.x += v.x; accEven.y += v.y; }
 		}
 		const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
 		const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);

@@ -38,11 +38,16 @@ constexpr int kGlobalWindow = -1;   // window too large for a stage: gather from
 constexpr int kEmptyWindow = -2;    // no valid sample can be reached
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 
+// One stage: up to 32 windows of consecutive transmitters of one receiver.
+// Window w is (txd byte offset t * P * 4, base, kind, t): sample idx of a
+// staged window sits at stage element idx + base; kind is kGlobalWindow or
+// kEmptyWindow for windows that carry no bytes, else 0.
 struct StageMeta {
 	int count;
-	int lastOfRx;
-	int pad[2];
-	int4 win[kMaxWindows];  // (tx, lo, off, 0) per window
+	int lastOfRx;   // the stage ends its receiver
+	int firstOdd;   // its first transmitter is odd
+	int anyGlobal;  // some window is gathered from global memory
+	int4 win[kMaxWindows];
 };
 
 // Shared-memory layout (byte offsets), computed identically on host and
@@ -128,22 +133,40 @@ template<int S> struct Sample<false, S> {
 	}
 };
 
-// Contribution of one window to one grid point: delay d = txd + rxd,
-// idx = floor(d), k = d - idx; both taps from the stage buffer (or from
-// global memory for a window that did not fit a stage), (1-k) s0 + k s1.
-template<typename SP>
-__device__ __forceinline__ void gather_window(int4 wm, const typename SP::T* buf, const typename SP::T* sig,
-		size_t txStride, unsigned r, size_t sigStride, float txdv, float rxd, bool active, unsigned lastIdx, float2& v)
+// floor(d) by one round-down add against 2^23 (split_delay of the plain
+// kernel): every d outside [0, 2^23) gives an index the unsigned test rejects.
+__device__ __forceinline__ int split_delay(float d, float& k)
 {
-	const float d = fmaxf(__fadd_rn(txdv, rxd), -1.0f);
 	const float t0 = __fadd_rd(d, 8388608.0f);
-	const float k = d - (t0 - 8388608.0f);
-	const int i = __float_as_int(t0) - 0x4B000000;
-	if (active && static_cast<unsigned>(i) <= lastIdx) {
+	k = d - (t0 - 8388608.0f);
+	return static_cast<int>(__float_as_uint(t0) - 0x4B000000u);
+}
+
+// Contribution of one staged (or empty) window to one grid point: delay
+// d = txd + rxd, idx = floor(d), k = d - idx, acc += (1-k) s[idx] + k s[idx+1].
+// Every delay of the tile lies inside its window, so the range test alone
+// guards the stage read; an empty window rejects every index.
+template<typename SP>
+__device__ __forceinline__ void gather_staged(const typename SP::T* buf, int base, float txdv, float rxd,
+		unsigned lastIdx, float2& acc)
+{
+	float k;
+	const int i = split_delay(__fadd_rn(txdv, rxd), k);
+	if (static_cast<unsigned>(i) <= lastIdx) SP::accumulate(buf + (i + base), k, acc);
+}
+
+// Any window kind: staged, empty, or gathered from global memory.
+template<typename SP>
+__device__ __forceinline__ void gather_any(int4 wm, const typename SP::T* buf, const typename SP::T* sig,
+		size_t txStride, unsigned r, size_t sigStride, float txdv, float rxd, unsigned lastIdx, float2& acc)
+{
+	float k;
+	const int i = split_delay(__fadd_rn(txdv, rxd), k);
+	if (static_cast<unsigned>(i) <= lastIdx) {
 		if (wm.z >= 0) {
-			SP::accumulate(buf + (i - wm.y + wm.z), k, v);
+			SP::accumulate(buf + (i + wm.y), k, acc);
 		} else if (wm.z == kGlobalWindow) {
-			SP::accumulate(sig + wm.x * txStride + static_cast<size_t>(r) * sigStride + i, k, v);
+			SP::accumulate(sig + wm.w * txStride + static_cast<size_t>(r) * sigStride + i, k, acc);
 		}
 	}
 }
@@ -181,11 +204,15 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 	const int slot = warp * 32 + lane;
 	const unsigned nE = p.numTx + p.numRx;
 
+	// A consumer thread beyond the grid's edge takes the delays of the
+	// nearest grid point of its tile (and stores nothing), so that every
+	// consumer delay lies inside every window of the tile.
 	float px = 0.f, py = 0.f, pz = 0.f;
-	if (active) {
-		px = p.grid[3 * pix];
-		py = p.grid[3 * pix + 1];
-		pz = p.grid[3 * pix + 2];
+	if (!producer) {
+		const unsigned q = min(col, p.ncols - 1) * p.nrows + min(row, p.nrows - 1);
+		px = p.grid[3 * q];
+		py = p.grid[3 * q + 1];
+		pz = p.grid[3 * q + 2];
 	}
 	// Transmit-delay table and per-warp min/max of every element's delay.
 	if (!producer) {
@@ -199,8 +226,7 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 				const unsigned r = e - p.numTx;
 				v = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
 			}
-			float mn = active ? v : __int_as_float(0x7f800000);   // +inf
-			float mx = active ? v : __int_as_float(0xff800000);   // -inf
+			float mn = v, mx = v;
 			for (int o = 16; o > 0; o >>= 1) {
 				mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
 				mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -279,16 +305,19 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 				// always fits, since an oversized window carries no bytes.
 				const bool fits = t < p.numTx && incl <= capBytes;
 				const int n = __popc(__ballot_sync(0xffffffffu, fits));
+				const bool anyGlobal = __ballot_sync(0xffffffffu, fits && kind == kGlobalWindow) != 0u;
 				const unsigned total = __shfl_sync(0xffffffffu, incl, n - 1);
 				const unsigned excl = incl - wb;
 				StageMeta& m = sm.meta[s];
 				if (lane < n) {
-					const int off = (kind == 0) ? static_cast<int>(excl / sizeof(T)) : kind;
-					m.win[lane] = make_int4(static_cast<int>(t), lo, off, 0);
+					const int base = (kind == 0) ? static_cast<int>(excl / sizeof(T)) - lo : 0;
+					m.win[lane] = make_int4(static_cast<int>(t * (P * 4u)), base, kind, static_cast<int>(t));
 				}
 				if (lane == 0) {
 					m.count = n;
 					m.lastOfRx = (t0 + n == p.numTx) ? 1 : 0;
+					m.firstOdd = static_cast<int>(t0 & 1u);
+					m.anyGlobal = anyGlobal ? 1 : 0;
 				}
 				__threadfence_block();
 				__syncwarp();
@@ -316,6 +345,7 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 	} else {
 		// ------------------------------------------------------------ consumers
 		const unsigned lastIdx = static_cast<unsigned>(L - 2);
+		const char* txdSlot = reinterpret_cast<const char*>(sm.txd + slot);
 		float2 total = make_float2(0.f, 0.f);
 		CFState<CF> cf;
 		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
@@ -330,33 +360,37 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 			}
 			const StageMeta& m = sm.meta[s];
 			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
-			const int n = m.count;
-			// Windows of a stage are consecutive transmitters of receiver r, so
-			// a pair (w, w + 1) holds one even and one odd transmitter; their
-			// gathers are independent and go to the even / odd accumulators.
-			int w = 0;
-			for (; w + 1 < n; w += 2) {
-				const int4 wa = m.win[w];
-				const int4 wb = m.win[w + 1];
-				float2 va = make_float2(0.f, 0.f), vb = make_float2(0.f, 0.f);
-				gather_window<SP>(wa, buf, sig, txStride, r, p.sigStride, sm.txd[wa.x * P + slot], rxd, active, lastIdx, va);
-				gather_window<SP>(wb, buf, sig, txStride, r, p.sigStride, sm.txd[wb.x * P + slot], rxd, active, lastIdx, vb);
-				if (wa.x & 1) {
-					accOdd.x += va.x; accOdd.y += va.y;
-					accEven.x += vb.x; accEven.y += vb.y;
-				} else {
-					accEven.x += va.x; accEven.y += va.y;
-					accOdd.x += vb.x; accOdd.y += vb.y;
+			const int4 head = *reinterpret_cast<const int4*>(&m.count);
+			const int n = head.x;
+			// Windows of a stage are consecutive transmitters of receiver r:
+			// window w goes to the accumulator of its transmitter's parity. With
+			// the accumulators swapped for a stage that starts on an odd
+			// transmitter, even w is always `a0` and odd w `a1`.
+			float2 a0 = accEven, a1 = accOdd;
+			if (head.z) { a0 = accOdd; a1 = accEven; }
+			if (!head.w) {
+				int w = 0;
+				for (; w + 1 < n; w += 2) {
+					const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
+					const int2 wb = *reinterpret_cast<const int2*>(&m.win[w + 1]);
+					gather_staged<SP>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, a0);
+					gather_staged<SP>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, a1);
+				}
+				if (w < n) {
+					const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
+					gather_staged<SP>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, a0);
+				}
+			} else {
+				for (int w = 0; w < n; ++w) {
+					const int4 wa = m.win[w];
+					const float txdv = *reinterpret_cast<const float*>(txdSlot + wa.x);
+					if (w & 1) gather_any<SP>(wa, buf, sig, txStride, r, p.sigStride, txdv, rxd, lastIdx, a1);
+					else gather_any<SP>(wa, buf, sig, txStride, r, p.sigStride, txdv, rxd, lastIdx, a0);
 				}
 			}
-			if (w < n) {
-				const int4 wa = m.win[w];
-				float2 va = make_float2(0.f, 0.f);
-				gather_window<SP>(wa, buf, sig, txStride, r, p.sigStride, sm.txd[wa.x * P + slot], rxd, active, lastIdx, va);
-				if (wa.x & 1) { accOdd.x += va.x; accOdd.y += va.y; }
-				else { accEven.x += va.x; accEven.y += va.y; }
-			}
-			const int last = m.lastOfRx;
+			if (head.z) { accOdd = a0; accEven = a1; }
+			else { accEven = a0; accOdd = a1; }
+			const int last = head.y;
 			__syncwarp();
 			if (lane == 0) mbar_arrive(&sm.empty[s]);
 			++it;
