@@ -65,6 +65,16 @@ typedef enum usgb_storage {
 	USGB_STORE_BF16 = 2
 } usgb_storage;
 
+/* Precision of the per-pixel delays in the staged delay-and-sum kernel. The
+ * reference computes them in FP32 (VectorialSTAProcessor.h:265-277); FP32
+ * delays of d samples are off by up to about 8 * 2^-24 * d samples, which
+ * exceeds 1/64 sample beyond d = 32768 (deep grids at high upsampling). */
+typedef enum usgb_delay_precision {
+	USGB_DELAY_AUTO = 0, /* FP64 geometry for the pixel tiles whose largest delay exceeds 32768 samples, FP32 elsewhere */
+	USGB_DELAY_FP32 = 1, /* FP32 everywhere, as the reference */
+	USGB_DELAY_FP64 = 2  /* FP64 geometry everywhere */
+} usgb_delay_precision;
+
 /*
  * Frame description. Mirrors the constructor arguments of
  * VectorialSTAProcessor(config, acquisition, upsamplingFactor, coherenceFactor,
@@ -150,6 +160,13 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);
+
+/* Delay precision of the staged kernel (usgb_delay_precision; new contexts:
+ * USGB_DELAY_AUTO). FP64 tiles compute each pixel's transmit and receive
+ * delays in double and sum them as 32-bit fixed point with 2^-10 sample
+ * resolution. No counterpart in the reference, which is FP32 throughout; the
+ * plain kernel (variant 0) always uses FP32. */
+int usgb_set_delay_precision(usgb_ctx* ctx, uint32_t mode);
 
 /* Times every staged configuration that fits (tile rows x stage bytes x
  * stages, plus the plain kernel) on the given prepared signals, `iterations`

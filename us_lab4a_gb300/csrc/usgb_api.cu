@@ -8,6 +8,7 @@
 #include <new>
 #include <sstream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -15,12 +16,13 @@
 #include "../../include/usgb.h"
 #include "usgb_common.cuh"
 #include "usgb_internal.h"
+#include "usgb_tables.h"
 
 namespace {
 
-thread_local std::string g_createError;
+using usgb::host::kPi;
 
-constexpr double kPi = 3.14159265358979323846;
+thread_local std::string g_createError;
 
 struct Failure {
 	int code;
@@ -43,98 +45,19 @@ struct Failure {
 		}                                                                                     \
 	} while (0)
 
-// FFTUtil::nextFastEvenSize (src/fft/FFTUtil.h:85-135).
-unsigned next_fast_even_size(unsigned n)
-{
-	if (n & 1U) ++n;
-	for (;;) {
-		unsigned m = n;
-		while ((m & 1U) == 0) m >>= 1;
-		while (m % 3 == 0) m /= 3;
-		while (m % 5 == 0) m /= 5;
-		if (m == 1) return n;
-		n += 2;
-	}
-}
-
-// Kaiser-windowed sinc of Interpolator::prepare (src/util/Interpolator.h:64-111,
-// src/util/KaiserWindow.h:45-93), evaluated in float with the same mixed
-// float/double expressions as Interpolator<float>.
-std::vector<float> interpolator_taps(unsigned U, float halfTransitionWidth)
-{
-	const double kaiserTolerance = 1.0e-4;
-	const float tol_dB = -20.0 * std::log10(kaiserTolerance);
-	float beta;
-	if (tol_dB > 50) {
-		beta = 0.1102 * (tol_dB - 8.7);
-	} else if (tol_dB > 21) {
-		const double k = tol_dB - 21.0;
-		beta = 0.5842 * std::pow(k, 0.4) + 0.07886 * k;
-	} else {
-		beta = 0.0;
-	}
-	const float finalTransitionWidth = (halfTransitionWidth * 2) / U;
-	const double sz = std::ceil((tol_dB - 7.95) / (2.285 * finalTransitionWidth * kPi) + 1.0);
-	const unsigned windowSize = static_cast<unsigned>(sz);
-	const float twoUp = 2 * U;
-	const unsigned n = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
-
-	std::vector<float> window(n);
-	const float c1 = 2 / static_cast<float>(n - 1U);
-	const float c2 = 1 / std::cyl_bessel_if(0.0f, beta);
-	for (unsigned i = 0; i < n; ++i) {
-		const float k = c1 * i - 1;
-		float x = 1 - k * k;
-		if (x < 0.0f) x = 0.0f;
-		window[i] = c2 * std::cyl_bessel_if(0.0f, beta * std::sqrt(x));
-	}
-	const float numPeriods = (n - 1U) / twoUp;
-	const double step = static_cast<double>(numPeriods - (-numPeriods)) / (n - 1U);
-	std::vector<float> taps(n);
-	for (unsigned i = 0; i < n; ++i) {
-		const float xi = (i == 0) ? -numPeriods : static_cast<float>(-numPeriods + i * step);
-		const double arg = kPi * xi;
-		const double s = (std::abs(arg) < 1.0e-5) ? 1.0 - arg * arg / 6.0 : std::sin(arg) / arg;
-		taps[i] = static_cast<float>(s);
-		taps[i] *= window[i];
-	}
-	return taps;
-}
-
-// The fixed 4x FIR of the real-RF path, from the recipe stated in
-// src/util/Interpolator4X.h:56-66 (kaiser(81, 5) .* sinc(linspace(-10, 10, 81))).
-std::vector<float> interpolator4x_taps()
-{
-	const unsigned n = 80;
-	const double beta = 5.0;
-	const double i0b = std::cyl_bessel_i(0.0, beta);
-	std::vector<float> h(n + 1);
-	for (unsigned i = 0; i <= n; ++i) {
-		const double r = 2.0 * i / n - 1.0;
-		double arg = 1.0 - r * r;
-		if (arg < 0.0) arg = 0.0;
-		const double w = std::cyl_bessel_i(0.0, beta * std::sqrt(arg)) / i0b;
-		const double xv = -10.0 + 20.0 * i / n;
-		const double s = (xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv);
-		h[i] = static_cast<float>(s * w);
-	}
-	return h;
-}
-
 }  // namespace
 
 struct usgb_ctx {
 	usgb_sta_params prm{};
 	std::vector<float> txXY, rxXY, apod;
-	unsigned numSignals = 0, L = 0, N = 0, M = 0, U = 1, deadZone = 0, tapsPerPhase = 1, tapsStride = 4;
-	unsigned twHiCount = 0, csHiCount = 0;
-	std::vector<unsigned long long> divMagic;
+	unsigned numSignals = 0, L = 0, U = 1, deadZone = 0, tapsPerPhase = 1, tapsStride = 4;
+	usgb::host::FFTTables fft;   // Hilbert FFT plan (analytic path)
+	bool stageTw = false;        // per-stage twiddle tables fit in shared memory
 	unsigned sigStride = 0;
 	size_t sigBytes = 0;
 	size_t elemBytes = 0;
 	float invCT = 0, signalOffset = 0, valueCoef = 0, pcfFactor = 0, scale = 1;
 	bool analytic = true;
-	std::vector<int> radices;
 
 	float* d_txXY = nullptr;
 	float* d_rxXY = nullptr;
@@ -142,6 +65,7 @@ struct usgb_ctx {
 	float* d_polyTaps = nullptr;
 	float2* d_tw = nullptr;
 	float2* d_cs = nullptr;
+	float2* d_stw = nullptr;
 	unsigned* d_perm = nullptr;
 	float* d_rf = nullptr;
 	void* d_sig = nullptr;
@@ -161,6 +85,7 @@ struct usgb_ctx {
 	cudaStream_t stream = nullptr;
 	bool ownStream = false;
 	int dasVariant = 0;
+	int delayMode = USGB_DELAY_AUTO;
 	unsigned tileRows = 8;
 	unsigned stageBytes = 16384;
 	unsigned stages = 4;
@@ -168,7 +93,7 @@ struct usgb_ctx {
 
 	~usgb_ctx()
 	{
-		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_cs, d_perm, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
+		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_cs, d_stw, d_perm, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
 		for (void* p : dev) if (p) cudaFree(p);
 		if (h_rf) cudaFreeHost(h_rf);
 		if (h_out) cudaFreeHost(h_out);
@@ -209,84 +134,28 @@ namespace {
 
 void build_tables(usgb_ctx* c)
 {
-	// FIR.
-	std::vector<float> taps;
-	if (!c->analytic) {
-		taps = interpolator4x_taps();
-	} else if (c->U > 1) {
-		taps = interpolator_taps(c->U, 0.2f);
-	} else {
-		taps = {1.0f};
+	usgb::host::PolyTaps poly;
+	if (!usgb::host::make_poly_taps(c->analytic, c->U, poly)) {
+		USGB_FAIL(USGB_ERR_INVALID_STATE, "FIR length is not 2*U*K + 1 for upsampling " << c->U);
 	}
-	const unsigned T = static_cast<unsigned>(taps.size());
-	if (c->U > 1 && ((T - 1) % (2 * c->U) != 0)) USGB_FAIL(USGB_ERR_INVALID_STATE, "FIR length " << T << " is not 2*U*K + 1");
-	const unsigned K = (c->U > 1) ? (T - 1) / (2 * c->U) : 0;
-	c->tapsPerPhase = 2 * K + 1;
-	c->tapsStride = (c->tapsPerPhase + 3) & ~3u;
-	std::vector<float> poly(static_cast<size_t>(c->U) * c->tapsStride, 0.f);
-	for (unsigned r = 0; r < c->U; ++r) {
-		for (unsigned t = 0; t < c->tapsPerPhase; ++t) {
-			const unsigned j = r + t * c->U;
-			poly[r * c->tapsStride + t] = (j < T) ? taps[j] : 0.f;
-		}
-	}
-	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.size() * sizeof(float)));
-	USGB_CUDA(cudaMemcpy(c->d_polyTaps, poly.data(), poly.size() * sizeof(float), cudaMemcpyHostToDevice));
+	c->tapsPerPhase = poly.tapsPerPhase;
+	c->tapsStride = poly.tapsStride;
+	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.poly.size() * sizeof(float)));
+	USGB_CUDA(cudaMemcpy(c->d_polyTaps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice));
 
 	if (!c->analytic) return;
-	// Hilbert FFT: N = max(nextFastEvenSize(L + 1024), 2048)
-	// (src/util/HilbertEnvelope.h:152), computed as an N/2-point complex FFT.
-	c->N = std::max(next_fast_even_size(c->L + 1024U), 2048U);
-	c->M = c->N / 2;
-	unsigned m = c->M;
-	c->radices.clear();
-	while (m % 4 == 0) { c->radices.push_back(4); m /= 4; }
-	while (m % 2 == 0) { c->radices.push_back(2); m /= 2; }
-	while (m % 3 == 0) { c->radices.push_back(3); m /= 3; }
-	while (m % 5 == 0) { c->radices.push_back(5); m /= 5; }
-	if (m != 1 || c->radices.size() > static_cast<size_t>(usgb::kMaxFFTStages)) {
-		USGB_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << c->M << " not supported");
-	}
-	const unsigned M = c->M;
-	// Two-level twiddle tables: W^m = hi[m / S] * lo[m % S], S = kTwiddleSplit.
-	const unsigned S = usgb::kTwiddleSplit;
-	c->twHiCount = (M + S - 1) / S;
-	c->csHiCount = (M / 2 + 1 + S - 1) / S;
-	std::vector<float2> tw(S + c->twHiCount), cs(S + c->csHiCount);
-	auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
-	for (unsigned j = 0; j < S; ++j) tw[j] = unit(-2.0 * kPi * static_cast<double>(j) / M);
-	for (unsigned q = 0; q < c->twHiCount; ++q) tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
-	for (unsigned j = 0; j < S; ++j) cs[j] = unit(kPi * static_cast<double>(j) / M);
-	for (unsigned q = 0; q < c->csHiCount; ++q) cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
-	// Multiply-shift division by each DIF stage's sub-block length:
-	// floor(b / sub) = (b * ceil(2^40 / sub)) >> 40, exact for b, sub < 2^20.
-	c->divMagic.clear();
-	{
-		unsigned Ms = M;
-		for (int r : c->radices) {
-			const unsigned sub = Ms / static_cast<unsigned>(r);
-			c->divMagic.push_back(((1ULL << 40) + sub - 1) / sub);
-			Ms = sub;
-		}
-	}
-	// Digit-reversed position of bin k after the in-place DIF stages:
-	// k = k0 + r0 (k1 + r1 (k2 + ...)) sits at sum_s k_s * M / (r0 ... r_s).
-	std::vector<unsigned> perm(M);
-	for (unsigned k = 0; k < M; ++k) {
-		unsigned kk = k, pos = 0, span = M;
-		for (int r : c->radices) {
-			span /= static_cast<unsigned>(r);
-			pos += (kk % r) * span;
-			kk /= r;
-		}
-		perm[k] = pos;
-	}
-	USGB_CUDA(cudaMalloc(&c->d_tw, tw.size() * sizeof(float2)));
-	USGB_CUDA(cudaMalloc(&c->d_cs, cs.size() * sizeof(float2)));
-	USGB_CUDA(cudaMalloc(&c->d_perm, M * sizeof(unsigned)));
-	USGB_CUDA(cudaMemcpy(c->d_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice));
-	USGB_CUDA(cudaMemcpy(c->d_cs, cs.data(), cs.size() * sizeof(float2), cudaMemcpyHostToDevice));
-	USGB_CUDA(cudaMemcpy(c->d_perm, perm.data(), M * sizeof(unsigned), cudaMemcpyHostToDevice));
+	usgb::host::FFTTables& t = c->fft;
+	if (!usgb::host::make_fft_tables(c->L, t)) USGB_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << t.M << " not supported");
+	auto upload = [](auto** dst, const auto& v) {
+		using E = typename std::decay_t<decltype(v)>::value_type;
+		USGB_CUDA(cudaMalloc(dst, std::max<size_t>(v.size(), 1) * sizeof(E)));
+		if (!v.empty()) USGB_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice));
+	};
+	upload(&c->d_tw, t.tw);
+	upload(&c->d_cs, t.cs);
+	upload(&c->d_stw, t.stageTw);
+	upload(&c->d_perm, t.perm);
+	c->stageTw = true;  // cleared by check_prep_fits when the tables do not fit
 }
 
 void check_and_derive(usgb_ctx* c, const usgb_sta_params* p)
@@ -398,17 +267,13 @@ usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
 	pp.polyTaps = c->d_polyTaps;
 	pp.deadZone = c->deadZone;
 	pp.outScale = c->scale;
-	pp.M = c->M;
-	pp.numStages = static_cast<int>(c->radices.size());
-	for (size_t i = 0; i < c->radices.size(); ++i) {
-		pp.radix[i] = c->radices[i];
-		pp.divMagic[i] = c->divMagic[i];
+	if (c->analytic) {
+		usgb::host::set_fft_params(pp, c->fft);
+		pp.tw = c->d_tw;
+		pp.cs = c->d_cs;
+		pp.perm = c->d_perm;
+		pp.stw = c->stageTw ? c->d_stw : nullptr;
 	}
-	pp.tw = c->d_tw;
-	pp.twHiCount = c->twHiCount;
-	pp.cs = c->d_cs;
-	pp.csHiCount = c->csHiCount;
-	pp.perm = c->d_perm;
 	return pp;
 }
 
@@ -433,6 +298,12 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.invScale = 1.0f / c->scale;
 	dp.pcfFactor = c->pcfFactor;
 	dp.scfP = c->prm.scf_p;
+	dp.delayMode = c->delayMode;
+	{
+		const double upFs = static_cast<double>(c->prm.sampling_frequency) * c->U;
+		dp.invCTd = upFs / c->prm.propagation_speed;
+		dp.signalOffsetd = upFs * c->prm.peak_offset / c->prm.center_frequency;
+	}
 	dp.value = d_value;
 	dp.factor = d_factor;
 	dp.errWord = c->d_err;
@@ -490,13 +361,16 @@ void choose_default_das(usgb_ctx* c)
 	c->dasVariant = 0;
 }
 
-void check_prep_fits(const usgb_ctx* c)
+void check_prep_fits(usgb_ctx* c)
 {
 	int dev = 0, maxSmem = 0;
 	USGB_CUDA(cudaGetDevice(&dev));
 	USGB_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-	const usgb::PrepParams pp = prep_params(c, nullptr, nullptr);
-	const size_t need = usgb::prep_smem_bytes(pp, c->analytic);
+	size_t need = usgb::prep_smem_bytes(prep_params(c, nullptr, nullptr), c->analytic);
+	if (c->stageTw && need > static_cast<size_t>(maxSmem)) {
+		c->stageTw = false;  // every FFT stage reads the two-level table instead
+		need = usgb::prep_smem_bytes(prep_params(c, nullptr, nullptr), c->analytic);
+	}
 	if (need > static_cast<size_t>(maxSmem)) {
 		USGB_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation: needs " << need
 				<< " bytes of shared memory, the device offers " << maxSmem << " (signal length " << c->L << ").");
@@ -700,7 +574,7 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 {
 	if (!c) return USGB_ERR_INVALID_PARAMETER;
 	if (signal_length) *signal_length = c->L;
-	if (fft_size) *fft_size = c->N;
+	if (fft_size) *fft_size = c->fft.N;
 	if (signal_stride) *signal_stride = c->sigStride;
 	if (signal_bytes) *signal_bytes = c->sigBytes;
 	return USGB_OK;
@@ -729,6 +603,14 @@ int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t 
 		c->tileRows = rows;
 		c->stageBytes = cap;
 		c->stages = nst;
+	});
+}
+
+int usgb_set_delay_precision(usgb_ctx* c, uint32_t mode)
+{
+	return guarded(c, [&] {
+		if (mode > USGB_DELAY_FP64) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay precision: " << mode << '.');
+		c->delayMode = static_cast<int>(mode);
 	});
 }
 

@@ -53,11 +53,12 @@ struct StageMeta {
 // Shared-memory layout (byte offsets), computed identically on host and
 // device, for at most maxTx / maxRx elements.
 struct StagedLayout {
-	unsigned bars, meta, minmax, partial, txd, stage, total;
+	unsigned bars, tileMax, meta, minmax, partial, txd, stage, total;
 	__host__ __device__ StagedLayout(unsigned maxTx, unsigned maxRx, unsigned trows, unsigned capBytes, unsigned stages)
 	{
 		bars = 0;
-		meta = (2 * stages * 8 + 15) & ~15u;
+		tileMax = 2 * stages * 8;
+		meta = (tileMax + 8 + 15) & ~15u;
 		minmax = meta + stages * static_cast<unsigned>(sizeof(StageMeta));
 		minmax = (minmax + 15) & ~15u;
 		partial = minmax + 2 * (maxTx + maxRx) * 4;
@@ -73,6 +74,7 @@ struct StagedLayout {
 struct Smem {
 	uint64_t* full;
 	uint64_t* empty;
+	int* tileMax;    // [2]: largest transmit / receive delay of the tile (bits of a float >= 0)
 	StageMeta* meta;
 	float* minT;     // [maxTx]
 	float* maxT;     // [maxTx]
@@ -80,7 +82,7 @@ struct Smem {
 	float* maxR;     // [maxRx]
 	float* partMin;  // [TROWS][maxTx + maxRx]
 	float* partMax;
-	float* txd;      // [maxTx][P]
+	float* txd;      // [maxTx][P]: FP32 delays, or fixed-point delays (int bits) in an FP64 tile
 	unsigned char* stageBuf;
 	unsigned nst;
 	unsigned capBytes;
@@ -93,6 +95,7 @@ __device__ __forceinline__ Smem carve(unsigned char* smem, const StagedLayout& l
 	Smem s;
 	s.full = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	s.empty = s.full + nst;
+	s.tileMax = reinterpret_cast<int*>(smem + lay.tileMax);
 	s.meta = reinterpret_cast<StageMeta*>(smem + lay.meta);
 	s.minT = reinterpret_cast<float*>(smem + lay.minmax);
 	s.maxT = s.minT + maxTx;
@@ -111,6 +114,7 @@ __device__ __forceinline__ Smem carve(unsigned char* smem, const StagedLayout& l
 template<bool ANALYTIC, int S> struct Sample;
 template<int S> struct Sample<true, S> {
 	using T = typename Complex<S>::T;
+	static constexpr bool kAnalytic = true;
 	static constexpr int kAlign = 16 / static_cast<int>(sizeof(T));  // elements per 16 bytes
 	static __device__ __forceinline__ void accumulate(const T* s, float k, float2& acc)
 	{
@@ -125,6 +129,7 @@ template<int S> struct Sample<true, S> {
 };
 template<int S> struct Sample<false, S> {
 	using T = typename Real<S>::T;
+	static constexpr bool kAnalytic = false;
 	static constexpr int kAlign = 16 / static_cast<int>(sizeof(T));
 	static __device__ __forceinline__ void accumulate(const T* s, float k, float2& acc)
 	{
@@ -133,8 +138,36 @@ template<int S> struct Sample<false, S> {
 	}
 };
 
-// floor(d) by one round-down add against 2^23 (split_delay of the plain
-// kernel): every d outside [0, 2^23) gives an index the unsigned test rejects.
+// ----------------------------------------------------------------- delays
+// FP32 tiles: delay d = fl(txd + rxd) as in the reference; floor(d) by one
+// round-down add against 2^23 (split_delay of the plain kernel): every d
+// outside [0, 2^23) gives an index the unsigned range test rejects.
+//
+// FP64 tiles: the per-pixel transmit and receive delays are computed in
+// double and stored as int32 fixed point with F fractional bits, F chosen per
+// tile so that every term stays below 2^30 in magnitude (a sum never
+// overflows): F = 30 - ceil(log2(largest |term| + 2)), at most 20 (2^-20
+// sample) and at least 9 for delays up to 2^21 samples. A gather adds the two
+// integers, idx = q >> F (floor, negative for negative delays) and k = the
+// low F bits / 2^F, both exact.
+struct Fixed {
+	int F;           // fractional bits
+	int mask;        // 2^F - 1
+	int shift;       // 23 - F: places the fraction in a float mantissa
+	double scale;    // 2^F
+};
+
+__device__ __forceinline__ Fixed fixed_format(float largest)
+{
+	const int e = ((__float_as_int(largest + 2.0f) >> 23) & 0xff) - 126;  // largest + 2 < 2^e
+	Fixed f;
+	f.F = max(9, min(20, 30 - e));
+	f.mask = (1 << f.F) - 1;
+	f.shift = 23 - f.F;
+	f.scale = static_cast<double>(1 << f.F);
+	return f;
+}
+
 __device__ __forceinline__ int split_delay(float d, float& k)
 {
 	const float t0 = __fadd_rd(d, 8388608.0f);
@@ -142,26 +175,66 @@ __device__ __forceinline__ int split_delay(float d, float& k)
 	return static_cast<int>(__float_as_uint(t0) - 0x4B000000u);
 }
 
-// Contribution of one staged (or empty) window to one grid point: delay
-// d = txd + rxd, idx = floor(d), k = d - idx, acc += (1-k) s[idx] + k s[idx+1].
-// Every delay of the tile lies inside its window, so the range test alone
-// guards the stage read; an empty window rejects every index.
-template<typename SP>
-__device__ __forceinline__ void gather_staged(const typename SP::T* buf, int base, float txdv, float rxd,
-		unsigned lastIdx, float2& acc)
+__device__ __forceinline__ float to_fixed(double tau, const Fixed& f)
+{
+	return __int_as_float(__double2int_rn(fmin(fmax(tau * f.scale, -1073741823.0), 1073741823.0)));
+}
+
+__device__ __forceinline__ double distance3d_z0_f64(float ex, float ey, float px, float py, float pz)
+{
+	const double dx = static_cast<double>(px) - ex;
+	const double dy = static_cast<double>(py) - ey;
+	const double dz = pz;
+	return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+template<bool Q> struct Delay;
+template<> struct Delay<false> {
+	static __device__ __forceinline__ int split(float txv, float rxv, float& k, const Fixed&)
+	{
+		return split_delay(__fadd_rn(txv, rxv), k);
+	}
+	static __device__ __forceinline__ float rx(const DasParams& p, unsigned r, float px, float py, float pz,
+			const Fixed&)
+	{
+		return __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
+	}
+};
+template<> struct Delay<true> {
+	static __device__ __forceinline__ int split(float txv, float rxv, float& k, const Fixed& f)
+	{
+		const int q = __float_as_int(txv) + __float_as_int(rxv);
+		k = __int_as_float(0x3F800000 | ((q & f.mask) << f.shift)) - 1.0f;
+		return q >> f.F;
+	}
+	static __device__ __forceinline__ float rx(const DasParams& p, unsigned r, float px, float py, float pz,
+			const Fixed& f)
+	{
+		return to_fixed(distance3d_z0_f64(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz) * p.invCTd, f);
+	}
+};
+
+// Contribution of one staged (or empty) window to one grid point:
+// acc += (1-k) s[idx] + k s[idx+1]. Every delay of the tile lies inside its
+// window, so the range test alone guards the stage read; an empty window
+// rejects every index.
+template<typename SP, bool Q>
+__device__ __forceinline__ void gather_staged(const typename SP::T* buf, int base, float txv, float rxv,
+		unsigned lastIdx, const Fixed& fx, float2& acc)
 {
 	float k;
-	const int i = split_delay(__fadd_rn(txdv, rxd), k);
+	const int i = Delay<Q>::split(txv, rxv, k, fx);
 	if (static_cast<unsigned>(i) <= lastIdx) SP::accumulate(buf + (i + base), k, acc);
 }
 
 // Any window kind: staged, empty, or gathered from global memory.
-template<typename SP>
+template<typename SP, bool Q>
 __device__ __forceinline__ void gather_any(int4 wm, const typename SP::T* buf, const typename SP::T* sig,
-		size_t txStride, unsigned r, size_t sigStride, float txdv, float rxd, unsigned lastIdx, float2& acc)
+		size_t txStride, unsigned r, size_t sigStride, float txv, float rxv, unsigned lastIdx, const Fixed& fx,
+		float2& acc)
 {
 	float k;
-	const int i = split_delay(__fadd_rn(txdv, rxd), k);
+	const int i = Delay<Q>::split(txv, rxv, k, fx);
 	if (static_cast<unsigned>(i) <= lastIdx) {
 		if (wm.z >= 0) {
 			SP::accumulate(buf + (i + wm.y), k, acc);
@@ -183,6 +256,206 @@ __device__ __forceinline__ void init_barriers(const Smem& sm, int trows)
 	__syncthreads();
 }
 
+// ------------------------------------------------------------- producer
+// The 32 lanes size 32 consecutive transmit windows of the current receiver
+// at once; a prefix sum packs as many as fit into the stage, lane 0 arms the
+// stage's barrier with the total byte count and every lane issues its own
+// bulk copy. `margin` widens every window (FP64 tiles: their delays may sit
+// a fraction of a sample outside the FP32 bounds the windows come from).
+template<typename SP, int TROWS>
+__device__ bool produce(const DasParams& p, const Smem& sm, int& it, float margin)
+{
+	using T = typename SP::T;
+	constexpr int P = 32 * TROWS;
+	const int nst = static_cast<int>(sm.nst);
+	const unsigned capBytes = sm.capBytes;
+	const int lane = threadIdx.x & 31;
+	const int L = static_cast<int>(p.L);
+	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
+	const T* sig = reinterpret_cast<const T*>(p.sig);
+	const int itStart = it;
+	// Ring slot and phase of stage `it`, carried along (no division per stage).
+	int s = it % nst;
+	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
+	bool ok = true;
+	for (unsigned r = 0; r < p.numRx && ok; ++r) {
+		unsigned t0 = 0;
+		while (t0 < p.numTx) {
+			if (it >= nst) {
+				bool w = true;
+				if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], phase ^ 1u, kWaitLimitNs);
+				w = __shfl_sync(0xffffffffu, w, 0);
+				if (!w) {
+					if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+					ok = false;
+					break;
+				}
+			}
+			const unsigned t = t0 + lane;
+			int lo = 0, kind = kEmptyWindow;
+			unsigned wb = 0;
+			if (t < p.numTx) {
+				const float a = __fadd_rn(sm.minT[t], sm.minR[r]);
+				const float b = __fadd_rn(sm.maxT[t], sm.maxR[r]);
+				// Window [lo, hi] of sample indices (a valid gather reads idx and idx + 1).
+				const float lof = fmaxf(floorf(a) - margin, 0.0f);
+				const float hif = fminf(floorf(b) + 1.0f + margin, static_cast<float>(L - 1));
+				if (lof <= static_cast<float>(L - 2) && hif >= 1.0f && hif >= lof) {
+					lo = static_cast<int>(lof) & ~(SP::kAlign - 1);
+					const unsigned cnt = static_cast<unsigned>(static_cast<int>(hif) - lo + 1);
+					wb = (cnt * static_cast<unsigned>(sizeof(T)) + 15u) & ~15u;
+					if (wb > capBytes) {  // larger than a whole stage: consumers read global memory
+						kind = kGlobalWindow;
+						wb = 0;
+					} else {
+						kind = 0;
+					}
+				}
+			}
+			unsigned incl = wb;
+			for (int o = 1; o < 32; o <<= 1) {
+				const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+				if (lane >= o) incl += v;
+			}
+			// Lanes that fit form a prefix (incl is non-decreasing); lane 0
+			// always fits, since an oversized window carries no bytes.
+			const bool fits = t < p.numTx && incl <= capBytes;
+			const int n = __popc(__ballot_sync(0xffffffffu, fits));
+			const bool anyGlobal = __ballot_sync(0xffffffffu, fits && kind == kGlobalWindow) != 0u;
+			const unsigned total = __shfl_sync(0xffffffffu, incl, n - 1);
+			const unsigned excl = incl - wb;
+			StageMeta& m = sm.meta[s];
+			if (lane < n) {
+				const int base = (kind == 0) ? static_cast<int>(excl / sizeof(T)) - lo : 0;
+				m.win[lane] = make_int4(static_cast<int>(t * (P * 4u)), base, kind, static_cast<int>(t));
+			}
+			if (lane == 0) {
+				m.count = n;
+				m.lastOfRx = (t0 + n == p.numTx) ? 1 : 0;
+				m.firstOdd = static_cast<int>(t0 & 1u);
+				m.anyGlobal = anyGlobal ? 1 : 0;
+			}
+			__threadfence_block();
+			__syncwarp();
+			if (lane == 0) mbar_arrive_expect_tx(&sm.full[s], total);
+			__syncwarp();
+			if (lane < n && wb > 0) {
+				const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
+				bulk_copy_g2s(sm.stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &sm.full[s]);
+			}
+			t0 += static_cast<unsigned>(n);
+			++it;
+			if (++s == nst) {
+				s = 0;
+				phase ^= 1u;
+			}
+		}
+	}
+	// Let this tile's last copies land before the block moves on or exits.
+	if (lane == 0) {
+		const int from = (it - nst > itStart) ? it - nst : itStart;
+		for (int j = from; j < it; ++j) {
+			if (!mbar_wait_bounded(&sm.full[j % nst], (j / nst) & 1, kWaitLimitNs)) {
+				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+				ok = false;
+				break;
+			}
+		}
+	}
+	return ok;
+}
+
+// ------------------------------------------------------------- consumers
+// Receiver-major: per receiver, every staged window (one per transmitter) of
+// the grid point; its even / odd transmitter terms go to two accumulators.
+template<typename SP, int CF, int TROWS, bool Q>
+__device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, float py, float pz, bool active,
+		unsigned pix, const Fixed& fx)
+{
+	using T = typename SP::T;
+	const int nst = static_cast<int>(sm.nst);
+	const unsigned capBytes = sm.capBytes;
+	const int slot = threadIdx.x;
+	const unsigned lastIdx = p.L - 2;
+	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
+	const T* sig = reinterpret_cast<const T*>(p.sig);
+	const char* txdSlot = reinterpret_cast<const char*>(sm.txd + slot);
+	float2 total = make_float2(0.f, 0.f);
+	CFState<CF> cf;
+	float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+	unsigned r = 0;
+	float rxd = Delay<Q>::rx(p, 0, px, py, pz, fx);
+	// Ring slot and phase of stage `it`, carried along (no division per stage).
+	int s = it % nst;
+	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
+	while (r < p.numRx) {
+		if (!mbar_wait_bounded(&sm.full[s], phase, kWaitLimitNs)) {
+			atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+			return false;
+		}
+		const StageMeta& m = sm.meta[s];
+		const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
+		const int4 head = *reinterpret_cast<const int4*>(&m.count);
+		const int n = head.x;
+		// Windows of a stage are consecutive transmitters of receiver r:
+		// window w goes to the accumulator of its transmitter's parity. With
+		// the accumulators swapped for a stage that starts on an odd
+		// transmitter, even w is always `a0` and odd w `a1`.
+		float2 a0 = accEven, a1 = accOdd;
+		if (head.z) { a0 = accOdd; a1 = accEven; }
+		if (!head.w) {
+			int w = 0;
+			// Four windows per iteration (two per accumulator): four independent
+			// delay / load chains in flight per thread.
+#pragma unroll 2
+			for (; w + 1 < n; w += 2) {
+				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
+				const int2 wb = *reinterpret_cast<const int2*>(&m.win[w + 1]);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, a0);
+				gather_staged<SP, Q>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, fx, a1);
+			}
+			if (w < n) {
+				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, a0);
+			}
+		} else {
+			for (int w = 0; w < n; ++w) {
+				const int4 wa = m.win[w];
+				const float txv = *reinterpret_cast<const float*>(txdSlot + wa.x);
+				if (w & 1) gather_any<SP, Q>(wa, buf, sig, txStride, r, p.sigStride, txv, rxd, lastIdx, fx, a1);
+				else gather_any<SP, Q>(wa, buf, sig, txStride, r, p.sigStride, txv, rxd, lastIdx, fx, a0);
+			}
+		}
+		if (head.z) { accOdd = a0; accEven = a1; }
+		else { accEven = a0; accOdd = a1; }
+		const int last = head.y;
+		__syncwarp();
+		if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.empty[s]);
+		++it;
+		if (++s == nst) {
+			s = 0;
+			phase ^= 1u;
+		}
+		if (last) {
+			const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
+			const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
+			total.x += rs.x;
+			total.y += rs.y;
+			cf.add(rs);
+			accEven = make_float2(0.f, 0.f);
+			accOdd = make_float2(0.f, 0.f);
+			++r;
+			if (r < p.numRx) rxd = Delay<Q>::rx(p, r, px, py, pz, fx);
+		}
+	}
+	if (active) {
+		const float v = SP::kAnalytic ? magnitude(total) : total.x;
+		p.value[pix] = v * p.valueCoef;
+		p.factor[pix] = cf.result(p.numRx, p, total);
+	}
+	return true;
+}
+
 // One tile (bx, by) of one frame. `it` is the block's running stage counter
 // (the same value in every thread on entry and on exit). Returns false after a
 // wait gave up (the error is recorded in p.errWord).
@@ -190,10 +463,7 @@ template<int S, int CF, bool ANALYTIC, int TROWS>
 __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, unsigned by, int& it)
 {
 	using SP = Sample<ANALYTIC, S>;
-	using T = typename SP::T;
 	constexpr int P = 32 * TROWS;
-	const int nst = static_cast<int>(sm.nst);
-	const unsigned capBytes = sm.capBytes;
 	const int warp = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
 	const bool producer = warp == TROWS;
@@ -214,7 +484,11 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 		py = p.grid[3 * q + 1];
 		pz = p.grid[3 * q + 2];
 	}
-	// Transmit-delay table and per-warp min/max of every element's delay.
+	if (threadIdx.x == 0) {
+		sm.tileMax[0] = 0;
+		sm.tileMax[1] = 0;
+	}
+	// FP32 transmit-delay table and per-warp min/max of every element's delay.
 	if (!producer) {
 		for (unsigned e = 0; e < nE; ++e) {
 			float v;
@@ -238,183 +512,36 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 		}
 	}
 	__syncthreads();
+	float topT = 0.f, topR = 0.f;
 	for (unsigned e = threadIdx.x; e < nE; e += blockDim.x) {
 		float mn = sm.partMin[e], mx = sm.partMax[e];
 		for (int w = 1; w < TROWS; ++w) {
 			mn = fminf(mn, sm.partMin[w * sm.maxE + e]);
 			mx = fmaxf(mx, sm.partMax[w * sm.maxE + e]);
 		}
-		if (e < p.numTx) { sm.minT[e] = mn; sm.maxT[e] = mx; }
-		else { sm.minR[e - p.numTx] = mn; sm.maxR[e - p.numTx] = mx; }
+		if (e < p.numTx) { sm.minT[e] = mn; sm.maxT[e] = mx; topT = fmaxf(topT, mx); }
+		else { sm.minR[e - p.numTx] = mn; sm.maxR[e - p.numTx] = mx; topR = fmaxf(topR, mx); }
 	}
+	// Non-negative floats order like their bit patterns.
+	if (topT > 0.f) atomicMax(&sm.tileMax[0], __float_as_int(topT));
+	if (topR > 0.f) atomicMax(&sm.tileMax[1], __float_as_int(topR));
 	__syncthreads();
 
-	const int L = static_cast<int>(p.L);
-	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
-	const T* sig = reinterpret_cast<const T*>(p.sig);
-	bool ok = true;
-
-	if (producer) {
-		// -------------------------------------------------------------- producer
-		// The 32 lanes size 32 consecutive transmit windows of the current
-		// receiver at once; a prefix sum packs as many as fit into the stage,
-		// lane 0 arms the stage's barrier with the total byte count and every
-		// lane issues its own bulk copy.
-		const int itStart = it;
-		for (unsigned r = 0; r < p.numRx && ok; ++r) {
-			unsigned t0 = 0;
-			while (t0 < p.numTx) {
-				const int s = it % nst;
-				if (it >= nst) {
-					bool w = true;
-					if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], ((it / nst) - 1) & 1, kWaitLimitNs);
-					w = __shfl_sync(0xffffffffu, w, 0);
-					if (!w) {
-						if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-						ok = false;
-						break;
-					}
-				}
-				const unsigned t = t0 + lane;
-				int lo = 0, kind = kEmptyWindow;
-				unsigned wb = 0;
-				if (t < p.numTx) {
-					const float a = __fadd_rn(sm.minT[t], sm.minR[r]);
-					const float b = __fadd_rn(sm.maxT[t], sm.maxR[r]);
-					// Window [lo, hi] of sample indices (a valid gather reads idx and idx + 1).
-					const float lof = fmaxf(floorf(a), 0.0f);
-					const float hif = fminf(floorf(b) + 1.0f, static_cast<float>(L - 1));
-					if (lof <= static_cast<float>(L - 2) && hif >= 1.0f && hif >= lof) {
-						lo = static_cast<int>(lof) & ~(SP::kAlign - 1);
-						const unsigned cnt = static_cast<unsigned>(static_cast<int>(hif) - lo + 1);
-						wb = (cnt * static_cast<unsigned>(sizeof(T)) + 15u) & ~15u;
-						if (wb > capBytes) {  // larger than a whole stage: consumers read global memory
-							kind = kGlobalWindow;
-							wb = 0;
-						} else {
-							kind = 0;
-						}
-					}
-				}
-				unsigned incl = wb;
-				for (int o = 1; o < 32; o <<= 1) {
-					const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
-					if (lane >= o) incl += v;
-				}
-				// Lanes that fit form a prefix (incl is non-decreasing); lane 0
-				// always fits, since an oversized window carries no bytes.
-				const bool fits = t < p.numTx && incl <= capBytes;
-				const int n = __popc(__ballot_sync(0xffffffffu, fits));
-				const bool anyGlobal = __ballot_sync(0xffffffffu, fits && kind == kGlobalWindow) != 0u;
-				const unsigned total = __shfl_sync(0xffffffffu, incl, n - 1);
-				const unsigned excl = incl - wb;
-				StageMeta& m = sm.meta[s];
-				if (lane < n) {
-					const int base = (kind == 0) ? static_cast<int>(excl / sizeof(T)) - lo : 0;
-					m.win[lane] = make_int4(static_cast<int>(t * (P * 4u)), base, kind, static_cast<int>(t));
-				}
-				if (lane == 0) {
-					m.count = n;
-					m.lastOfRx = (t0 + n == p.numTx) ? 1 : 0;
-					m.firstOdd = static_cast<int>(t0 & 1u);
-					m.anyGlobal = anyGlobal ? 1 : 0;
-				}
-				__threadfence_block();
-				__syncwarp();
-				if (lane == 0) mbar_arrive_expect_tx(&sm.full[s], total);
-				__syncwarp();
-				if (lane < n && wb > 0) {
-					const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
-					bulk_copy_g2s(sm.stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &sm.full[s]);
-				}
-				t0 += static_cast<unsigned>(n);
-				++it;
-			}
-		}
-		// Let this tile's last copies land before the block moves on or exits.
-		if (lane == 0) {
-			const int from = (it - nst > itStart) ? it - nst : itStart;
-			for (int j = from; j < it; ++j) {
-				if (!mbar_wait_bounded(&sm.full[j % nst], (j / nst) & 1, kWaitLimitNs)) {
-					atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-					ok = false;
-					break;
-				}
-			}
-		}
-	} else {
-		// ------------------------------------------------------------ consumers
-		const unsigned lastIdx = static_cast<unsigned>(L - 2);
-		const char* txdSlot = reinterpret_cast<const char*>(sm.txd + slot);
-		float2 total = make_float2(0.f, 0.f);
-		CFState<CF> cf;
-		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
-		unsigned r = 0;
-		float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[0]), __ldg(&p.rxXY[1]), px, py, pz), p.invCT);
-		while (r < p.numRx) {
-			const int s = it % nst;
-			if (!mbar_wait_bounded(&sm.full[s], (it / nst) & 1, kWaitLimitNs)) {
-				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
-				ok = false;
-				break;
-			}
-			const StageMeta& m = sm.meta[s];
-			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
-			const int4 head = *reinterpret_cast<const int4*>(&m.count);
-			const int n = head.x;
-			// Windows of a stage are consecutive transmitters of receiver r:
-			// window w goes to the accumulator of its transmitter's parity. With
-			// the accumulators swapped for a stage that starts on an odd
-			// transmitter, even w is always `a0` and odd w `a1`.
-			float2 a0 = accEven, a1 = accOdd;
-			if (head.z) { a0 = accOdd; a1 = accEven; }
-			if (!head.w) {
-				int w = 0;
-				for (; w + 1 < n; w += 2) {
-					const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
-					const int2 wb = *reinterpret_cast<const int2*>(&m.win[w + 1]);
-					gather_staged<SP>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, a0);
-					gather_staged<SP>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, a1);
-				}
-				if (w < n) {
-					const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
-					gather_staged<SP>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, a0);
-				}
-			} else {
-				for (int w = 0; w < n; ++w) {
-					const int4 wa = m.win[w];
-					const float txdv = *reinterpret_cast<const float*>(txdSlot + wa.x);
-					if (w & 1) gather_any<SP>(wa, buf, sig, txStride, r, p.sigStride, txdv, rxd, lastIdx, a1);
-					else gather_any<SP>(wa, buf, sig, txStride, r, p.sigStride, txdv, rxd, lastIdx, a0);
-				}
-			}
-			if (head.z) { accOdd = a0; accEven = a1; }
-			else { accEven = a0; accOdd = a1; }
-			const int last = head.y;
-			__syncwarp();
-			if (lane == 0) mbar_arrive(&sm.empty[s]);
-			++it;
-			if (last) {
-				const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
-				const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
-				total.x += rs.x;
-				total.y += rs.y;
-				cf.add(rs);
-				accEven = make_float2(0.f, 0.f);
-				accOdd = make_float2(0.f, 0.f);
-				++r;
-				if (r < p.numRx) {
-					rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
-				}
-			}
-		}
-		if (ok && active) {
-			const float v = ANALYTIC ? magnitude(total) : total.x;
-			p.value[pix] = v * p.valueCoef;
-			p.factor[pix] = cf.result(p.numRx, p, total);
+	// FP64 geometry where the FP32 delays could be off by more than 1/64
+	// sample: the tile's largest delay is above kDeepDelaySamples.
+	const float topTx = __int_as_float(sm.tileMax[0]), topRx = __int_as_float(sm.tileMax[1]);
+	const bool q = p.delayMode == 2 || (p.delayMode == 0 && topTx + topRx > kDeepDelaySamples);
+	const Fixed fx = fixed_format(fmaxf(fmaxf(topTx, topRx), fabsf(p.signalOffset)));
+	if (q && !producer) {
+		// Each thread replaces only its own column of the table.
+		for (unsigned t = 0; t < p.numTx; ++t) {
+			const double dist = distance3d_z0_f64(__ldg(&p.txXY[2 * t]), __ldg(&p.txXY[2 * t + 1]), px, py, pz);
+			sm.txd[t * P + slot] = to_fixed(p.signalOffsetd + dist * p.invCTd, fx);
 		}
 	}
-	return ok;
+	if (producer) return produce<SP, TROWS>(p, sm, it, q ? 2.0f : 0.0f);
+	return q ? consume<SP, CF, TROWS, true>(p, sm, it, px, py, pz, active, pix, fx)
+	         : consume<SP, CF, TROWS, false>(p, sm, it, px, py, pz, active, pix, fx);
 }
 
 // Single frame: one block per tile.

@@ -10,6 +10,10 @@ namespace usgb {
 constexpr int kPrepThreads = 512;
 constexpr int kMaxFFTStages = 24;
 constexpr unsigned kTwiddleSplit = 128;   // two-level twiddle tables: W^m = hi[m / 128] * lo[m % 128]
+// FP32 delays (a sum of two rounded products of rounded distances) are off by
+// at most about 8 * 2^-24 * d samples; above 32768 samples that can exceed
+// 1/64 sample, and the staged kernel switches the tile to FP64 geometry.
+constexpr float kDeepDelaySamples = 32768.0f;
 
 // One launch of the signal-preparation kernel over `numSignals` A-scans.
 struct PrepParams {
@@ -35,6 +39,12 @@ struct PrepParams {
 	const float2* cs;            // csLo (128) then csHi: (cos, sin)(pi k / M), k <= M/2
 	unsigned csHiCount;
 	const unsigned* perm;        // M entries, digit-reversed position of bin k
+	// Per-stage twiddle tables (stage s >= 1: W_Ms^j, j < Ms / radix, at
+	// stw + stwOffset[s]); null when they do not fit in shared memory, and
+	// every stage then reads the two-level table.
+	const float2* stw;
+	unsigned stwCount;
+	unsigned stwOffset[kMaxFFTStages];
 };
 
 size_t prep_smem_bytes(const PrepParams& p, bool analytic);
@@ -57,6 +67,13 @@ struct DasParams {
 	float invScale;              // 1 / storage scale
 	float pcfFactor;             // gamma / sigma0
 	float scfP;
+	// Delay precision of the staged kernel: 0 = FP64 geometry for the tiles
+	// whose FP32 delay error could exceed 1/64 sample (largest delay above
+	// kDeepDelaySamples), FP32 elsewhere; 1 = FP32 everywhere; 2 = FP64
+	// everywhere. invCTd / signalOffsetd are invCT / signalOffset in double.
+	int delayMode;
+	double invCTd;
+	double signalOffsetd;
 	float* value;
 	float* factor;
 	unsigned* errWord;

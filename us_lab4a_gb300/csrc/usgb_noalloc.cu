@@ -35,6 +35,7 @@
 #include "../../include/usgb.h"
 #include "usgb_common.cuh"
 #include "usgb_internal.h"
+#include "usgb_tables.h"
 
 namespace {
 
@@ -42,7 +43,7 @@ constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 
-constexpr double kPi = 3.14159265358979323846;
+using usgb::host::kPi;
 
 std::mutex g_addrMutex;
 std::vector<void*> g_scratchAddr;  // per device ordinal; nullptr until looked up
@@ -81,65 +82,9 @@ void* scratch_address()
 	return g_scratchAddr[dev];
 }
 
-unsigned next_fast_even(unsigned n)
-{
-	if (n & 1U) ++n;
-	for (;;) {
-		unsigned m = n;
-		while ((m & 1U) == 0) m >>= 1;
-		while (m % 3 == 0) m /= 3;
-		while (m % 5 == 0) m /= 5;
-		if (m == 1) return n;
-		n += 2;
-	}
-}
-
-// Kaiser-windowed sinc of the analytic path (Interpolator::prepare,
-// src/util/Interpolator.h:64-111), in float.
-std::vector<float> analytic_taps(unsigned U)
-{
-	const float halfTransitionWidth = 0.2f;
-	const float tol_dB = -20.0 * std::log10(1.0e-4);
-	const float beta = 0.1102 * (tol_dB - 8.7);
-	const float finalTransitionWidth = (halfTransitionWidth * 2) / U;
-	const unsigned windowSize = static_cast<unsigned>(std::ceil((tol_dB - 7.95) / (2.285 * finalTransitionWidth * kPi) + 1.0));
-	const float twoUp = 2 * U;
-	const unsigned n = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
-	const float c1 = 2 / static_cast<float>(n - 1U);
-	const float c2 = 1 / std::cyl_bessel_if(0.0f, beta);
-	const float numPeriods = (n - 1U) / twoUp;
-	const double step = static_cast<double>(numPeriods - (-numPeriods)) / (n - 1U);
-	std::vector<float> taps(n);
-	for (unsigned i = 0; i < n; ++i) {
-		const float k = c1 * i - 1;
-		float x = 1 - k * k;
-		if (x < 0.0f) x = 0.0f;
-		const float w = c2 * std::cyl_bessel_if(0.0f, beta * std::sqrt(x));
-		const float xi = (i == 0) ? -numPeriods : static_cast<float>(-numPeriods + i * step);
-		const double arg = kPi * xi;
-		taps[i] = static_cast<float>((std::abs(arg) < 1.0e-5) ? 1.0 - arg * arg / 6.0 : std::sin(arg) / arg);
-		taps[i] *= w;
-	}
-	return taps;
-}
-
-// The fixed 4x FIR of the real path (kaiser(81, 5) .* sinc(linspace(-10, 10, 81))).
-std::vector<float> real4x_taps()
-{
-	const double i0b = std::cyl_bessel_i(0.0, 5.0);
-	std::vector<float> h(81);
-	for (unsigned i = 0; i <= 80; ++i) {
-		const double r = 2.0 * i / 80 - 1.0;
-		const double w = std::cyl_bessel_i(0.0, 5.0 * std::sqrt(std::max(0.0, 1.0 - r * r))) / i0b;
-		const double xv = -10.0 + 20.0 * i / 80;
-		h[i] = static_cast<float>(((xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv)) * w);
-	}
-	return h;
-}
-
 // Byte layout of one call inside the scratch array.
 struct Layout {
-	size_t err, taps, tw, cs, perm, tx, rx, apod, sig, total;
+	size_t err, taps, tw, cs, stw, perm, tx, rx, apod, sig, total;
 };
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -189,58 +134,13 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	const unsigned numSignals = p->num_tx * p->num_rx;
 
 	// ---- host tables (no device memory involved) ----
-	const std::vector<float> taps = !analytic ? real4x_taps() : (U > 1 ? analytic_taps(U) : std::vector<float>{1.0f});
-	const unsigned T = static_cast<unsigned>(taps.size());
-	const unsigned K = (U > 1) ? (T - 1) / (2 * U) : 0;
-	const unsigned tapsPerPhase = 2 * K + 1;
-	const unsigned tapsStride = (tapsPerPhase + 3) & ~3u;
-	std::vector<float> poly(static_cast<size_t>(U) * tapsStride, 0.f);
-	for (unsigned r = 0; r < U; ++r)
-		for (unsigned t = 0; t < tapsPerPhase; ++t)
-			if (r + t * U < T) poly[r * tapsStride + t] = taps[r + t * U];
-
+	usgb::host::PolyTaps poly;
+	if (!usgb::host::make_poly_taps(analytic, U, poly)) NA_FAIL(USGB_ERR_INVALID_STATE, "FIR length is not 2*U*K + 1");
 	usgb::PrepParams pp{};
-	std::vector<float2> tw, cs;
-	std::vector<unsigned> perm;
+	usgb::host::FFTTables fft;
 	if (analytic) {
-		const unsigned N = std::max(next_fast_even(L + 1024U), 2048U);
-		const unsigned M = N / 2;
-		std::vector<int> radices;
-		unsigned m = M;
-		while (m % 4 == 0) { radices.push_back(4); m /= 4; }
-		while (m % 2 == 0) { radices.push_back(2); m /= 2; }
-		while (m % 3 == 0) { radices.push_back(3); m /= 3; }
-		while (m % 5 == 0) { radices.push_back(5); m /= 5; }
-		if (m != 1 || radices.size() > static_cast<size_t>(usgb::kMaxFFTStages)) NA_FAIL(USGB_ERR_INVALID_STATE, "FFT size not supported");
-		const unsigned S = usgb::kTwiddleSplit;
-		pp.M = M;
-		pp.twHiCount = (M + S - 1) / S;
-		pp.csHiCount = (M / 2 + 1 + S - 1) / S;
-		auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
-		tw.resize(S + pp.twHiCount);
-		cs.resize(S + pp.csHiCount);
-		for (unsigned j = 0; j < S; ++j) tw[j] = unit(-2.0 * kPi * j / M);
-		for (unsigned q = 0; q < pp.twHiCount; ++q) tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
-		for (unsigned j = 0; j < S; ++j) cs[j] = unit(kPi * j / M);
-		for (unsigned q = 0; q < pp.csHiCount; ++q) cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
-		perm.resize(M);
-		for (unsigned k = 0; k < M; ++k) {
-			unsigned kk = k, pos = 0, span = M;
-			for (int r : radices) {
-				span /= static_cast<unsigned>(r);
-				pos += (kk % r) * span;
-				kk /= r;
-			}
-			perm[k] = pos;
-		}
-		pp.numStages = static_cast<int>(radices.size());
-		unsigned Ms = M;
-		for (size_t i = 0; i < radices.size(); ++i) {
-			pp.radix[i] = radices[i];
-			const unsigned sub = Ms / static_cast<unsigned>(radices[i]);
-			pp.divMagic[i] = ((1ULL << 40) + sub - 1) / sub;
-			Ms = sub;
-		}
+		if (!usgb::host::make_fft_tables(L, fft)) NA_FAIL(USGB_ERR_INVALID_STATE, "FFT size not supported");
+		usgb::host::set_fft_params(pp, fft);
 	}
 	std::vector<float> apod(p->num_rx, 1.0f);
 	if (analytic && p->rx_apod) apod.assign(p->rx_apod, p->rx_apod + p->num_rx);
@@ -251,10 +151,11 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	Layout lay{};
 	size_t off = 0;
 	lay.err = off; off = align256(off + sizeof(unsigned));
-	lay.taps = off; off = align256(off + poly.size() * sizeof(float));
-	lay.tw = off; off = align256(off + tw.size() * sizeof(float2));
-	lay.cs = off; off = align256(off + cs.size() * sizeof(float2));
-	lay.perm = off; off = align256(off + perm.size() * sizeof(unsigned));
+	lay.taps = off; off = align256(off + poly.poly.size() * sizeof(float));
+	lay.tw = off; off = align256(off + fft.tw.size() * sizeof(float2));
+	lay.cs = off; off = align256(off + fft.cs.size() * sizeof(float2));
+	lay.stw = off; off = align256(off + fft.stageTw.size() * sizeof(float2));
+	lay.perm = off; off = align256(off + fft.perm.size() * sizeof(unsigned));
 	lay.tx = off; off = align256(off + 2 * p->num_tx * sizeof(float));
 	lay.rx = off; off = align256(off + 2 * p->num_rx * sizeof(float));
 	lay.apod = off; off = align256(off + apod.size() * sizeof(float));
@@ -269,11 +170,15 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	// ---- device work: everything below writes into the fixed array ----
 	unsigned char* base = static_cast<unsigned char*>(scratch_address());
 	NA_CUDA(cudaMemsetAsync(base + lay.err, 0, sizeof(unsigned), stream));
-	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.data(), poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
 	if (analytic) {
-		NA_CUDA(cudaMemcpyAsync(base + lay.tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
-		NA_CUDA(cudaMemcpyAsync(base + lay.cs, cs.data(), cs.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
-		NA_CUDA(cudaMemcpyAsync(base + lay.perm, perm.data(), perm.size() * sizeof(unsigned), cudaMemcpyHostToDevice, stream));
+		NA_CUDA(cudaMemcpyAsync(base + lay.tw, fft.tw.data(), fft.tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
+		NA_CUDA(cudaMemcpyAsync(base + lay.cs, fft.cs.data(), fft.cs.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
+		if (!fft.stageTw.empty()) {
+			NA_CUDA(cudaMemcpyAsync(base + lay.stw, fft.stageTw.data(), fft.stageTw.size() * sizeof(float2),
+					cudaMemcpyHostToDevice, stream));
+		}
+		NA_CUDA(cudaMemcpyAsync(base + lay.perm, fft.perm.data(), fft.perm.size() * sizeof(unsigned), cudaMemcpyHostToDevice, stream));
 	}
 	NA_CUDA(cudaMemcpyAsync(base + lay.tx, p->tx_xy, 2 * p->num_tx * sizeof(float), cudaMemcpyHostToDevice, stream));
 	NA_CUDA(cudaMemcpyAsync(base + lay.rx, p->rx_xy, 2 * p->num_rx * sizeof(float), cudaMemcpyHostToDevice, stream));
@@ -286,8 +191,8 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	pp.ns = p->num_samples;
 	pp.U = U;
 	pp.L = L;
-	pp.tapsPerPhase = tapsPerPhase;
-	pp.tapsStride = tapsStride;
+	pp.tapsPerPhase = poly.tapsPerPhase;
+	pp.tapsStride = poly.tapsStride;
 	pp.polyTaps = reinterpret_cast<const float*>(base + lay.taps);
 	pp.deadZone = static_cast<unsigned>(dzd);
 	const float scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
@@ -295,10 +200,12 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	pp.tw = reinterpret_cast<const float2*>(base + lay.tw);
 	pp.cs = reinterpret_cast<const float2*>(base + lay.cs);
 	pp.perm = reinterpret_cast<const unsigned*>(base + lay.perm);
+	pp.stw = (analytic && !fft.stageTw.empty()) ? reinterpret_cast<const float2*>(base + lay.stw) : nullptr;
 
 	int dev = 0, maxSmem = 0;
 	NA_CUDA(cudaGetDevice(&dev));
 	NA_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+	if (pp.stw && usgb::prep_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) pp.stw = nullptr;
 	if (usgb::prep_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) {
 		NA_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation (signal length " << L << ").");
 	}
@@ -323,6 +230,9 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	dp.invScale = 1.0f / scale;
 	dp.pcfFactor = p->pcf_gamma / static_cast<float>(kPi / std::sqrt(3.0));
 	dp.scfP = p->scf_p;
+	dp.delayMode = USGB_DELAY_AUTO;
+	dp.invCTd = static_cast<double>(p->sampling_frequency) * U / p->propagation_speed;
+	dp.signalOffsetd = static_cast<double>(p->sampling_frequency) * U * p->peak_offset / p->center_frequency;
 	dp.value = d_value;
 	dp.factor = d_factor;
 	dp.errWord = reinterpret_cast<unsigned*>(base + lay.err);

@@ -19,16 +19,18 @@
 //   convolution the reference computes with an FFT overlap-save filter.
 // * The N-point real FFT of the zero-padded signal is done as an N/2-point
 //   complex FFT of the even/odd-packed samples, in place in shared memory
-//   (mixed radix 2/3/4/5, decimation in frequency, output in digit-reversed
+//   (mixed radix 2/3/4/5/6/8/9, decimation in frequency, output in digit-reversed
 //   order; the packed buffer read as floats is the signal itself). The
 //   Hilbert multiplier -i*sgn(k) and the real-FFT split are folded into one
 //   pass over digit-reversed pairs (k, M-k), and the inverse is an in-place
 //   decimation-in-time FFT that consumes the digit-reversed order and returns
 //   the imaginary part y[n] in natural order. The real part of the analytic
 //   signal is the DC-free input itself, recomputed at store time.
-// * Twiddles come from two-level tables in shared memory
-//   (W^m = hi[m / 128] * lo[m % 128]); stage indices use multiply-shift
-//   division by host-computed constants.
+// * Each butterfly reads one twiddle W_Ms^j and forms its powers in
+//   registers: the first stage from a two-level table (W^m = hi[m / 128] *
+//   lo[m % 128]), later stages from per-stage tables indexed by j, so that
+//   consecutive lanes read consecutive words. Stage indices use
+//   multiply-shift division by host-computed constants.
 #include <cuda_runtime.h>
 
 #include "usgb_common.cuh"
@@ -108,6 +110,99 @@ template<int SIGN> struct SmallDFT<5, SIGN> {
 	}
 };
 
+template<int SIGN> struct SmallDFT<8, SIGN> {
+	static __device__ __forceinline__ void run(float2* v)
+	{
+		// Two 4-point DFTs of the even and odd inputs, then X[k] = E[k] +
+		// W8^k O[k] and X[k + 4] = E[k] - W8^k O[k], W8 = exp(SIGN 2 pi i / 8).
+		float2 e[4] = {v[0], v[2], v[4], v[6]};
+		float2 o[4] = {v[1], v[3], v[5], v[7]};
+		SmallDFT<4, SIGN>::run(e);
+		SmallDFT<4, SIGN>::run(o);
+		const float r = 0.70710678118654752440f;
+		const float sg = static_cast<float>(SIGN);
+		const float2 o1 = make_float2(r * (o[1].x - sg * o[1].y), r * (o[1].y + sg * o[1].x));
+		const float2 o2 = cmuli(o[2], sg);
+		const float2 o3 = make_float2(r * (-o[3].x - sg * o[3].y), r * (sg * o[3].x - o[3].y));
+		v[0] = cadd(e[0], o[0]);
+		v[4] = csub(e[0], o[0]);
+		v[1] = cadd(e[1], o1);
+		v[5] = csub(e[1], o1);
+		v[2] = cadd(e[2], o2);
+		v[6] = csub(e[2], o2);
+		v[3] = cadd(e[3], o3);
+		v[7] = csub(e[3], o3);
+	}
+};
+
+// (cos, sin)(2 pi m / R) for the composite radices (m < R).
+template<int R> __device__ __forceinline__ float2 root(int m);
+template<> __device__ __forceinline__ float2 root<6>(int m)
+{
+	switch (m) {
+	case 0: return make_float2(1.0f, 0.0f);
+	case 1: return make_float2(0.5f, 0.86602540378443864676f);
+	case 2: return make_float2(-0.5f, 0.86602540378443864676f);
+	case 3: return make_float2(-1.0f, 0.0f);
+	case 4: return make_float2(-0.5f, -0.86602540378443864676f);
+	default: return make_float2(0.5f, -0.86602540378443864676f);
+	}
+}
+template<> __device__ __forceinline__ float2 root<9>(int m)
+{
+	switch (m) {
+	case 0: return make_float2(1.0f, 0.0f);
+	case 1: return make_float2(0.76604444311897803520f, 0.64278760968653932632f);
+	case 2: return make_float2(0.17364817766693034885f, 0.98480775301220805936f);
+	case 3: return make_float2(-0.5f, 0.86602540378443864676f);
+	case 4: return make_float2(-0.93969262078590838405f, 0.34202014332566873304f);
+	case 5: return make_float2(-0.93969262078590838405f, -0.34202014332566873304f);
+	case 6: return make_float2(-0.5f, -0.86602540378443864676f);
+	case 7: return make_float2(0.17364817766693034885f, -0.98480775301220805936f);
+	default: return make_float2(0.76604444311897803520f, -0.64278760968653932632f);
+	}
+}
+// DFT of size R = R1 R2 by the two-factor decomposition: input n = R2 n1 +
+// n2, output k = k1 + R1 k2; R2 DFTs of size R1, internal twiddles
+// W_R^(n2 k1), then R1 DFTs of size R2 (all in registers).
+template<int R1, int R2, int SIGN>
+__device__ __forceinline__ void composite_dft(float2* v)
+{
+	constexpr int R = R1 * R2;
+	float2 a[R];
+#pragma unroll
+	for (int n2 = 0; n2 < R2; ++n2) {
+		float2 t[R1];
+#pragma unroll
+		for (int n1 = 0; n1 < R1; ++n1) t[n1] = v[R2 * n1 + n2];
+		SmallDFT<R1, SIGN>::run(t);
+#pragma unroll
+		for (int k1 = 0; k1 < R1; ++k1) {
+			float2 x = t[k1];
+			if (n2 * k1 != 0) {
+				const float2 w = root<R>(n2 * k1);
+				x = cmul(x, make_float2(w.x, static_cast<float>(SIGN) * w.y));
+			}
+			a[n2 * R1 + k1] = x;
+		}
+	}
+#pragma unroll
+	for (int k1 = 0; k1 < R1; ++k1) {
+		float2 t[R2];
+#pragma unroll
+		for (int n2 = 0; n2 < R2; ++n2) t[n2] = a[n2 * R1 + k1];
+		SmallDFT<R2, SIGN>::run(t);
+#pragma unroll
+		for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = t[k2];
+	}
+}
+template<int SIGN> struct SmallDFT<6, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<3, 2, SIGN>(v); }
+};
+template<int SIGN> struct SmallDFT<9, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<3, 3, SIGN>(v); }
+};
+
 // Bit patterns of one stored complex sample as 32-bit words (no address-of,
 // so the values stay in registers).
 __device__ __forceinline__ void sample_words(float2 c, unsigned* w) { w[0] = __float_as_uint(c.x); w[1] = __float_as_uint(c.y); }
@@ -128,16 +223,30 @@ __device__ __forceinline__ float2 twiddle(const float2* lo, const float2* hi, un
 	return cmul(hi[m / kTwiddleSplit], lo[m % kTwiddleSplit]);
 }
 
+// w[q] = w[1]^q for q = 2 .. R-1, as w[q/2] w[q - q/2] (about log2(q)
+// products deep).
+template<int R>
+__device__ __forceinline__ void twiddle_powers(float2* w)
+{
+#pragma unroll
+	for (int q = 2; q < R; ++q) w[q] = cmul(w[q / 2], w[q - q / 2]);
+}
+
 // One in-place stage over `data` (M points), blocks of span Ms, radix R.
 // Forward (DIF): DFT_R of the R inputs at stride Ms/R, then twiddle
-// W_Ms^(p j). Inverse (DIT, the transpose): conjugate twiddle, then DFT_R.
+// W_Ms^(q j). Inverse (DIT, the transpose): conjugate twiddle, then DFT_R.
+// W_Ms^j comes from the stage's own table `st` (consecutive j in consecutive
+// lanes: no bank conflicts) or, without one, from the two-level table; its
+// powers are formed in registers. The last stage (Ms = R) has no twiddles;
+// elsewhere j = 0 multiplies by exactly 1.
 template<int R, bool INVERSE>
-__device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, const float2* twHi, unsigned M,
-		unsigned Ms, unsigned long long magic)
+__device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, const float2* twHi, const float2* st,
+		unsigned M, unsigned Ms, unsigned long long magic)
 {
 	const unsigned sub = Ms / R;
 	const unsigned twStride = M / Ms;
 	const unsigned nb = M / R;
+	const bool twiddled = sub > 1;
 	for (unsigned b = threadIdx.x; b < nb; b += blockDim.x) {
 		const unsigned blk = static_cast<unsigned>((static_cast<unsigned long long>(b) * magic) >> 40);
 		const unsigned j = b - blk * sub;
@@ -145,16 +254,21 @@ __device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, cons
 		float2 v[R];
 #pragma unroll
 		for (int q = 0; q < R; ++q) v[q] = data[base + q * sub];
+		float2 w[R];
+		if (twiddled) {
+			w[1] = st ? st[j] : twiddle(twLo, twHi, j * twStride);
+			twiddle_powers<R>(w);
+		}
 		if (!INVERSE) {
 			SmallDFT<R, -1>::run(v);
-			if (j != 0) {
+			if (twiddled) {
 #pragma unroll
-				for (int q = 1; q < R; ++q) v[q] = cmul(v[q], twiddle(twLo, twHi, q * j * twStride));
+				for (int q = 1; q < R; ++q) v[q] = cmul(v[q], w[q]);
 			}
 		} else {
-			if (j != 0) {
+			if (twiddled) {
 #pragma unroll
-				for (int q = 1; q < R; ++q) v[q] = cmulc(v[q], twiddle(twLo, twHi, q * j * twStride));
+				for (int q = 1; q < R; ++q) v[q] = cmulc(v[q], w[q]);
 			}
 			SmallDFT<R, +1>::run(v);
 		}
@@ -164,18 +278,22 @@ __device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, cons
 }
 
 template<bool INVERSE>
-__device__ void fft_run(float2* data, const PrepParams& p, const float2* twLo, const float2* twHi)
+__device__ __noinline__ void fft_run(float2* data, const PrepParams& p, const float2* twLo, const float2* twHi, const float2* stw)
 {
 	unsigned spans[kMaxFFTStages];
 	unsigned Ms = p.M;
 	for (int s = 0; s < p.numStages; ++s) { spans[s] = Ms; Ms /= p.radix[s]; }
 	for (int i = 0; i < p.numStages; ++i) {
 		const int s = INVERSE ? p.numStages - 1 - i : i;
+		const float2* st = (stw && s > 0) ? stw + p.stwOffset[s] : nullptr;
 		switch (p.radix[s]) {
-		case 2: fft_stage<2, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
-		case 3: fft_stage<3, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
-		case 4: fft_stage<4, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
-		default: fft_stage<5, INVERSE>(data, twLo, twHi, p.M, spans[s], p.divMagic[s]); break;
+		case 2: fft_stage<2, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 3: fft_stage<3, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 4: fft_stage<4, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 5: fft_stage<5, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 6: fft_stage<6, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 8: fft_stage<8, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		default: fft_stage<9, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		}
 		__syncthreads();
 	}
@@ -201,7 +319,7 @@ __device__ float block_sum(float v, float* red)
 
 // Shared-memory layout of the prep kernels (float offsets).
 struct PrepLayout {
-	unsigned data, rfs, taps, twLo, twHi, csLo, csHi, red, total;
+	unsigned data, rfs, taps, twLo, twHi, csLo, csHi, stw, red, total;
 	__host__ __device__ PrepLayout(const PrepParams& p, bool analytic)
 	{
 		const unsigned K = (p.tapsPerPhase - 1) / 2;
@@ -212,7 +330,8 @@ struct PrepLayout {
 		twHi = twLo + (analytic ? 2 * kTwiddleSplit : 0);
 		csLo = twHi + (analytic ? 2 * p.twHiCount : 0);
 		csHi = csLo + (analytic ? 2 * kTwiddleSplit : 0);
-		red = csHi + (analytic ? 2 * p.csHiCount : 0);
+		stw = csHi + (analytic ? 2 * p.csHiCount : 0);
+		red = stw + ((analytic && p.stw) ? 2 * p.stwCount : 0);
 		total = red + 32;
 	}
 };
@@ -238,6 +357,10 @@ __device__ void load_inputs(const PrepParams& p, const PrepLayout& lay, float* s
 		const unsigned ncs = 2 * (kTwiddleSplit + p.csHiCount);
 		const float* csg = reinterpret_cast<const float*>(p.cs);
 		for (unsigned i = threadIdx.x; i < ncs; i += blockDim.x) sm[lay.csLo + i] = __ldg(&csg[i]);
+		if (p.stw) {
+			const float* stg = reinterpret_cast<const float*>(p.stw);
+			for (unsigned i = threadIdx.x; i < 2 * p.stwCount; i += blockDim.x) sm[lay.stw + i] = __ldg(&stg[i]);
+		}
 	}
 	__syncthreads();
 }
@@ -341,6 +464,22 @@ __device__ void store_pass(const PrepParams& p, const float* rfs, const float* t
 			for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
 				float o[U];
 				fir_outputs<NT, U>(rfs, taps, b, o);
+				// y[bU .. bU + U) as 16-byte loads (scalar loads at the U-float
+				// lane stride would conflict U-fold in the banks).
+				float y[U];
+				if constexpr (U % 4 == 0) {
+#pragma unroll
+					for (int r = 0; r < U; r += 4) {
+						const float4 t = *reinterpret_cast<const float4*>(ys + b * U + r);
+						y[r] = t.x;
+						y[r + 1] = t.y;
+						y[r + 2] = t.z;
+						y[r + 3] = t.w;
+					}
+				} else {
+#pragma unroll
+					for (int r = 0; r < U; ++r) y[r] = ys[b * U + r];
+				}
 				constexpr int perVec = 16 / static_cast<int>(sizeof(CT));  // samples per 16-byte store
 				if constexpr (U % perVec == 0) {
 #pragma unroll
@@ -348,16 +487,14 @@ __device__ void store_pass(const PrepParams& p, const float* rfs, const float* t
 						unsigned w[4];
 #pragma unroll
 						for (int j = 0; j < perVec; ++j) {
-							const CT c = Complex<S>::pack((o[r0 + j] - mean) * sc, ys[b * U + r0 + j] * invM * sc);
+							const CT c = Complex<S>::pack((o[r0 + j] - mean) * sc, y[r0 + j] * invM * sc);
 							sample_words(c, w + j * (sizeof(CT) / 4));
 						}
 						*reinterpret_cast<uint4*>(out + b * U + r0) = make_uint4(w[0], w[1], w[2], w[3]);
 					}
 				} else {
 #pragma unroll
-					for (int r = 0; r < U; ++r) {
-						out[b * U + r] = Complex<S>::pack((o[r] - mean) * sc, ys[b * U + r] * invM * sc);
-					}
+					for (int r = 0; r < U; ++r) out[b * U + r] = Complex<S>::pack((o[r] - mean) * sc, y[r] * invM * sc);
 				}
 			}
 		} else {
@@ -399,6 +536,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	const float2* twHi = reinterpret_cast<const float2*>(sm + lay.twHi);
 	const float2* csLo = reinterpret_cast<const float2*>(sm + lay.csLo);
 	const float2* csHi = reinterpret_cast<const float2*>(sm + lay.csHi);
+	const float2* stw = p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr;
 	const unsigned L = p.L;
 
 	// 1. Upsampled signal into the packed buffer, zero past L.
@@ -411,7 +549,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	__syncthreads();
 
 	// 3. Forward FFT (digit-reversed output).
-	fft_run<false>(data, p, twLo, twHi);
+	fft_run<false>(data, p, twLo, twHi, stw);
 
 	// 4. Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
 	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0.
@@ -435,7 +573,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	__syncthreads();
 
 	// 5. Inverse FFT (natural-order output: y[n] * M at float index n).
-	fft_run<true>(data, p, twLo, twHi);
+	fft_run<true>(data, p, twLo, twHi, stw);
 
 	// 6. Store (x[n] - mean, y[n]) for n < L; x is recomputed from the A-scan.
 	store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);

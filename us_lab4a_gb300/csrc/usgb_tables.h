@@ -1,0 +1,232 @@
+// Host-side tables of the signal-preparation kernels, shared by every entry
+// point: the polyphase FIR of the upsampler and the plan of the Hilbert FFT
+// (radices, division constants, twiddles, digit-reversal permutation).
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "usgb_internal.h"
+
+namespace usgb {
+namespace host {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// FFTUtil::nextFastEvenSize (src/fft/FFTUtil.h:85-135): the smallest even
+// n' >= n whose odd part has no prime factor above 5.
+inline unsigned next_fast_even_size(unsigned n)
+{
+	if (n & 1U) ++n;
+	for (;;) {
+		unsigned m = n;
+		while ((m & 1U) == 0) m >>= 1;
+		while (m % 3 == 0) m /= 3;
+		while (m % 5 == 0) m /= 5;
+		if (m == 1) return n;
+		n += 2;
+	}
+}
+
+// Kaiser-windowed sinc of Interpolator::prepare (src/util/Interpolator.h:64-111,
+// src/util/KaiserWindow.h:45-93), evaluated in float with the same mixed
+// float/double expressions as Interpolator<float>.
+inline std::vector<float> interpolator_taps(unsigned U, float halfTransitionWidth)
+{
+	const double kaiserTolerance = 1.0e-4;
+	const float tol_dB = -20.0 * std::log10(kaiserTolerance);
+	float beta;
+	if (tol_dB > 50) {
+		beta = 0.1102 * (tol_dB - 8.7);
+	} else if (tol_dB > 21) {
+		const double k = tol_dB - 21.0;
+		beta = 0.5842 * std::pow(k, 0.4) + 0.07886 * k;
+	} else {
+		beta = 0.0;
+	}
+	const float finalTransitionWidth = (halfTransitionWidth * 2) / U;
+	const double sz = std::ceil((tol_dB - 7.95) / (2.285 * finalTransitionWidth * kPi) + 1.0);
+	const unsigned windowSize = static_cast<unsigned>(sz);
+	const float twoUp = 2 * U;
+	const unsigned n = static_cast<unsigned>(std::ceil((windowSize - 1) / twoUp) * twoUp) + 1U;
+
+	std::vector<float> window(n);
+	const float c1 = 2 / static_cast<float>(n - 1U);
+	const float c2 = 1 / std::cyl_bessel_if(0.0f, beta);
+	for (unsigned i = 0; i < n; ++i) {
+		const float k = c1 * i - 1;
+		float x = 1 - k * k;
+		if (x < 0.0f) x = 0.0f;
+		window[i] = c2 * std::cyl_bessel_if(0.0f, beta * std::sqrt(x));
+	}
+	const float numPeriods = (n - 1U) / twoUp;
+	const double step = static_cast<double>(numPeriods - (-numPeriods)) / (n - 1U);
+	std::vector<float> taps(n);
+	for (unsigned i = 0; i < n; ++i) {
+		const float xi = (i == 0) ? -numPeriods : static_cast<float>(-numPeriods + i * step);
+		const double arg = kPi * xi;
+		const double s = (std::abs(arg) < 1.0e-5) ? 1.0 - arg * arg / 6.0 : std::sin(arg) / arg;
+		taps[i] = static_cast<float>(s);
+		taps[i] *= window[i];
+	}
+	return taps;
+}
+
+// The fixed 4x FIR of the real-RF path, from the recipe stated in
+// src/util/Interpolator4X.h:56-66 (kaiser(81, 5) .* sinc(linspace(-10, 10, 81))).
+inline std::vector<float> interpolator4x_taps()
+{
+	const unsigned n = 80;
+	const double beta = 5.0;
+	const double i0b = std::cyl_bessel_i(0.0, beta);
+	std::vector<float> h(n + 1);
+	for (unsigned i = 0; i <= n; ++i) {
+		const double r = 2.0 * i / n - 1.0;
+		double arg = 1.0 - r * r;
+		if (arg < 0.0) arg = 0.0;
+		const double w = std::cyl_bessel_i(0.0, beta * std::sqrt(arg)) / i0b;
+		const double xv = -10.0 + 20.0 * i / n;
+		const double s = (xv == 0.0) ? 1.0 : std::sin(kPi * xv) / (kPi * xv);
+		h[i] = static_cast<float>(s * w);
+	}
+	return h;
+}
+
+// The upsampler's FIR in polyphase form: poly[r][t] = h[r + tU] for the U
+// phases, each padded to a multiple of 4 taps. Returns false when the FIR
+// length is not 2UK + 1.
+struct PolyTaps {
+	std::vector<float> poly;
+	unsigned tapsPerPhase = 1, tapsStride = 4;
+};
+
+inline bool make_poly_taps(bool analytic, unsigned U, PolyTaps& out)
+{
+	std::vector<float> taps;
+	if (!analytic) {
+		taps = interpolator4x_taps();
+	} else if (U > 1) {
+		taps = interpolator_taps(U, 0.2f);
+	} else {
+		taps = {1.0f};
+	}
+	const unsigned T = static_cast<unsigned>(taps.size());
+	if (U > 1 && ((T - 1) % (2 * U) != 0)) return false;
+	const unsigned K = (U > 1) ? (T - 1) / (2 * U) : 0;
+	out.tapsPerPhase = 2 * K + 1;
+	out.tapsStride = (out.tapsPerPhase + 3) & ~3u;
+	out.poly.assign(static_cast<size_t>(U) * out.tapsStride, 0.f);
+	for (unsigned r = 0; r < U; ++r) {
+		for (unsigned t = 0; t < out.tapsPerPhase; ++t) {
+			const unsigned j = r + t * U;
+			out.poly[r * out.tapsStride + t] = (j < T) ? taps[j] : 0.f;
+		}
+	}
+	return true;
+}
+
+// Plan of the Hilbert FFT of an L-sample A-scan: N = max(nextFastEvenSize(L +
+// 1024), 2048) (src/util/HilbertEnvelope.h:152), computed as an M = N/2-point
+// complex FFT.
+struct FFTTables {
+	unsigned N = 0, M = 0;
+	std::vector<int> radices;                     // DIF order
+	std::vector<unsigned long long> divMagic;     // per stage: ceil(2^40 / sub)
+	std::vector<float2> tw, cs;                   // two-level tables (lo 128, then hi)
+	unsigned twHiCount = 0, csHiCount = 0;
+	std::vector<unsigned> perm;                   // digit-reversed position of bin k
+	// Stage tables: for stage s >= 1 (span Ms, radix R), W_Ms^j for j < Ms / R,
+	// at stageTwOffset[s] (stage 0 reads the two-level table).
+	std::vector<float2> stageTw;
+	std::vector<unsigned> stageTwOffset;
+};
+
+inline bool make_fft_tables(unsigned L, FFTTables& t)
+{
+	t.N = std::max(next_fast_even_size(L + 1024U), 2048U);
+	t.M = t.N / 2;
+	const unsigned M = t.M;
+	unsigned m = M;
+	int e2 = 0, e3 = 0, e5 = 0;
+	while (m % 2 == 0) { m /= 2; ++e2; }
+	while (m % 3 == 0) { m /= 3; ++e3; }
+	while (m % 5 == 0) { m /= 5; ++e5; }
+	if (m != 1) return false;
+	// Few passes over the buffer: radix 8 for the power of two (one 4 for a
+	// remainder of 4; a remainder of 2 pairs with a 3 as radix 6), radix 9
+	// for the power of three (a remaining 3 alone), radix 5 for the rest. The
+	// power-of-two radices run first (long blocks), the odd ones last, where
+	// the blocks are short and odd strides keep the shared-memory banks apart.
+	t.radices.clear();
+	for (; e2 >= 3; e2 -= 3) t.radices.push_back(8);
+	if (e2 == 2) { t.radices.push_back(4); e2 = 0; }
+	bool two = e2 == 1;
+	bool three = (e3 % 2) == 1;
+	if (two && three) { t.radices.push_back(6); two = three = false; }
+	if (two) t.radices.push_back(2);
+	for (int i = 0; i < e3 / 2; ++i) t.radices.push_back(9);
+	if (three) t.radices.push_back(3);
+	for (int i = 0; i < e5; ++i) t.radices.push_back(5);
+	if (t.radices.size() > static_cast<size_t>(kMaxFFTStages)) return false;
+
+	auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
+	const unsigned S = kTwiddleSplit;
+	t.twHiCount = (M + S - 1) / S;
+	t.csHiCount = (M / 2 + 1 + S - 1) / S;
+	t.tw.resize(S + t.twHiCount);
+	t.cs.resize(S + t.csHiCount);
+	for (unsigned j = 0; j < S; ++j) t.tw[j] = unit(-2.0 * kPi * static_cast<double>(j) / M);
+	for (unsigned q = 0; q < t.twHiCount; ++q) t.tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
+	for (unsigned j = 0; j < S; ++j) t.cs[j] = unit(kPi * static_cast<double>(j) / M);
+	for (unsigned q = 0; q < t.csHiCount; ++q) t.cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
+
+	// Multiply-shift division by each stage's sub-block length:
+	// floor(b / sub) = (b * ceil(2^40 / sub)) >> 40, exact for b, sub < 2^20.
+	t.divMagic.clear();
+	t.stageTw.clear();
+	t.stageTwOffset.assign(t.radices.size(), 0);
+	unsigned Ms = M;
+	for (size_t s = 0; s < t.radices.size(); ++s) {
+		const unsigned sub = Ms / static_cast<unsigned>(t.radices[s]);
+		t.divMagic.push_back(((1ULL << 40) + sub - 1) / sub);
+		if (s > 0) {
+			t.stageTwOffset[s] = static_cast<unsigned>(t.stageTw.size());
+			for (unsigned j = 0; j < sub; ++j) t.stageTw.push_back(unit(-2.0 * kPi * static_cast<double>(j) / Ms));
+		}
+		Ms = sub;
+	}
+	// Digit-reversed position of bin k after the in-place DIF stages:
+	// k = k0 + r0 (k1 + r1 (k2 + ...)) sits at sum_s k_s * M / (r0 ... r_s).
+	t.perm.resize(M);
+	for (unsigned k = 0; k < M; ++k) {
+		unsigned kk = k, pos = 0, span = M;
+		for (int r : t.radices) {
+			span /= static_cast<unsigned>(r);
+			pos += (kk % r) * span;
+			kk /= r;
+		}
+		t.perm[k] = pos;
+	}
+	return true;
+}
+
+// Fills the FFT fields of `pp` from `t` (device table pointers set by the caller).
+inline void set_fft_params(PrepParams& pp, const FFTTables& t)
+{
+	pp.M = t.M;
+	pp.numStages = static_cast<int>(t.radices.size());
+	for (size_t i = 0; i < t.radices.size(); ++i) {
+		pp.radix[i] = t.radices[i];
+		pp.divMagic[i] = t.divMagic[i];
+		pp.stwOffset[i] = t.stageTwOffset[i];
+	}
+	pp.twHiCount = t.twHiCount;
+	pp.csHiCount = t.csHiCount;
+	pp.stwCount = static_cast<unsigned>(t.stageTw.size());
+}
+
+}  // namespace host
+}  // namespace usgb

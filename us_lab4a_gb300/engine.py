@@ -115,6 +115,13 @@ class StaEngine:
         """0: plain kernel; 1: staged kernel (tile_rows in {4, 8, 16}, stages in [2, 16])."""
         self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, stage_bytes, stages))
 
+    DELAY_PRECISION = {"auto": 0, "fp32": 1, "fp64": 2}
+
+    def set_delay_precision(self, mode: str) -> None:
+        """"auto" (FP64 geometry only for tiles whose delays exceed 32768
+        samples), "fp32" (as the reference) or "fp64"; staged kernel only."""
+        self._check(self._lib.usgb_set_delay_precision(self._h, self.DELAY_PRECISION[mode]))
+
     def das_config(self):
         v, r, b, n = C.c_int(), C.c_uint32(), C.c_uint32(), C.c_uint32()
         self._check(self._lib.usgb_get_das_config(self._h, C.byref(v), C.byref(r), C.byref(b), C.byref(n)))

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_PKG, "libusgb.so")
 USGB_PATH_ANALYTIC, USGB_PATH_REAL = 0, 1
 USGB_CF_NONE, USGB_CF_PCF, USGB_CF_SCF, USGB_CF_MF = 0, 1, 2, 3
 USGB_STORE_F32, USGB_STORE_F16, USGB_STORE_BF16 = 0, 1, 2
+USGB_DELAY_AUTO, USGB_DELAY_FP32, USGB_DELAY_FP64 = 0, 1, 2
 
 _FP = C.POINTER(C.c_float)
 
@@ -55,6 +56,7 @@ SIGNATURES = {
     "usgb_signal_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                    C.POINTER(C.c_uint32), C.POINTER(C.c_size_t)]),
     "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "usgb_set_delay_precision": (C.c_int, [C.c_void_p, C.c_uint32]),
     "usgb_get_das_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                       C.POINTER(C.c_uint32)]),
     "usgb_autotune_das": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
