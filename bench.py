@@ -368,9 +368,9 @@ def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
     batched_*   frames/s of all frames in one persistent preparation launch +
                 one persistent staged delay-and-sum launch, replayed from a
                 CUDA graph, tile shape autotuned on the batch;
-    serving_f16 the continuous-batching loop over the same frames arriving as
-                a Poisson stream (host RF in, host image out): frames/s,
-                p50/p99 latency from arrival to image in host memory;
+    serving     run_serving(): the serving configuration (these frames plus
+                large ones as Poisson streams) through the continuous-batching
+                loop, FP16 batched against plain FP32;
     err_db      peak-relative error of each form's image against the FP64
                 oracle on the `oracle_frames` smallest frames (worst case)."""
     import torch
@@ -378,7 +378,6 @@ def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
     import oracle
     from us_lab4a_gb300 import StaEngine, workloads
     from us_lab4a_gb300.batch import Batch, BatchItem
-    from us_lab4a_gb300.serving import Request, ServingLoop, poisson_arrivals
     s = torch.cuda.Stream(device=dev)
     frames = workloads.mixed(num_frames, storage="f16")
     with torch.cuda.stream(s):
@@ -451,29 +450,57 @@ def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
         if storage == "f16":
             best_f16 = cfg
     torch.cuda.synchronize(dev)
-    # Serving: the same frames as requests (pinned host RF), saturating Poisson arrivals.
-    arrivals = poisson_arrivals(num_frames, rate=2000.0, seed=11)
-    reqs = [Request(i, fr.spec, fr.grid_xyz, rfs[i].cpu().pin_memory(), float(t))
-            for i, (fr, t) in enumerate(zip(frames, arrivals))]
-    loop = ServingLoop(hbm_budget_bytes=150 << 30, max_batch=num_frames, max_elements=128, das_config=best_f16,
-                       device=dev)
-    loop.run(reqs, keep_images=False)  # creates the resident slots
-    for r in reqs:
-        r.done = None
-    st = loop.run(reqs, keep_images=True)
-    loop.close()
-    worst = -1e9
-    for i in small:
-        worst = max(worst, _db(float(np.abs(reqs[i].value.astype(np.float64) - refs[i]).max()),
-                               float(np.abs(refs[i]).max())))
-    out["serving_f16"] = {"frames_per_s": st["frames_per_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                          "arrival_rate": 2000.0, "batches": st["batches"], "mean_batch": st["mean_batch"],
-                          "hbm_budget_gb": 150, "peak_resident_gb": st["peak_resident_bytes"] / 1e9,
-                          "err_db": worst}
+    out["serving"] = run_serving(dev, frames, rfs, refs, small, best_f16)
     base = out["plain_f32"]["frames_per_s"]
     out["speedup_vs_plain_f32"] = {"batched_f16": out["batched_f16"]["frames_per_s"] / base,
-                                   "serving_f16": st["frames_per_s"] / base}
+                                   "batched_f32": out["batched_f32"]["frames_per_s"] / base}
     out["err_db_oracle_frames"] = len(small)
+    return out
+
+
+def run_serving(dev, frames, rfs, refs, small, das_config, rates=(50.0, 200.0, 2000.0), n_large=5):
+    """The serving configuration: the mixed-size frames plus ~10 % large frames
+    (128 elements, 4096 samples, 8x, 1024 x 1024, Blackman, SCF) arriving as a
+    Poisson stream at each rate in `rates`, RF in pinned host memory, images
+    back in host memory, HBM budget 150 GB. The continuous-batching loop with
+    FP16 storage and batched graph launches against the same loop serving the
+    plain FP32 form (one frame at a time, plain kernel). Latency = arrival to
+    image in host memory."""
+    from dataclasses import replace
+    from us_lab4a_gb300 import workloads
+    from us_lab4a_gb300.serving import Request, ServingLoop, poisson_arrivals
+    large = [workloads.large_serving_frame(seed=1004 + i, storage="f16") for i in range(n_large)]
+    allf = list(frames) + large
+    host_rf = [rf.cpu().pin_memory() for rf in rfs] + [fr.make_rf_torch(dev).cpu().pin_memory() for fr in large]
+    order = np.random.default_rng(12).permutation(len(allf))  # large frames spread through the stream
+    out = {"workload": f"{len(frames)} mixed-size frames + {n_large} frames of 128 elements, 4096 samples, 8x, "
+                       f"1024x1024, SCF; Poisson arrivals; host RF in, host image out",
+           "frames": len(allf), "hbm_budget_gb": 150}
+    for name, storage, plain in (("batched_f16", "f16", False), ("plain_f32", "f32", True)):
+        loop = ServingLoop(hbm_budget_bytes=150 << 30, max_batch=len(allf), max_elements=128,
+                           das_config=None if plain else das_config, device=dev, plain=plain)
+
+        def requests(rate):
+            arr = poisson_arrivals(len(allf), rate, seed=11)
+            return [Request(int(i), replace(allf[i].spec, storage=storage), allf[i].grid_xyz, host_rf[i], float(t))
+                    for i, t in zip(order, arr)]
+        loop.run(requests(max(rates)), keep_images=False)  # resident slots, captured graphs
+        per_rate = []
+        for rate in rates:
+            reqs = requests(rate)
+            st = loop.run(reqs, keep_images=(rate == max(rates)))
+            row = {"arrival_rate": rate, "frames_per_s": st["frames_per_s"], "p50_ms": st["p50_ms"],
+                   "p99_ms": st["p99_ms"], "batches": st["batches"], "mean_batch": st["mean_batch"]}
+            if rate == max(rates):
+                by_id = {r.rid: r for r in reqs}
+                row["err_db"] = max(_db(float(np.abs(by_id[i].value.astype(np.float64) - refs[i]).max()),
+                                        float(np.abs(refs[i]).max())) for i in small)
+            per_rate.append(row)
+        out[name] = {"rates": per_rate, "peak_resident_gb": loop.peak_bytes / 1e9}
+        loop.close()
+    sat_f16 = out["batched_f16"]["rates"][-1]["frames_per_s"]
+    sat_f32 = out["plain_f32"]["rates"][-1]["frames_per_s"]
+    out["speedup_at_saturation"] = sat_f16 / sat_f32
     return out
 
 

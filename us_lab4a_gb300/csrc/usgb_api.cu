@@ -462,10 +462,10 @@ const char* usgb_last_error(const usgb_ctx* c)
 int usgb_set_stream(usgb_ctx* c, void* s)
 {
 	return guarded(c, [&] {
-		if (c->ownStream && c->stream) {
-			USGB_CUDA(cudaStreamSynchronize(c->stream));
-			USGB_CUDA(cudaStreamDestroy(c->stream));
-		}
+		// Work queued on the previous stream (e.g. RF transfers started by
+		// usgb_submit_rf) finishes before the context moves.
+		if (c->stream) USGB_CUDA(cudaStreamSynchronize(c->stream));
+		if (c->ownStream && c->stream) USGB_CUDA(cudaStreamDestroy(c->stream));
 		c->ownStream = false;
 		c->stream = static_cast<cudaStream_t>(s);
 	});
@@ -503,7 +503,15 @@ int usgb_submit_rf(usgb_ctx* c, uint32_t tx, const float* rf, uint32_t num_rx, u
 			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Data size mismatch.");
 		}
 		const size_t n = static_cast<size_t>(num_rx) * num_samples;
-		std::memcpy(c->h_rf + static_cast<size_t>(tx) * n, rf, n * sizeof(float));
+		float* staged = c->h_rf + static_cast<size_t>(tx) * n;
+		std::memcpy(staged, rf, n * sizeof(float));
+		// The transfer of this transmit event starts now, on the context's
+		// stream, while the caller copies the next one (usgb_process waits for
+		// the stream before it returns, so the staging area is free again by
+		// the next frame; a repeated submission is transferred again, after the
+		// first, in stream order).
+		USGB_CUDA(cudaMemcpyAsync(c->d_rf + static_cast<size_t>(tx) * n, staged, n * sizeof(float),
+				cudaMemcpyHostToDevice, c->stream));
 		c->submitted[tx] = 1;
 	});
 }
@@ -516,14 +524,12 @@ int usgb_process(usgb_ctx* c, float* value, float* factor)
 			if (!c->submitted[t]) USGB_FAIL(USGB_ERR_INVALID_STATE, "RF of tx " << t << " has not been submitted.");
 		}
 		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
-		const size_t rfBytes = static_cast<size_t>(c->numSignals) * c->prm.num_samples * sizeof(float);
 		if (c->hOutCap < 2 * static_cast<size_t>(c->npix)) {
 			if (c->h_out) { cudaFreeHost(c->h_out); c->h_out = nullptr; c->hOutCap = 0; }
 			USGB_CUDA(cudaMallocHost(&c->h_out, 2 * static_cast<size_t>(c->npix) * sizeof(float)));
 			c->hOutCap = 2 * static_cast<size_t>(c->npix);
 		}
-		USGB_CUDA(cudaMemcpyAsync(c->d_rf, c->h_rf, rfBytes, cudaMemcpyHostToDevice, c->stream));
-		run_frame(c, c->d_rf, c->d_value, c->d_factor);
+		run_frame(c, c->d_rf, c->d_value, c->d_factor);  // the RF transfers were queued by usgb_submit_rf
 		USGB_CUDA(cudaMemcpyAsync(c->h_out, c->d_value, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
 		USGB_CUDA(cudaMemcpyAsync(c->h_out + c->npix, c->d_factor, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
 		USGB_CUDA(cudaStreamSynchronize(c->stream));

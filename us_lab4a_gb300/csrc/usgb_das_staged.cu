@@ -53,14 +53,16 @@ struct StageMeta {
 // Shared-memory layout (byte offsets), computed identically on host and
 // device, for at most maxTx / maxRx elements.
 struct StagedLayout {
-	unsigned bars, tileMax, meta, minmax, partial, txd, stage, total;
+	unsigned bars, tileMax, zero, meta, rxinfo, minmax, partial, txd, stage, total;
 	__host__ __device__ StagedLayout(unsigned maxTx, unsigned maxRx, unsigned trows, unsigned capBytes, unsigned stages)
 	{
 		bars = 0;
 		tileMax = 2 * stages * 8;
-		meta = (tileMax + 8 + 15) & ~15u;
-		minmax = meta + stages * static_cast<unsigned>(sizeof(StageMeta));
-		minmax = (minmax + 15) & ~15u;
+		zero = (tileMax + 8 + 15) & ~15u;
+		meta = zero + 16;
+		rxinfo = meta + stages * static_cast<unsigned>(sizeof(StageMeta));
+		rxinfo = (rxinfo + 15) & ~15u;
+		minmax = rxinfo + maxRx * 16;
 		partial = minmax + 2 * (maxTx + maxRx) * 4;
 		txd = partial + 2 * trows * (maxTx + maxRx) * 4;
 		txd = (txd + 15) & ~15u;
@@ -75,11 +77,13 @@ struct Smem {
 	uint64_t* full;
 	uint64_t* empty;
 	int* tileMax;    // [2]: largest transmit / receive delay of the tile (bits of a float >= 0)
+	const unsigned char* zero;  // 16 zero bytes: the two taps of a gather that is out of range
 	StageMeta* meta;
 	float* minT;     // [maxTx]
 	float* maxT;     // [maxTx]
 	float* minR;     // [maxRx]
 	float* maxR;     // [maxRx]
+	float4* rxinfo;  // [maxRx]: receiver (x, y, apodization / storage scale, 0)
 	float* partMin;  // [TROWS][maxTx + maxRx]
 	float* partMax;
 	float* txd;      // [maxTx][P]: FP32 delays, or fixed-point delays (int bits) in an FP64 tile
@@ -96,7 +100,9 @@ __device__ __forceinline__ Smem carve(unsigned char* smem, const StagedLayout& l
 	s.full = reinterpret_cast<uint64_t*>(smem + lay.bars);
 	s.empty = s.full + nst;
 	s.tileMax = reinterpret_cast<int*>(smem + lay.tileMax);
+	s.zero = smem + lay.zero;
 	s.meta = reinterpret_cast<StageMeta*>(smem + lay.meta);
+	s.rxinfo = reinterpret_cast<float4*>(smem + lay.rxinfo);
 	s.minT = reinterpret_cast<float*>(smem + lay.minmax);
 	s.maxT = s.minT + maxTx;
 	s.minR = s.maxT + maxTx;
@@ -194,10 +200,10 @@ template<> struct Delay<false> {
 	{
 		return split_delay(__fadd_rn(txv, rxv), k);
 	}
-	static __device__ __forceinline__ float rx(const DasParams& p, unsigned r, float px, float py, float pz,
+	static __device__ __forceinline__ float rx(const DasParams& p, float4 e, float px, float py, float pz,
 			const Fixed&)
 	{
-		return __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
+		return __fmul_rn(distance3d_z0(e.x, e.y, px, py, pz), p.invCT);
 	}
 };
 template<> struct Delay<true> {
@@ -207,24 +213,27 @@ template<> struct Delay<true> {
 		k = __int_as_float(0x3F800000 | ((q & f.mask) << f.shift)) - 1.0f;
 		return q >> f.F;
 	}
-	static __device__ __forceinline__ float rx(const DasParams& p, unsigned r, float px, float py, float pz,
+	static __device__ __forceinline__ float rx(const DasParams& p, float4 e, float px, float py, float pz,
 			const Fixed& f)
 	{
-		return to_fixed(distance3d_z0_f64(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz) * p.invCTd, f);
+		return to_fixed(distance3d_z0_f64(e.x, e.y, px, py, pz) * p.invCTd, f);
 	}
 };
 
 // Contribution of one staged (or empty) window to one grid point:
 // acc += (1-k) s[idx] + k s[idx+1]. Every delay of the tile lies inside its
 // window, so the range test alone guards the stage read; an empty window
-// rejects every index.
+// rejects every index. Branch-free: an index out of range reads both taps
+// from the zero slot with k = 0 (adds exactly 0, whatever the delay was).
 template<typename SP, bool Q>
 __device__ __forceinline__ void gather_staged(const typename SP::T* buf, int base, float txv, float rxv,
-		unsigned lastIdx, const Fixed& fx, float2& acc)
+		unsigned lastIdx, const Fixed& fx, const typename SP::T* zero, float2& acc)
 {
 	float k;
 	const int i = Delay<Q>::split(txv, rxv, k, fx);
-	if (static_cast<unsigned>(i) <= lastIdx) SP::accumulate(buf + (i + base), k, acc);
+	const bool ok = static_cast<unsigned>(i) <= lastIdx;
+	const typename SP::T* src = ok ? buf + (i + base) : zero;
+	SP::accumulate(src, ok ? k : 0.0f, acc);
 }
 
 // Any window kind: staged, empty, or gathered from global memory.
@@ -246,6 +255,7 @@ __device__ __forceinline__ void gather_any(int4 wm, const typename SP::T* buf, c
 
 __device__ __forceinline__ void init_barriers(const Smem& sm, int trows)
 {
+	if (threadIdx.x < 4) reinterpret_cast<unsigned*>(const_cast<unsigned char*>(sm.zero))[threadIdx.x] = 0u;
 	if (threadIdx.x == 0) {
 		for (unsigned s = 0; s < sm.nst; ++s) {
 			mbar_init(&sm.full[s], 1);
@@ -380,11 +390,15 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
 	const T* sig = reinterpret_cast<const T*>(p.sig);
 	const char* txdSlot = reinterpret_cast<const char*>(sm.txd + slot);
+	const T* zero = reinterpret_cast<const T*>(sm.zero);
 	float2 total = make_float2(0.f, 0.f);
 	CFState<CF> cf;
 	float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
 	unsigned r = 0;
-	float rxd = Delay<Q>::rx(p, 0, px, py, pz, fx);
+	// Receiver r's delay, and the next receiver's computed one receiver
+	// ahead (its latency hides behind the current receiver's gathers).
+	float rxd = Delay<Q>::rx(p, sm.rxinfo[0], px, py, pz, fx);
+	float rxdNext = (p.numRx > 1) ? Delay<Q>::rx(p, sm.rxinfo[1], px, py, pz, fx) : 0.0f;
 	// Ring slot and phase of stage `it`, carried along (no division per stage).
 	int s = it % nst;
 	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
@@ -411,12 +425,12 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 			for (; w + 1 < n; w += 2) {
 				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
 				const int2 wb = *reinterpret_cast<const int2*>(&m.win[w + 1]);
-				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, a0);
-				gather_staged<SP, Q>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, fx, a1);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, a0);
+				gather_staged<SP, Q>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, fx, zero, a1);
 			}
 			if (w < n) {
 				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
-				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, a0);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, a0);
 			}
 		} else {
 			for (int w = 0; w < n; ++w) {
@@ -438,14 +452,15 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 		}
 		if (last) {
 			const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
-			const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
+			const float2 rs = receiver_sum(acc, sm.rxinfo[r].z);
 			total.x += rs.x;
 			total.y += rs.y;
 			cf.add(rs);
 			accEven = make_float2(0.f, 0.f);
 			accOdd = make_float2(0.f, 0.f);
 			++r;
-			if (r < p.numRx) rxd = Delay<Q>::rx(p, r, px, py, pz, fx);
+			rxd = rxdNext;
+			if (r + 1 < p.numRx) rxdNext = Delay<Q>::rx(p, sm.rxinfo[r + 1], px, py, pz, fx);
 		}
 	}
 	if (active) {
@@ -487,6 +502,9 @@ __device__ bool staged_tile(const DasParams& p, const Smem& sm, unsigned bx, uns
 	if (threadIdx.x == 0) {
 		sm.tileMax[0] = 0;
 		sm.tileMax[1] = 0;
+	}
+	for (unsigned r = threadIdx.x; r < p.numRx; r += blockDim.x) {
+		sm.rxinfo[r] = make_float4(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), __ldg(&p.apod[r]) * p.invScale, 0.f);
 	}
 	// FP32 transmit-delay table and per-warp min/max of every element's delay.
 	if (!producer) {

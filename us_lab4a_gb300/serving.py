@@ -72,13 +72,18 @@ class _InFlight:
 
 class ServingLoop:
     def __init__(self, hbm_budget_bytes: int, max_batch: int = 48, max_elements: int = 128,
-                 use_graph: bool = True, device="cuda:0", das_config: Optional[Tuple[int, int, int]] = None):
+                 use_graph: bool = True, device="cuda:0", das_config: Optional[Tuple[int, int, int]] = None,
+                 plain: bool = False):
+        """plain=True serves the plain form instead: every admitted frame is
+        processed on its own (one preparation launch and one plain
+        delay-and-sum launch per frame), for comparison with the batched form."""
         import torch
         self.torch = torch
         self.device = torch.device(device)
         self.budget = int(hbm_budget_bytes)
         self.max_batch = max_batch
         self.use_graph = use_graph
+        self.plain = plain
         self.batches = [Batch(max_batch, max_elements), Batch(max_batch, max_elements)]
         if das_config:
             for b in self.batches:
@@ -114,6 +119,8 @@ class ServingLoop:
                 return None
         torch = self.torch
         eng = StaEngine(req.spec)
+        if self.plain:
+            eng.set_das_variant(0)
         g = torch.as_tensor(np.ascontiguousarray(req.grid_xyz, np.float32), device=self.device)
         eng.set_grid_device(g)
         torch.cuda.synchronize(self.device)
@@ -183,8 +190,13 @@ class ServingLoop:
                     with torch.cuda.stream(stream):
                         for req, slot in work:
                             slot.rf.copy_(req.rf, non_blocking=True)
-                        items = [BatchItem(slot.engine, slot.rf, slot.value, slot.factor) for _, slot in work]
-                        self.batches[idx].run(items, stream, use_graph=self.use_graph)
+                        if self.plain:
+                            for _, slot in work:
+                                slot.engine.set_stream(stream)
+                                slot.engine.process_device(slot.rf, slot.value, slot.factor)
+                        else:
+                            items = [BatchItem(slot.engine, slot.rf, slot.value, slot.factor) for _, slot in work]
+                            self.batches[idx].run(items, stream, use_graph=self.use_graph)
                         for _, slot in work:
                             slot.host_value.copy_(slot.value, non_blocking=True)
                             slot.host_factor.copy_(slot.factor, non_blocking=True)
