@@ -139,6 +139,22 @@ int usgb_set_stream(usgb_ctx* ctx, void* cuda_stream);
 int usgb_set_grid_device(usgb_ctx* ctx, const float* d_xyz, uint32_t ncols, uint32_t nrows);
 int usgb_process_device(usgb_ctx* ctx, const float* d_rf, float* d_value, float* d_factor);
 
+/* One whole frame from host memory: rf = num_tx * num_rx * num_samples floats
+ * (transmit-major, as the submitted rows), value / factor = ncols * nrows
+ * floats (factor may be NULL). Synchronous, like usgb_process. On devices
+ * that reach pageable host memory through the host's page tables (Grace-based
+ * GB300 systems) the kernels read the RF and write the images in place, with
+ * no staging copy; elsewhere the RF is copied in and the images out. No
+ * counterpart in the reference (its acquisition delivers one transmit event
+ * at a time, usgb_submit_rf). */
+int usgb_process_rf(usgb_ctx* ctx, const float* rf, float* value, float* factor);
+
+/* Direct host-memory access of usgb_process_rf: enable = 0 forces the copy
+ * path; enable = 1 fails with USGB_ERR_UNSUPPORTED where the device cannot.
+ * usgb_get_host_direct reports whether it is available and enabled. */
+int usgb_set_host_direct(usgb_ctx* ctx, int enable);
+int usgb_get_host_direct(const usgb_ctx* ctx, int* available, int* enabled);
+
 /* The two stages separately. d_signals holds num_tx * num_rx A-scans of
  * signal_stride samples (complex (re, im) pairs on the analytic path, reals on
  * the real path) in the context's storage type. */

@@ -109,6 +109,26 @@ def test_host_and_device_paths_agree(cuda):
     assert np.array_equal(vh, vd) and np.array_equal(fh, fd)
 
 
+def test_whole_frame_host_entry_point_paths_agree(cuda):
+    """usgb_process_rf reading the host RF in place (where the device reaches
+    pageable host memory) or through a copy, and the reference data flow
+    (usgb_submit_rf per transmit event + usgb_process), give the same image."""
+    from us_lab4a_gb300 import StaEngine, workloads
+    fr = workloads.cf2d(small=True)
+    rf = fr.make_rf_numpy()
+    with StaEngine(fr.spec) as eng:
+        eng.set_grid(fr.grid_xyz)
+        available, enabled = eng.host_direct()
+        assert enabled == available
+        vs, fs = eng.process_submitted(rf)
+        vd, fd = eng.process_host(rf)
+        eng.set_host_direct(False)
+        vc, fc = eng.process_host(rf)
+        vs2, fs2 = eng.process_submitted(rf)   # the submitted rows are still the frame's
+    for v, f in ((vd, fd), (vc, fc), (vs2, fs2)):
+        assert np.array_equal(v, vs) and np.array_equal(f, fs)
+
+
 @pytest.mark.parametrize("U,ns", [(1, 333), (4, 512), (8, 640), (3, 500)])
 def test_analytic_signal_matches_oracle(cuda, oracle_lib, U, ns):
     """The prepared tensor (upsampling, DC removal, Hilbert) against the oracle."""

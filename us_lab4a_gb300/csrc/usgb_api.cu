@@ -84,6 +84,8 @@ struct usgb_ctx {
 
 	cudaStream_t stream = nullptr;
 	bool ownStream = false;
+	bool hostDirectAvailable = false;  // kernels can read/write pageable host memory (host page tables)
+	bool hostDirect = false;
 	int dasVariant = 0;
 	int delayMode = USGB_DELAY_AUTO;
 	unsigned tileRows = 8;
@@ -432,6 +434,14 @@ int usgb_create(const usgb_sta_params* params, usgb_ctx** out)
 		check_prep_fits(c);
 		choose_default_das(c);
 		alloc_frame(c);
+		{
+			int dev = 0, pageable = 0, hostTables = 0;
+			USGB_CUDA(cudaGetDevice(&dev));
+			USGB_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+			USGB_CUDA(cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+			c->hostDirectAvailable = pageable && hostTables;
+			c->hostDirect = c->hostDirectAvailable;
+		}
 		USGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
 		c->ownStream = true;
 		*out = c;
@@ -539,6 +549,49 @@ int usgb_process(usgb_ctx* c, float* value, float* factor)
 		std::memcpy(value, c->h_out, c->npix * sizeof(float));
 		if (factor) std::memcpy(factor, c->h_out + c->npix, c->npix * sizeof(float));
 	});
+}
+
+int usgb_process_rf(usgb_ctx* c, const float* rf, float* value, float* factor)
+{
+	return guarded(c, [&] {
+		if (!rf || !value) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null host pointer");
+		if (!c->gridSet) USGB_FAIL(USGB_ERR_INVALID_STATE, "The grid has not been set.");
+		if (c->hostDirect) {
+			// The preparation kernel reads the RF and the delay-and-sum writes
+			// the images in host memory, through the host's page tables.
+			run_frame(c, rf, value, factor ? factor : c->d_factor);
+		} else {
+			const size_t rfBytes = static_cast<size_t>(c->numSignals) * c->prm.num_samples * sizeof(float);
+			USGB_CUDA(cudaMemcpyAsync(c->d_rf, rf, rfBytes, cudaMemcpyHostToDevice, c->stream));
+			run_frame(c, c->d_rf, c->d_value, c->d_factor);
+			USGB_CUDA(cudaMemcpyAsync(value, c->d_value, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+			if (factor) {
+				USGB_CUDA(cudaMemcpyAsync(factor, c->d_factor, c->npix * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+			}
+		}
+		USGB_CUDA(cudaStreamSynchronize(c->stream));
+		unsigned errWord = 0;
+		USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+		if (errWord) USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+	});
+}
+
+int usgb_set_host_direct(usgb_ctx* c, int enable)
+{
+	return guarded(c, [&] {
+		if (enable && !c->hostDirectAvailable) {
+			USGB_FAIL(USGB_ERR_UNSUPPORTED, "This device cannot access pageable host memory through the host's page tables.");
+		}
+		c->hostDirect = enable != 0;
+	});
+}
+
+int usgb_get_host_direct(const usgb_ctx* c, int* available, int* enabled)
+{
+	if (!c) return USGB_ERR_INVALID_PARAMETER;
+	if (available) *available = c->hostDirectAvailable ? 1 : 0;
+	if (enabled) *enabled = c->hostDirect ? 1 : 0;
+	return USGB_OK;
 }
 
 int usgb_process_device(usgb_ctx* c, const float* d_rf, float* d_value, float* d_factor)

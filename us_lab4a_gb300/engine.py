@@ -156,11 +156,31 @@ class StaEngine:
                                            factor.ctypes.data_as(C.POINTER(C.c_float))))
         return value, factor
 
-    def process_host(self, rf: np.ndarray):
-        """Whole frame from a (num_tx, num_rx, ns) host array."""
+    def process_submitted(self, rf: np.ndarray):
+        """Whole frame through the reference's data flow: one usgb_submit_rf per
+        transmit event, then usgb_process."""
         for t in range(rf.shape[0]):
             self.submit_rf(t, rf[t])
         return self.process()
+
+    def process_host(self, rf: np.ndarray):
+        """Whole frame from a (num_tx, num_rx, ns) host array (usgb_process_rf:
+        read in place where the device reaches host memory directly)."""
+        rf = np.ascontiguousarray(rf, np.float32)
+        value = np.empty((self.ncols, self.nrows), np.float32)
+        factor = np.empty((self.ncols, self.nrows), np.float32)
+        self._check(self._lib.usgb_process_rf(self._h, C.c_void_p(rf.ctypes.data), C.c_void_p(value.ctypes.data),
+                                              C.c_void_p(factor.ctypes.data)))
+        return value, factor
+
+    def set_host_direct(self, enable: bool) -> None:
+        self._check(self._lib.usgb_set_host_direct(self._h, int(enable)))
+
+    def host_direct(self):
+        """(available, enabled) for direct host-memory access."""
+        a, e = C.c_int(), C.c_int()
+        self._check(self._lib.usgb_get_host_direct(self._h, C.byref(a), C.byref(e)))
+        return bool(a.value), bool(e.value)
 
     # -- device path (torch CUDA tensors) ---------------------------------
     def set_stream(self, stream) -> None:
