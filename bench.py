@@ -334,7 +334,8 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": spec.storage if spec.storage != "f32" else "f32",
             "data": "synthetic (seeded point + speckle scatterers)",
             "config": {"workload": desc, "storage": spec.storage, "das_kernel": ("plain" if das_cfg["variant"] == 0 else
-                           f"staged (tile 32x{das_cfg['tile_rows']}, {das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
+                           ("staged" if das_cfg["variant"] == 1 else "receiver-group")
+                           + f" (tile 32x{das_cfg['tile_rows']}, {das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
                            + (", autotuned)" if args.autotune else ")")),
                        "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
                        "parallelism": f"replicas x{world}"},

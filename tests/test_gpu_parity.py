@@ -259,22 +259,24 @@ def _staged_cases():
     return [("cf2d-pcf", workloads.cf2d(small=True)), ("cf2d-mf", workloads.cf2d(small=True, coherence="mf")),
             ("plain2d", workloads.plain2d(small=True)), ("real-scf", real),
             ("matrix3d-f16", workloads.matrix3d(small=True)),
-            ("cf2d-bf16", workloads.with_storage(workloads.cf2d(small=True, coherence="scf"), "bf16"))]
+            ("cf2d-bf16", workloads.with_storage(workloads.cf2d(small=True, coherence="scf"), "bf16")),
+            ("plain2d-12el", workloads.plain2d(tiny=True))]
 
 
 @pytest.mark.parametrize("rows,stage_bytes", [(8, 16384), (4, 4096), (16, 1024)])
 @pytest.mark.parametrize("name,frame", _staged_cases(), ids=[n for n, _ in _staged_cases()])
 def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes):
-    """The shared-memory staged kernel reads the same samples with the same
-    weights in the same order as the plain kernel: the images are identical,
-    also when windows overflow a stage (1 KiB stages force the global-memory
-    path) and for partial tiles."""
+    """The shared-memory staged kernel and the receiver-group kernel read the
+    same samples with the same weights in the same order as the plain kernel:
+    the images are identical, also when windows overflow a stage (small stages
+    force the global-memory path), for partial tiles and for a receiver count
+    that leaves a partial receiver group (12 elements)."""
     import torch
     from us_lab4a_gb300 import StaEngine
     rf = torch.as_tensor(frame.make_rf_numpy(), device=cuda)
     g = torch.as_tensor(frame.grid_xyz, device=cuda)
     out = []
-    for variant in (0, 1):
+    for variant in (0, 1, 2):
         with StaEngine(frame.spec) as eng:
             eng.set_stream(torch.cuda.current_stream())
             eng.set_das_variant(variant, rows, stage_bytes)
@@ -284,5 +286,6 @@ def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes)
             eng.process_device(rf, v, f)
             eng.synchronize()
             out.append((v.cpu().numpy(), f.cpu().numpy()))
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1])
+    for variant in (1, 2):
+        assert np.array_equal(out[0][0], out[variant][0]), variant
+        assert np.array_equal(out[0][1], out[variant][1]), variant

@@ -347,6 +347,12 @@ size_t max_smem()
 // Default delay-and-sum kernel: the staged kernel with 32 x 8 tiles, 16 KiB
 // stages and the deepest pipeline that fits in shared memory (then 32 x 4
 // tiles), else the plain kernel.
+size_t das_smem_bytes(const usgb_ctx* c, int variant, unsigned rows, unsigned cap, unsigned nst)
+{
+	return variant == 2 ? usgb::das_group_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst)
+	                    : usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst);
+}
+
 void choose_default_das(usgb_ctx* c)
 {
 	for (unsigned rows : {8u, 4u}) {
@@ -642,17 +648,17 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return guarded(c, [&] {
-		if (variant != 0 && variant != 1) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
+		if (variant < 0 || variant > 2) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
 		const unsigned rows = tile_rows ? tile_rows : c->tileRows;
 		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
 		const unsigned nst = stages ? stages : c->stages;
-		if (variant == 1) {
+		if (variant != 0) {
 			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
 			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
 				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 			}
 			if (nst < 2 || nst > 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage count must be in [2, 16].");
-			const size_t need = usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst);
+			const size_t need = das_smem_bytes(c, variant, rows, cap, nst);
 			if (need > max_smem()) {
 				USGB_FAIL(USGB_ERR_UNSUPPORTED, "Staged delay-and-sum needs " << need << " bytes of shared memory (device: "
 						<< max_smem() << "); use fewer tile rows, stages or smaller stages.");
@@ -695,11 +701,12 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		const unsigned iters = iterations ? iterations : 3;
 		struct Cand { int variant; unsigned rows, cap, stages; };
 		std::vector<Cand> cands;
-		for (unsigned rows : {4u, 8u, 16u})
-			for (unsigned cap : {8192u, 16384u, 32768u})
-				for (unsigned nst : {2u, 4u, 6u, 8u, 12u, 16u})
-					if (usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst) <= max_smem())
-						cands.push_back({1, rows, cap, nst});
+		for (int variant : {1, 2})
+			for (unsigned rows : {4u, 8u, 16u})
+				for (unsigned cap : {8192u, 16384u, 32768u})
+					for (unsigned nst : {2u, 3u, 4u})
+						if (das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
+							cands.push_back({variant, rows, cap, nst});
 		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});
 		cudaEvent_t e0, e1;
 		USGB_CUDA(cudaEventCreate(&e0));

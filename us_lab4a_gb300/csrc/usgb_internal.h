@@ -84,9 +84,12 @@ struct DasParams {
 	unsigned stages;
 };
 
-// variant 0: plain kernel; 1: staged kernel.
+// variant 0: plain kernel; 1: staged kernel; 2: receiver-group kernel.
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
 cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
+// variant 2: receiver-group kernel (usgb_das_group.cu).
+cudaError_t launch_das_group(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
+size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages);
 
 // ---------------------------------------------------------------------------
 // Batched (multi-frame) launches: persistent blocks walk the work items of
