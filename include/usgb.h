@@ -170,9 +170,13 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
 /* Selects the delay-and-sum kernel: 0 = plain (one thread per point, gathers
  * from global memory), 1 = staged (per tile of 32 columns x tile_rows rows,
  * the A-scan windows the tile needs are bulk-copied into a shared-memory ring
- * of `stages` stages of stage_bytes each). 0 for tile_rows / stage_bytes /
- * stages keeps the current value. New contexts start with the staged kernel
- * at the deepest ring that fits in shared memory. */
+ * of `stages` stages of stage_bytes each; receiver by receiver, transmit
+ * delays in a per-point table), 2 = receiver-group (the same ring, filled
+ * receiver group by receiver group; a group's receive delays and sums stay in
+ * registers, no per-point table, so arrays of hundreds of elements stage as
+ * well). 0 for tile_rows / stage_bytes / stages keeps the current value. New
+ * contexts start with the receiver-group kernel (4 rows, 2 x 32 KiB) where it
+ * fits. */
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);
@@ -242,6 +246,8 @@ int usgb_batch_create(uint32_t max_frames, uint32_t max_elements, uint32_t max_s
 void usgb_batch_destroy(usgb_batch* batch);
 const char* usgb_batch_last_error(const usgb_batch* batch);
 int usgb_batch_set_das_config(usgb_batch* batch, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
+/* Delay-and-sum kernel of the batch: 2 = receiver-group (default), 1 = staged. */
+int usgb_batch_set_das_variant(usgb_batch* batch, int variant);
 int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
 int usgb_batch_synchronize(usgb_batch* batch);
 

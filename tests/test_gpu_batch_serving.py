@@ -22,9 +22,10 @@ def _alone(frame, cuda, das_config):
         return v.cpu().numpy(), f.cpu().numpy()
 
 
+@pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("use_graph", [False, True])
 @pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_batch_equals_frames_alone(cuda, use_graph, storage):
+def test_batch_equals_frames_alone(cuda, use_graph, storage, variant):
     import torch
     from us_lab4a_gb300 import StaEngine, workloads
     from us_lab4a_gb300.batch import Batch, BatchItem
@@ -32,7 +33,7 @@ def test_batch_equals_frames_alone(cuda, use_graph, storage):
     cfg = (4, 16384, 2)
     stream = torch.cuda.current_stream()
     batch = Batch(max_frames=16, max_elements=16)
-    batch.set_das_config(*cfg)
+    batch.set_das_config(*cfg, variant=variant)
     engines, items = [], []
     for fr in frames:
         eng = StaEngine(fr.spec)

@@ -41,21 +41,30 @@ class Batch:
             from .errors import from_status
             raise from_status(rc, self._lib.usgb_batch_last_error(self._h).decode())
 
-    # (tile rows, stage bytes, stages) tried by autotune(), most likely first.
-    CANDIDATES = ((4, 16384, 2), (4, 8192, 2), (8, 16384, 2), (4, 16384, 4), (8, 32768, 2), (16, 32768, 2))
+    # (variant, tile rows, stage bytes, stages) tried by autotune(), most likely first.
+    CANDIDATES = ((2, 4, 32768, 2), (2, 4, 16384, 2), (2, 8, 32768, 2), (2, 4, 16384, 3), (2, 8, 16384, 2),
+                  (1, 4, 32768, 2), (1, 4, 16384, 2), (1, 8, 16384, 2))
 
-    def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int) -> None:
+    def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int, variant: int = None) -> None:
+        """Tile shape of the batched delay-and-sum; variant 2 = receiver-group
+        kernel, 1 = staged kernel (None keeps the current one)."""
+        if variant is not None and variant != getattr(self, "_variant", 2):
+            # Shrink first so that the variant switch fits, then set the shape.
+            self._check(self._lib.usgb_batch_set_das_config(self._h, 4, 8192, 2))
+            self._check(self._lib.usgb_batch_set_das_variant(self._h, variant))
+            self._variant = variant
         self._check(self._lib.usgb_batch_set_das_config(self._h, tile_rows, stage_bytes, stages))
-        self.das_config = (tile_rows, stage_bytes, stages)
+        self.das_config = (getattr(self, "_variant", 2), tile_rows, stage_bytes, stages)
 
     def autotune(self, items: Sequence[BatchItem], stream, candidates=None, repeats: int = 1):
-        """Time the whole batch (graph replay) under each staged-kernel shape
-        that fits and keep the fastest. Returns ((rows, stage_bytes, stages), ms)."""
+        """Time the whole batch (graph replay) under each kernel / tile shape
+        that fits and keep the fastest. Returns ((variant, rows, stage_bytes,
+        stages), ms)."""
         import torch
         best = None
         for cfg in candidates or self.CANDIDATES:
             try:
-                self.set_das_config(*cfg)
+                self.set_das_config(cfg[1], cfg[2], cfg[3], variant=cfg[0])
             except Exception:
                 continue  # does not fit in shared memory for max_elements
             self.run(items, stream, use_graph=True)  # capture
@@ -71,7 +80,8 @@ class Batch:
                 best = (cfg, ms)
         if best is None:
             raise RuntimeError("no staged delay-and-sum shape fits this batch")
-        self.set_das_config(*best[0])
+        v, rows, cap, nst = best[0]
+        self.set_das_config(rows, cap, nst, variant=v)
         return best
 
     def run(self, items: Sequence[BatchItem], stream, use_graph: bool = True) -> None:

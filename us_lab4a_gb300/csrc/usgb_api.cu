@@ -105,7 +105,8 @@ struct usgb_ctx {
 
 struct usgb_batch {
 	unsigned maxFrames = 0, maxElements = 0, maxSignalLength = 0;
-	unsigned tileRows = 8, stageBytes = 16384, stages = 0;
+	int dasVariant = 2;      // 1: staged kernel, 2: receiver-group kernel
+	unsigned tileRows = 4, stageBytes = 32768, stages = 2;
 	unsigned numSMs = 0;
 	size_t descBytes = 0;
 	unsigned char* h_desc = nullptr;   // pinned: header, prep frames, DAS frames
@@ -355,6 +356,15 @@ size_t das_smem_bytes(const usgb_ctx* c, int variant, unsigned rows, unsigned ca
 
 void choose_default_das(usgb_ctx* c)
 {
+	for (unsigned cap : {32768u, 16384u, 8192u}) {
+		if (das_smem_bytes(c, 2, 4u, cap, 2u) <= max_smem()) {
+			c->dasVariant = 2;
+			c->tileRows = 4;
+			c->stageBytes = cap;
+			c->stages = 2;
+			return;
+		}
+	}
 	for (unsigned rows : {8u, 4u}) {
 		for (unsigned nst : {8u, 6u, 4u, 2u}) {
 			if (usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, 16384u, nst) <= max_smem()) {
@@ -806,6 +816,12 @@ int batch_guarded(usgb_batch* b, F&& f)
 	}
 }
 
+size_t batch_das_smem(const usgb_batch* b, int variant, unsigned rows, unsigned cap, unsigned nst)
+{
+	return variant == 2 ? usgb::das_group_smem_bytes(b->maxElements, b->maxElements, rows, cap, nst)
+	                    : usgb::das_staged_smem_bytes(b->maxElements, b->maxElements, rows, cap, nst);
+}
+
 }  // namespace
 
 extern "C" {
@@ -826,16 +842,9 @@ int usgb_batch_create(uint32_t max_frames, uint32_t max_elements, uint32_t max_s
 		USGB_CUDA(cudaGetDevice(&dev));
 		USGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 		b->numSMs = static_cast<unsigned>(sms);
-		for (unsigned nst : {8u, 6u, 4u, 2u}) {
-			if (usgb::das_staged_smem_bytes(max_elements, max_elements, b->tileRows, b->stageBytes, nst) <= max_smem()) {
-				b->stages = nst;
-				break;
-			}
-		}
-		if (!b->stages) {
-			b->tileRows = 4;
-			b->stages = 2;
-			if (usgb::das_staged_smem_bytes(max_elements, max_elements, 4, b->stageBytes, 2) > max_smem()) {
+		if (batch_das_smem(b, b->dasVariant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
+			b->stageBytes = 8192;
+			if (batch_das_smem(b, b->dasVariant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
 				USGB_FAIL(USGB_ERR_UNSUPPORTED, "max_elements too large for the batched delay-and-sum.");
 			}
 		}
@@ -866,6 +875,21 @@ const char* usgb_batch_last_error(const usgb_batch* b)
 	return b ? b->err.c_str() : g_createError.c_str();
 }
 
+int usgb_batch_set_das_variant(usgb_batch* b, int variant)
+{
+	return batch_guarded(b, [&] {
+		if (variant != 1 && variant != 2) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1 or 2.");
+		if (batch_das_smem(b, variant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
+			USGB_FAIL(USGB_ERR_UNSUPPORTED, "the current tile shape does not fit in shared memory for this variant.");
+		}
+		b->dasVariant = variant;
+		if (b->graph) {
+			cudaGraphExecDestroy(b->graph);
+			b->graph = nullptr;
+		}
+	});
+}
+
 int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return batch_guarded(b, [&] {
@@ -874,7 +898,7 @@ int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_
 			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 		}
 		if (stages < 2 || stages > 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage count must be in [2, 16].");
-		if (usgb::das_staged_smem_bytes(b->maxElements, b->maxElements, tile_rows, stage_bytes, stages) > max_smem()) {
+		if (batch_das_smem(b, b->dasVariant, tile_rows, stage_bytes, stages) > max_smem()) {
 			USGB_FAIL(USGB_ERR_UNSUPPORTED, "configuration does not fit in shared memory for max_elements "
 					<< b->maxElements << '.');
 		}
@@ -955,16 +979,25 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 		dc.tileRows = b->tileRows;
 		dc.stageBytes = b->stageBytes;
 		dc.stages = b->stages;
-		const size_t dasSmem = usgb::das_staged_smem_bytes(dc.maxTx, dc.maxRx, dc.tileRows, dc.stageBytes, dc.stages);
-		const unsigned dasPerSM = std::max<unsigned>(1, static_cast<unsigned>((228u * 1024u) / (dasSmem + 1024u)));
-		dc.blocks = b->numSMs * std::min(dasPerSM, 4u);
+		if (b->dasVariant == 2) {
+			dc.blocks = 0;  // the launcher fills the SMs (occupancy of the kernel at this shape)
+		} else {
+			const size_t dasSmem = usgb::das_staged_smem_bytes(dc.maxTx, dc.maxRx, dc.tileRows, dc.stageBytes, dc.stages);
+			const unsigned dasPerSM = std::max<unsigned>(1, static_cast<unsigned>((228u * 1024u) / (dasSmem + 1024u)));
+			dc.blocks = b->numSMs * std::min(dasPerSM, 4u);
+		}
+		const int variant = b->dasVariant;
 		const int storage = static_cast<int>(c0->prm.storage);
 		const bool analytic = c0->analytic;
 
 		auto enqueue = [&](cudaStream_t st) {
 			USGB_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc, b->descBytes, cudaMemcpyHostToDevice, st));
 			USGB_CUDA(usgb::launch_prep_batch(dPrep, dHdr, prepSmem, prepBlocks, storage, analytic, st));
-			USGB_CUDA(usgb::launch_das_staged_batch(dDas, dHdr, dc, storage, analytic, st));
+			if (variant == 2) {
+				USGB_CUDA(usgb::launch_das_group_batch(dDas, dHdr, dc, storage, analytic, st));
+			} else {
+				USGB_CUDA(usgb::launch_das_staged_batch(dDas, dHdr, dc, storage, analytic, st));
+			}
 		};
 		if (use_graph) {
 			// Re-capture when the launch shape changed (the kernels read the

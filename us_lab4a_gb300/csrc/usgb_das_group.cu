@@ -472,7 +472,101 @@ cudaError_t launch_group_cf(const DasParams& p, int cf, bool analytic, cudaStrea
 	}
 }
 
+template<int S, bool ANALYTIC, int TROWS>
+__device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, const GroupSmem& sm, unsigned bx,
+		unsigned by, int& it)
+{
+	if (!ANALYTIC) {
+		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TROWS>(p, sm, bx, by, it)
+		                      : group_tile<S, CF_NONE, false, TROWS>(p, sm, bx, by, it);
+	}
+	switch (cf) {
+	case CF_PCF: return group_tile<S, CF_PCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_SCF: return group_tile<S, CF_SCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_MF: return group_tile<S, CF_MF, true, TROWS>(p, sm, bx, by, it);
+	default: return group_tile<S, CF_NONE, true, TROWS>(p, sm, bx, by, it);
+	}
+}
+
+// Many frames: persistent blocks walk the tiles of every frame in the batch.
+template<int S, bool ANALYTIC, int TROWS>
+__global__ void __launch_bounds__((TROWS + 1) * 32)
+das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
+		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	__shared__ DasParams sp;
+	__shared__ int sAbort;
+	const GroupLayout lay(maxTx, maxRx, TROWS, capBytes, stages);
+	const GroupSmem sm = carve_group(smem, lay, maxTx, maxRx, TROWS, stages, capBytes);
+	if (threadIdx.x == 0) sAbort = 0;
+	init_group_barriers(sm, TROWS);
+	const unsigned count = hdr->count;
+	const unsigned totalTiles = hdr->totalTiles;
+	int it = 0;
+	unsigned f = 0;
+	for (unsigned w = blockIdx.x; w < totalTiles; w += gridDim.x) {
+		while (f + 1 < count && frames[f + 1].tileBegin <= w) ++f;  // work items are visited in increasing order
+		__syncthreads();  // the previous tile is done with sp and the shared tables
+		if (threadIdx.x == 0) sp = frames[f].das;
+		__syncthreads();
+		if (sAbort) break;
+		const unsigned local = w - frames[f].tileBegin;
+		const unsigned tilesX = frames[f].tilesX;
+		const bool ok = group_tile_any_cf<S, ANALYTIC, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
+		if (!ok) sAbort = 1;
+	}
+}
+
+template<int S, bool ANALYTIC, int TROWS>
+cudaError_t launch_group_batch_one(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		cudaStream_t stream)
+{
+	const GroupLayout lay(c.maxTx, c.maxRx, TROWS, c.stageBytes, c.stages);
+	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TROWS>;
+	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
+	if (e != cudaSuccess) return e;
+	unsigned blocks = c.blocks;
+	if (blocks == 0) {  // as many resident blocks as the SMs hold
+		int perSM = 0, dev = 0, sms = 0;
+		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, (TROWS + 1) * 32, lay.total)) != cudaSuccess) return e;
+		if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+		if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+		blocks = static_cast<unsigned>(sms) * static_cast<unsigned>(perSM > 0 ? perSM : 1);
+	}
+	kernel<<<blocks, (TROWS + 1) * 32, lay.total, stream>>>(frames, hdr, c.maxTx, c.maxRx, c.stageBytes, c.stages);
+	return cudaGetLastError();
+}
+
+template<int S, bool ANALYTIC>
+cudaError_t group_batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		cudaStream_t stream)
+{
+	switch (c.tileRows) {
+	case 4: return launch_group_batch_one<S, ANALYTIC, 4>(frames, hdr, c, stream);
+	case 16: return launch_group_batch_one<S, ANALYTIC, 16>(frames, hdr, c, stream);
+	default: return launch_group_batch_one<S, ANALYTIC, 8>(frames, hdr, c, stream);
+	}
+}
+
 }  // namespace
+
+cudaError_t launch_das_group_batch(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		int storage, bool analytic, cudaStream_t stream)
+{
+	if (analytic) {
+		switch (storage) {
+		case STORE_F16: return group_batch_rows<STORE_F16, true>(frames, hdr, c, stream);
+		case STORE_BF16: return group_batch_rows<STORE_BF16, true>(frames, hdr, c, stream);
+		default: return group_batch_rows<STORE_F32, true>(frames, hdr, c, stream);
+		}
+	}
+	switch (storage) {
+	case STORE_F16: return group_batch_rows<STORE_F16, false>(frames, hdr, c, stream);
+	case STORE_BF16: return group_batch_rows<STORE_BF16, false>(frames, hdr, c, stream);
+	default: return group_batch_rows<STORE_F32, false>(frames, hdr, c, stream);
+	}
+}
 
 size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages)
 {

@@ -120,7 +120,7 @@ struct BatchDasFrame {
 struct BatchDasConfig {
 	unsigned maxTx, maxRx;   // layout limits of the shared memory
 	unsigned tileRows, stageBytes, stages;
-	unsigned blocks;         // persistent grid size
+	unsigned blocks;         // persistent grid size (0: as many blocks as the SMs hold)
 };
 
 cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
@@ -128,5 +128,7 @@ cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* h
 cudaError_t launch_das_staged_batch(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
 		int storage, bool analytic, cudaStream_t stream);
 size_t das_staged_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages);
+cudaError_t launch_das_group_batch(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		int storage, bool analytic, cudaStream_t stream);
 
 }  // namespace usgb

@@ -87,7 +87,10 @@ class ServingLoop:
         self.batches = [Batch(max_batch, max_elements), Batch(max_batch, max_elements)]
         if das_config:
             for b in self.batches:
-                b.set_das_config(*das_config)
+                if len(das_config) == 4:  # (variant, rows, stage bytes, stages), as Batch.autotune returns
+                    b.set_das_config(das_config[1], das_config[2], das_config[3], variant=das_config[0])
+                else:                     # (rows, stage bytes, stages)
+                    b.set_das_config(*das_config)
         self.streams = [torch.cuda.Stream(device=self.device), torch.cuda.Stream(device=self.device)]
         self.idle: Dict[Tuple, List[Slot]] = {}
         self.used_bytes = 0
