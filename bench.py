@@ -205,8 +205,8 @@ def run_gpu(args):
     eng = StaEngine(spec)
     if args.das == "plain":
         eng.set_das_variant(0)
-    elif not args.autotune:
-        eng.set_das_variant(1, args.tile_rows, args.stage_bytes, args.stages)
+    elif args.das in ("staged", "group") and not args.autotune:
+        eng.set_das_variant(1 if args.das == "staged" else 2, args.tile_rows, args.stage_bytes, args.stages)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream)
     with torch.cuda.stream(stream):
@@ -218,8 +218,10 @@ def run_gpu(args):
     stream.synchronize()
     eng.set_grid_device(grid)
     info = eng.signal_info()
-    if args.das == "staged" and args.autotune:
-        # Pick the staged kernel's tile / stage shape on this frame (untimed).
+    if args.das != "plain" and args.autotune:
+        # Pick the delay-and-sum kernel and its tile / stage shape on this
+        # frame (untimed): staged and receiver-group kernels, every shape
+        # that fits, and the plain kernel.
         sig_t = torch.empty(info["signal_bytes"] // 4 + 1, dtype=torch.float32, device=dev)
         eng.prepare_signals_device(rf0, sig_t)
         eng.autotune_das(sig_t, value, factor, iterations=2)
@@ -513,10 +515,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cf2d", choices=["cf2d", "plain2d", "matrix3d"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
-    ap.add_argument("--das", default="staged", choices=["plain", "staged"])
-    ap.add_argument("--tile-rows", type=int, default=8)
-    ap.add_argument("--stage-bytes", type=int, default=16384)
-    ap.add_argument("--stages", type=int, default=8)
+    ap.add_argument("--das", default="auto", choices=["auto", "plain", "staged", "group"],
+                    help="delay-and-sum kernel; auto = autotuned over every kernel and shape")
+    ap.add_argument("--tile-rows", type=int, default=4)
+    ap.add_argument("--stage-bytes", type=int, default=32768)
+    ap.add_argument("--stages", type=int, default=2)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -199,6 +199,25 @@ int usgb_autotune_das(usgb_ctx* ctx, const void* d_signals, float* d_value, floa
 int usgb_synchronize(usgb_ctx* ctx);
 
 /*
+ * Image post-processing (the reference's dB image: envelope along each image
+ * column, ParallelHilbertEnvelope<float>::calculateDim2Value,
+ * src/parallel/ParallelHilbertEnvelope.h:83-95, then Util::linearToDecibels,
+ * src/util/Util.h:600-613). A usgb_post holds the FFT tables for columns of
+ * num_samples values (the grid's nrows).
+ *   usgb_post_envelope_device: d_out[c][n] = |analytic signal of column c|[n]
+ *     for num_columns columns of num_samples floats (column-major images as
+ *     the processors write them); d_in and d_out may be the same buffer.
+ *   usgb_post_decibels_device: in place, v / max|v| (unless the maximum is 0),
+ *     then 20 log10(v), or min_db at or below 10^(min_db / 20).
+ */
+typedef struct usgb_post usgb_post;
+int usgb_post_create(uint32_t num_samples, usgb_post** post);
+void usgb_post_destroy(usgb_post* post);
+const char* usgb_post_last_error(const usgb_post* post);
+int usgb_post_envelope_device(usgb_post* post, const float* d_in, float* d_out, uint32_t num_columns, void* stream);
+int usgb_post_decibels_device(usgb_post* post, float* d_data, size_t n, float min_db, void* stream);
+
+/*
  * One frame without any device allocation. No counterpart in the reference:
  * it exists for callers that must not allocate device memory while they run,
  * e.g. a host that has already given nearly all GPU memory to its own pool

@@ -5,6 +5,7 @@ this package, as the checker. The product (``us_lab4a_gb300``) never imports it.
 """
 from .oracle import (  # noqa: F401
     OracleSpec, available, build, lib_path, process, das, interp_taps, interp4x_taps,
-    upsample, hilbert, fft, remove_dc, scf, pcf, hilbert_fft_size, next_fast_even_size,
+    upsample, hilbert, envelope, linear_to_decibels, fft, remove_dc, scf, pcf, hilbert_fft_size,
+    next_fast_even_size,
     kaiser_beta, kaiser_size,
 )

@@ -243,6 +243,28 @@ def hilbert(x: np.ndarray, dtype=np.float64) -> np.ndarray:
     return out.view(np.complex64 if dtype == np.float32 else np.complex128)
 
 
+def envelope(x: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """HilbertEnvelope::calculate along the last axis (every row of x)."""
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    x = np.ascontiguousarray(x, dtype=dtype)
+    n = x.shape[-1]
+    out = np.zeros_like(x)
+    f = _lib().orc_envelope_f32 if dtype == np.float32 else _lib().orc_envelope_f64
+    f.argtypes = [C.POINTER(ct), C.c_uint, C.c_uint, C.POINTER(ct)]
+    _err(f(_ptr(x, ct), n, x.size // n, _ptr(out, ct)))
+    return out
+
+
+def linear_to_decibels(x: np.ndarray, min_db: float, dtype=np.float32) -> np.ndarray:
+    """Util::linearToDecibels(vector, minDecibels) over all of x (a copy)."""
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    out = np.array(x, dtype=dtype, copy=True, order="C")
+    f = _lib().orc_linear_to_decibels_f32 if dtype == np.float32 else _lib().orc_linear_to_decibels_f64
+    f.argtypes = [C.POINTER(ct), C.c_size_t, ct]
+    _err(f(_ptr(out, ct), out.size, min_db))
+    return out
+
+
 def fft(x: np.ndarray, sign: int = -1) -> np.ndarray:
     x = np.ascontiguousarray(x, dtype=np.complex128)
     out = np.zeros_like(x)

@@ -453,6 +453,15 @@ public:
 		const T coef = 2 / static_cast<T>(N);
 		for (unsigned i = 0; i < len; ++i) out[i] = C(coef * buf_[i].real(), coef * buf_[i].imag());
 	}
+	// HilbertEnvelope::calculate (src/util/HilbertEnvelope.h:211-232): the
+	// magnitude of the analytic signal, |coef * IFFT| (std::abs of the complex
+	// value, ComplexToScaledAbsoluteOp).
+	void envelope(const T* x, unsigned len, T* out)
+	{
+		std::vector<C> a(len);
+		analytic(x, len, a.data());
+		for (unsigned i = 0; i < len; ++i) out[i] = std::abs(a[i]);
+	}
 private:
 	FFT<T> fft_, half_;
 	std::vector<C> buf_, z_, wN_;
@@ -539,6 +548,25 @@ enum CFKind { CF_NONE = 0, CF_PCF = 1, CF_SCF = 2, CF_MF = 3 };
 // ---------------------------------------------------------------------------
 // Whole processor.
 // ---------------------------------------------------------------------------
+// Util::linearToDecibels(std::vector<T>&, T minDecibels) (src/util/Util.h:600-613):
+// normalize by the largest magnitude (Util::normalize, :1031-1037: nothing
+// when it is 0), then 20 log10(v), or minDecibels where v <= 10^(minDecibels/20)
+// (decibelsToLinear, :588-592, evaluated in T).
+template<typename T>
+void linear_to_decibels(T* data, std::size_t n, T minDecibels)
+{
+	T maxAbs = 0;
+	for (std::size_t i = 0; i < n; ++i) maxAbs = std::max(maxAbs, std::abs(data[i]));
+	if (maxAbs != 0) {
+		const T coeff = 1 / maxAbs;
+		for (std::size_t i = 0; i < n; ++i) data[i] *= coeff;
+	}
+	const T minVal = std::pow(T(10), minDecibels * T(0.05));
+	for (std::size_t i = 0; i < n; ++i) {
+		data[i] = (data[i] <= minVal) ? minDecibels : T(20) * std::log10(data[i]);
+	}
+}
+
 template<typename T>
 struct StaDesc {
 	unsigned numTx = 0;          // active transmit elements

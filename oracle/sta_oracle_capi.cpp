@@ -178,6 +178,32 @@ int orc_hilbert_f32(const float* x, unsigned len, float* out)
 		return 0;
 	} catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
+int orc_envelope_f64(const double* x, unsigned len, unsigned count, double* out)
+{
+	try {
+		orc::Hilbert<double> h;
+		for (unsigned c = 0; c < count; ++c) h.envelope(x + static_cast<size_t>(c) * len, len, out + static_cast<size_t>(c) * len);
+		return 0;
+	} catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+int orc_envelope_f32(const float* x, unsigned len, unsigned count, float* out)
+{
+	try {
+		orc::Hilbert<float> h;
+		for (unsigned c = 0; c < count; ++c) h.envelope(x + static_cast<size_t>(c) * len, len, out + static_cast<size_t>(c) * len);
+		return 0;
+	} catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+int orc_linear_to_decibels_f32(float* data, size_t n, float min_db)
+{
+	orc::linear_to_decibels<float>(data, n, min_db);
+	return 0;
+}
+int orc_linear_to_decibels_f64(double* data, size_t n, double min_db)
+{
+	orc::linear_to_decibels<double>(data, n, min_db);
+	return 0;
+}
 int orc_fft_f64(const double* in, unsigned n, int sign, double* out)
 {
 	orc::FFT<double> f(n);

@@ -56,6 +56,7 @@ def reference_vectors(ref_test: str) -> dict:
     r = lambda n: h5_float64(os.path.join(ref_test, n + ".h5"))  # noqa: E731
     v = {
         "hilbert_x": r("hilbert_x"), "hilbert_yr": r("hilbert_yr"), "hilbert_yi": r("hilbert_yi"),
+        "hilbert_ya": r("hilbert_ya"),
         "interp_source": r("interp_source"),
         "interp_2x": r("interp_2x"), "interp_8x": r("interp_8x"), "interp_64x": r("interp_64x"),
         "interp4x_x": r("interp_x"), "interp4x_y": r("interp_y"),
@@ -64,7 +65,7 @@ def reference_vectors(ref_test: str) -> dict:
         "kaiser_size_0.5": r("kaiser_size-trans_width_0.5"),
     }
     n = v["hilbert_x"].size
-    assert v["hilbert_yr"].size == n and v["hilbert_yi"].size == n
+    assert v["hilbert_yr"].size == n and v["hilbert_yi"].size == n and v["hilbert_ya"].size == n
     m = v["interp_source"].size
     for U in (2, 8, 64):
         assert v[f"interp_{U}x"].size == m * U, (U, v[f"interp_{U}x"].size)
@@ -147,9 +148,13 @@ def reference_frames() -> dict:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
     args = ap.parse_args()
     vec = reference_vectors(os.path.join(args.reference, "test"))
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
+    if args.vectors_only:
+        print("reference_vectors.npz", os.path.getsize(os.path.join(HERE, "reference_vectors.npz")))
+        return
     from oracle import ref
     if not ref.available():
         ref.build()

@@ -24,6 +24,27 @@ def test_hilbert_transform_golden(oracle_lib, golden_vectors):
     assert np.array_equal(oracle_lib.hilbert(x), yc)
 
 
+def test_hilbert_envelope_golden(oracle_lib, golden_vectors):
+    """TestMethod::testHilbertTransform (TestMethod.cpp:681-710), envelope part:
+    HilbertEnvelope::calculate against test/hilbert_ya.h5."""
+    x = golden_vectors["hilbert_x"]
+    ya = oracle_lib.envelope(x)
+    ref = golden_vectors["hilbert_ya"]
+    assert np.abs(ya - ref).max() / np.abs(ref).max() <= HILBERT_MAX_RELATIVE_ABS_ERROR
+
+
+def test_linear_to_decibels_rules(oracle_lib):
+    """Util::linearToDecibels (Util.h:600-613): normalized by the largest
+    magnitude, 20 log10, values at or below the floor set to the floor; an
+    all-zero input stays at the floor."""
+    x = np.array([0.0, 1e-6, 0.5, 2.0, -2.0, 1.0, 1e-3], np.float32)
+    y = oracle_lib.linear_to_decibels(x, -40.0)
+    assert y[3] == 0.0 and y[4] == -40.0 and y[0] == -40.0 and y[1] == -40.0
+    assert abs(y[2] - 20 * np.log10(0.25)) < 1e-5 and abs(y[5] - 20 * np.log10(0.5)) < 1e-5
+    assert y[6] == -40.0  # 1e-3 / 2 = 5e-4 < 10^-2
+    assert np.all(oracle_lib.linear_to_decibels(np.zeros(5, np.float32), -60.0) == -60.0)
+
+
 @pytest.mark.parametrize("U", [2, 8, 64])
 def test_interpolator_golden(oracle_lib, golden_vectors, U):
     """TestMethod::testInterpolator (TestMethod.cpp:746-794)."""

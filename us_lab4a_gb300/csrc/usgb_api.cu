@@ -713,9 +713,9 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		std::vector<Cand> cands;
 		for (int variant : {1, 2})
 			for (unsigned rows : {4u, 8u, 16u})
-				for (unsigned cap : {8192u, 16384u, 32768u})
+				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u})
 					for (unsigned nst : {2u, 3u, 4u})
-						if (das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
+						if ((variant == 2 || cap % 8192u == 0) && das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
 							cands.push_back({variant, rows, cap, nst});
 		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});
 		cudaEvent_t e0, e1;

@@ -94,20 +94,17 @@ das_direct_kernel(DasParams p)
 	CFState<CF> cf;
 	for (unsigned r = 0; r < p.numRx; ++r) {
 		const float rxd = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
-		// Per-transmitter terms go straight into an even and an odd
+		// The receiver's terms, transmitter by transmitter, into one
 		// accumulator (the order every delay-and-sum kernel of the library uses).
-		float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+		float2 acc = make_float2(0.f, 0.f);
 		const char* rsig = static_cast<const char*>(p.sig) + (static_cast<size_t>(r) * p.sigStride) * sample_bytes<S, ANALYTIC>();
 		for (unsigned t = 0; t < p.numTx; ++t) {
 			float k;
 			const int i = split_delay(__fadd_rn(txd[t * blockDim.x + tid], rxd), k);
 			if (static_cast<unsigned>(i) <= lastIdx) {
-				const char* s = rsig + (t * txStride + i) * sample_bytes<S, ANALYTIC>();
-				if (t & 1) gather<S, ANALYTIC>(s, k, accOdd);
-				else gather<S, ANALYTIC>(s, k, accEven);
+				gather<S, ANALYTIC>(rsig + (t * txStride + i) * sample_bytes<S, ANALYTIC>(), k, acc);
 			}
 		}
-		const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
 		const float2 rs = receiver_sum(acc, __ldg(&p.apod[r]) * p.invScale);
 		total.x += rs.x;
 		total.y += rs.y;

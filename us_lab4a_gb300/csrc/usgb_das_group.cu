@@ -12,8 +12,8 @@
 //
 // Arithmetic is the plain kernel's, term for term: delay = fl(fl(offset +
 // fl(dist_tx * invCT)) + fl(dist_rx * invCT)), the same index / fraction
-// split, each receiver's terms summed in transmitter order into an even- and
-// an odd-transmitter accumulator, receivers folded into the total in order.
+// split, each receiver's terms summed in transmitter order into one
+// accumulator, receivers folded into the total in order.
 // Window bounds come from per-element min/max exactly as in the staged kernel;
 // a window larger than stage_bytes / kGroup is gathered from global memory.
 // FP64 geometry for deep tiles, bounded waits and the error word behave as in
@@ -263,16 +263,14 @@ __device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un,
 template<typename SP, bool Q, bool FULL>
 __device__ __forceinline__ void group_unit(const DasParams& p, const GroupSmem& sm, const GroupStage& m, int u,
 		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
-		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx,
-		float2 (&accE)[kGroup], float2 (&accO)[kGroup])
+		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
 {
 	const int2 un = m.unit[u];
 	const float txv = Delay<Q>::tx(p, sm.txinfo[un.x], px, py, pz, fx);
 	const int4 b0 = *reinterpret_cast<const int4*>(&m.base[u][0]);
 	const int4 b1 = *reinterpret_cast<const int4*>(&m.base[u][4]);
 	const int base[kGroup] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-	if (un.x & 1) group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, accO);
-	else group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, accE);
+	group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, acc);
 }
 
 template<typename SP, int CF, bool Q>
@@ -292,12 +290,11 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 	for (unsigned g = 0; g < numGroups; ++g) {
 		const unsigned nrg = min(static_cast<unsigned>(kGroup), p.numRx - g * kGroup);
 		float rxd[kGroup];
-		float2 accE[kGroup], accO[kGroup];
+		float2 acc[kGroup];  // receiver g * kGroup + j's terms, in transmitter order
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
 			rxd[j] = (static_cast<unsigned>(j) < nrg) ? Delay<Q>::rx(p, sm.rxinfo[g * kGroup + j], px, py, pz, fx) : 0.0f;
-			accE[j] = make_float2(0.f, 0.f);
-			accO[j] = make_float2(0.f, 0.f);
+			acc[j] = make_float2(0.f, 0.f);
 		}
 		bool last = false;
 		while (!last) {
@@ -311,12 +308,12 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 			if (nrg == static_cast<unsigned>(kGroup)) {
 				for (int u = 0; u < head.x; ++u) {
 					group_unit<SP, Q, true>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
-							accE, accO);
+							acc);
 				}
 			} else {
 				for (int u = 0; u < head.x; ++u) {
 					group_unit<SP, Q, false>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
-							accE, accO);
+							acc);
 				}
 			}
 			last = head.y != 0;
@@ -331,8 +328,7 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
 			if (static_cast<unsigned>(j) < nrg) {
-				const float2 acc = make_float2(accE[j].x + accO[j].x, accE[j].y + accO[j].y);
-				const float2 rs = receiver_sum(acc, sm.rxinfo[g * kGroup + j].z);
+				const float2 rs = receiver_sum(acc[j], sm.rxinfo[g * kGroup + j].z);
 				total.x += rs.x;
 				total.y += rs.y;
 				cf.add(rs);
@@ -424,8 +420,12 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	         : group_consume<SP, CF, false>(p, sm, it, px, py, pz, active, pix, fx);
 }
 
+// Resident blocks per SM the register allocation is held to (shared memory
+// permitting): 5 for 4-row tiles (at most 81 registers a thread).
+template<int TROWS> constexpr int group_min_blocks() { return TROWS == 4 ? 5 : (TROWS == 8 ? 3 : 1); }
+
 template<int S, int CF, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32)
+__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
 das_group_kernel(DasParams p)
 {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -490,7 +490,7 @@ __device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, co
 
 // Many frames: persistent blocks walk the tiles of every frame in the batch.
 template<int S, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32)
+__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
 das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
 		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
 {

@@ -257,7 +257,7 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 	const T* zero = reinterpret_cast<const T*>(sm.zero);
 	float2 total = make_float2(0.f, 0.f);
 	CFState<CF> cf;
-	float2 accEven = make_float2(0.f, 0.f), accOdd = make_float2(0.f, 0.f);
+	float2 acc = make_float2(0.f, 0.f);  // receiver r's terms, in transmitter order
 	unsigned r = 0;
 	// Receiver r's delay, and the next receiver's computed one receiver
 	// ahead (its latency hides behind the current receiver's gathers).
@@ -275,37 +275,27 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 		const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
 		const int4 head = *reinterpret_cast<const int4*>(&m.count);
 		const int n = head.x;
-		// Windows of a stage are consecutive transmitters of receiver r:
-		// window w goes to the accumulator of its transmitter's parity. With
-		// the accumulators swapped for a stage that starts on an odd
-		// transmitter, even w is always `a0` and odd w `a1`.
-		float2 a0 = accEven, a1 = accOdd;
-		if (head.z) { a0 = accOdd; a1 = accEven; }
+		// Windows of a stage are consecutive transmitters of receiver r.
 		if (!head.w) {
 			int w = 0;
-			// Four windows per iteration (two per accumulator): four independent
-			// delay / load chains in flight per thread.
 #pragma unroll 2
 			for (; w + 1 < n; w += 2) {
 				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
 				const int2 wb = *reinterpret_cast<const int2*>(&m.win[w + 1]);
-				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, a0);
-				gather_staged<SP, Q>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, fx, zero, a1);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, acc);
+				gather_staged<SP, Q>(buf, wb.y, *reinterpret_cast<const float*>(txdSlot + wb.x), rxd, lastIdx, fx, zero, acc);
 			}
 			if (w < n) {
 				const int2 wa = *reinterpret_cast<const int2*>(&m.win[w]);
-				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, a0);
+				gather_staged<SP, Q>(buf, wa.y, *reinterpret_cast<const float*>(txdSlot + wa.x), rxd, lastIdx, fx, zero, acc);
 			}
 		} else {
 			for (int w = 0; w < n; ++w) {
 				const int4 wa = m.win[w];
 				const float txv = *reinterpret_cast<const float*>(txdSlot + wa.x);
-				if (w & 1) gather_any<SP, Q>(wa, buf, sig, txStride, r, p.sigStride, txv, rxd, lastIdx, fx, a1);
-				else gather_any<SP, Q>(wa, buf, sig, txStride, r, p.sigStride, txv, rxd, lastIdx, fx, a0);
+				gather_any<SP, Q>(wa, buf, sig, txStride, r, p.sigStride, txv, rxd, lastIdx, fx, acc);
 			}
 		}
-		if (head.z) { accOdd = a0; accEven = a1; }
-		else { accEven = a0; accOdd = a1; }
 		const int last = head.y;
 		__syncwarp();
 		if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.empty[s]);
@@ -315,13 +305,11 @@ __device__ bool consume(const DasParams& p, const Smem& sm, int& it, float px, f
 			phase ^= 1u;
 		}
 		if (last) {
-			const float2 acc = make_float2(accEven.x + accOdd.x, accEven.y + accOdd.y);
 			const float2 rs = receiver_sum(acc, sm.rxinfo[r].z);
 			total.x += rs.x;
 			total.y += rs.y;
 			cf.add(rs);
-			accEven = make_float2(0.f, 0.f);
-			accOdd = make_float2(0.f, 0.f);
+			acc = make_float2(0.f, 0.f);
 			++r;
 			rxd = rxdNext;
 			if (r + 1 < p.numRx) rxdNext = Delay<Q>::rx(p, sm.rxinfo[r + 1], px, py, pz, fx);

@@ -48,6 +48,9 @@ struct PrepParams {
 };
 
 size_t prep_smem_bytes(const PrepParams& p, bool analytic);
+// Envelope (|analytic signal|, no DC removal) of p.numSignals real sequences of
+// p.ns = p.L samples (U = 1, one FIR tap of 1), float output, p.outStride apart.
+cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream);
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream);
 
 // One launch of the delay-and-sum kernel over the grid points of one frame.

@@ -522,8 +522,10 @@ __device__ void store_pass(const PrepParams& p, const float* rfs, const float* t
 }
 
 // Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
-// the generic FIR loop.
-template<int S, int NT, int U>
+// the generic FIR loop. ENV: the envelope of the input itself instead
+// (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
+// used with U = 1 on image columns).
+template<int S, int NT, int U, bool ENV = false>
 __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 {
 	const PrepLayout lay(p, true);
@@ -544,8 +546,11 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	const float part = fir_pass<NT, U>(p, rfs, taps, xs);
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
 	//    (block_sum's barriers also order the writes above).
-	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
-	for (unsigned n = threadIdx.x; n < L; n += blockDim.x) xs[n] -= mean;
+	float mean = 0.f;
+	if constexpr (!ENV) {
+		mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
+		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) xs[n] -= mean;
+	}
 	__syncthreads();
 
 	// 3. Forward FFT (digit-reversed output).
@@ -576,7 +581,18 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	fft_run<true>(data, p, twLo, twHi, stw);
 
 	// 6. Store (x[n] - mean, y[n]) for n < L; x is recomputed from the A-scan.
-	store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);
+	if constexpr (ENV) {
+		// |x[n] + i y[n]| (the input itself is the real part).
+		const float invM = 1.0f / static_cast<float>(p.M);
+		float* out = reinterpret_cast<float*>(p.out) + static_cast<size_t>(a) * p.outStride;
+		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) {
+			const float x = rfs[n];
+			const float y = xs[n] * invM;
+			out[n] = sqrtf(x * x + y * y);
+		}
+	} else {
+		store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);
+	}
 	__syncthreads();  // shared memory is reused by the next A-scan of a batch
 }
 
@@ -713,6 +729,23 @@ cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* h
 	case STORE_BF16: return launch_batch<STORE_BF16, false>(frames, hdr, smem, blocks, stream);
 	default: return launch_batch<STORE_F32, false>(frames, hdr, smem, blocks, stream);
 	}
+}
+
+// Envelope of numSignals real columns of ns samples (U = 1, single tap).
+__global__ void __launch_bounds__(kPrepThreads, 1)
+envelope_kernel(PrepParams p)
+{
+	extern __shared__ __align__(16) float sm[];
+	prep_analytic_body<STORE_F32, 1, 1, true>(p, blockIdx.x, sm);
+}
+
+cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream)
+{
+	const size_t smem = prep_smem_bytes(p, true);
+	cudaError_t e = cudaFuncSetAttribute(envelope_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	envelope_kernel<<<p.numSignals, kPrepThreads, smem, stream>>>(p);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream)

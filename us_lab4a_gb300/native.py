@@ -58,6 +58,11 @@ SIGNATURES = {
     "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
     "usgb_set_delay_precision": (C.c_int, [C.c_void_p, C.c_uint32]),
     "usgb_batch_set_das_variant": (C.c_int, [C.c_void_p, C.c_int]),
+    "usgb_post_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
+    "usgb_post_destroy": (None, [C.c_void_p]),
+    "usgb_post_last_error": (C.c_char_p, [C.c_void_p]),
+    "usgb_post_envelope_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "usgb_post_decibels_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_void_p]),
     "usgb_process_rf": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "usgb_set_host_direct": (C.c_int, [C.c_void_p, C.c_int]),
     "usgb_get_host_direct": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
