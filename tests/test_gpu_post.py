@@ -59,5 +59,5 @@ def test_decibels_match_oracle(cuda, oracle_lib, min_db):
     floor = (ref == min_db)
     assert np.array_equal(floor, got == min_db)
     assert np.abs(got[~floor] - ref[~floor]).max() <= DB_TOL
-    assert got.max() == 0.0
+    assert abs(got.max()) <= 1e-5  # v * (1 / max) rounds to 1 within an ulp, as in the reference
     assert np.all(zeros == min_db)

@@ -42,8 +42,8 @@ class Batch:
             raise from_status(rc, self._lib.usgb_batch_last_error(self._h).decode())
 
     # (variant, tile rows, stage bytes, stages) tried by autotune(), most likely first.
-    CANDIDATES = ((2, 4, 32768, 2), (2, 4, 16384, 2), (2, 8, 32768, 2), (2, 4, 16384, 3), (2, 8, 16384, 2),
-                  (1, 4, 32768, 2), (1, 4, 16384, 2), (1, 8, 16384, 2))
+    CANDIDATES = ((2, 8, 24576, 2), (2, 8, 32768, 2), (2, 4, 32768, 2), (2, 4, 24576, 2), (2, 8, 20480, 2),
+                  (2, 4, 16384, 2), (1, 8, 24576, 3), (1, 4, 32768, 2), (1, 4, 16384, 2))
 
     def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int, variant: int = None) -> None:
         """Tile shape of the batched delay-and-sum; variant 2 = receiver-group
