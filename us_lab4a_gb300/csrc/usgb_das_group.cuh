@@ -1,0 +1,579 @@
+// Receiver-group delay-and-sum: one thread block per tile of 32 columns x
+// TROWS rows of grid points (lane = column, warp = row), like the staged
+// kernel (usgb_das_staged.cu), but the pairs are visited receiver group by
+// receiver group: for each group of kGroup receivers, every transmitter in
+// turn, with the group's kGroup windows (one per receiver) staged together as
+// one unit. A consumer thread keeps the group's receive delays and its kGroup
+// receiver sums in registers and computes each transmitter's delay once per
+// unit, so no per-pixel delay table lives in shared memory: a block holds
+// only its stage ring and a few per-element tables, several blocks fit on an
+// SM, and arrays of hundreds of elements (2D matrix probes) stage like small
+// ones.
+//
+// Arithmetic is the plain kernel's, term for term: delay = fl(fl(offset +
+// fl(dist_tx * invCT)) + fl(dist_rx * invCT)), the same index / fraction
+// split, each receiver's terms summed in transmitter order into one
+// accumulator, receivers folded into the total in order.
+// Window bounds come from per-element min/max exactly as in the staged kernel;
+// a window larger than stage_bytes / kGroup is gathered from global memory.
+// FP64 geometry for deep tiles, bounded waits and the error word behave as in
+// the staged kernel.
+//
+// This header holds the kernels; usgb_das_group_{f32,f16,bf16}.cu instantiate
+// them for one storage type each (compiled in parallel) and usgb_das_group.cu
+// dispatches.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "usgb_common.cuh"
+#include "usgb_das_cf.cuh"
+#include "usgb_das_tile.cuh"
+#include "usgb_internal.h"
+
+namespace usgb {
+
+namespace {
+
+using namespace tile;
+
+constexpr int kGroup = 8;                  // receivers per group
+constexpr int kMaxUnits = 32 / kGroup;     // units sized per producer pass (one lane per window)
+
+// One stage: up to kMaxUnits units (consecutive transmitters of one receiver
+// group). Window j of unit u: sample idx of receiver g * kGroup + j sits at
+// stage element idx + base[u][j].
+struct GroupStage {
+	int count;        // units in the stage
+	int lastOfGroup;  // the stage ends its receiver group
+	int anyGlobal;    // some window is gathered from global memory
+	int pad;
+	int2 unit[kMaxUnits];           // (transmitter, bit j set: window j from global memory)
+	int base[kMaxUnits][kGroup];
+};
+static_assert(sizeof(GroupStage) % 16 == 0, "stage metadata must stay 16-byte aligned");
+
+struct GroupLayout {
+	unsigned bars, tileMax, zero, meta, rxinfo, txinfo, minmax, partial, stage, total;
+	__host__ __device__ GroupLayout(unsigned maxTx, unsigned maxRx, unsigned trows, unsigned capBytes, unsigned stages)
+	{
+		bars = 0;
+		tileMax = 2 * stages * 8;
+		zero = (tileMax + 8 + 15) & ~15u;
+		meta = zero + 16;
+		rxinfo = meta + stages * static_cast<unsigned>(sizeof(GroupStage));
+		txinfo = rxinfo + maxRx * 16;
+		minmax = (txinfo + maxTx * 8 + 15) & ~15u;
+		partial = minmax + 2 * (maxTx + maxRx) * 4;
+		stage = partial + 2 * trows * (maxTx + maxRx) * 4;
+		stage = (stage + 127) & ~127u;
+		total = stage + stages * capBytes;
+	}
+};
+
+struct GroupSmem {
+	uint64_t* full;
+	uint64_t* empty;
+	int* tileMax;              // [2]: largest transmit / receive delay of the tile (bits of a float >= 0)
+	const unsigned char* zero; // 16 zero bytes
+	GroupStage* meta;
+	float4* rxinfo;            // [maxRx]: (x, y, apodization / storage scale, 0)
+	float2* txinfo;            // [maxTx]: (x, y)
+	float* minT;
+	float* maxT;
+	float* minR;
+	float* maxR;
+	float* partMin;            // [TROWS][maxTx + maxRx]
+	float* partMax;
+	unsigned char* stageBuf;
+	unsigned nst;
+	unsigned capBytes;
+	unsigned maxE;
+};
+
+__device__ __forceinline__ GroupSmem carve_group(unsigned char* smem, const GroupLayout& lay, unsigned maxTx,
+		unsigned maxRx, unsigned trows, unsigned nst, unsigned capBytes)
+{
+	GroupSmem s;
+	s.full = reinterpret_cast<uint64_t*>(smem + lay.bars);
+	s.empty = s.full + nst;
+	s.tileMax = reinterpret_cast<int*>(smem + lay.tileMax);
+	s.zero = smem + lay.zero;
+	s.meta = reinterpret_cast<GroupStage*>(smem + lay.meta);
+	s.rxinfo = reinterpret_cast<float4*>(smem + lay.rxinfo);
+	s.txinfo = reinterpret_cast<float2*>(smem + lay.txinfo);
+	s.minT = reinterpret_cast<float*>(smem + lay.minmax);
+	s.maxT = s.minT + maxTx;
+	s.minR = s.maxT + maxTx;
+	s.maxR = s.minR + maxRx;
+	s.partMin = reinterpret_cast<float*>(smem + lay.partial);
+	s.partMax = s.partMin + trows * (maxTx + maxRx);
+	s.stageBuf = smem + lay.stage;
+	s.nst = nst;
+	s.capBytes = capBytes;
+	s.maxE = maxTx + maxRx;
+	return s;
+}
+
+__device__ __forceinline__ void init_group_barriers(const GroupSmem& sm, int trows)
+{
+	if (threadIdx.x < 4) reinterpret_cast<unsigned*>(const_cast<unsigned char*>(sm.zero))[threadIdx.x] = 0u;
+	if (threadIdx.x == 0) {
+		for (unsigned s = 0; s < sm.nst; ++s) {
+			mbar_init(&sm.full[s], 1);
+			mbar_init(&sm.empty[s], trows);
+		}
+		fence_barrier_init();
+	}
+	__syncthreads();
+}
+
+// ------------------------------------------------------------- producer
+// Lane l sizes window (transmitter t0 + l / kGroup, receiver g * kGroup + l %
+// kGroup); a prefix sum over the lanes packs as many whole units as fit into
+// the stage; lane 0 arms the stage's barrier and every lane copies its window.
+template<typename SP>
+__device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, float margin)
+{
+	using T = typename SP::T;
+	const int nst = static_cast<int>(sm.nst);
+	const unsigned capBytes = sm.capBytes;
+	const unsigned winCap = (capBytes / kGroup) & ~15u;  // a unit always fits in one stage
+	const int lane = threadIdx.x & 31;
+	const int u = lane / kGroup, j = lane % kGroup;
+	const int L = static_cast<int>(p.L);
+	const size_t txStride = static_cast<size_t>(p.numRx) * p.sigStride;
+	const T* sig = reinterpret_cast<const T*>(p.sig);
+	const unsigned numGroups = (p.numRx + kGroup - 1) / kGroup;
+	const int itStart = it;
+	int s = it % nst;
+	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
+	bool ok = true;
+	for (unsigned g = 0; g < numGroups && ok; ++g) {
+		const unsigned r = g * kGroup + j;
+		unsigned t0 = 0;
+		while (t0 < p.numTx) {
+			if (it >= nst) {
+				bool w = true;
+				if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], phase ^ 1u, kWaitLimitNs);
+				w = __shfl_sync(0xffffffffu, w, 0);
+				if (!w) {
+					if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+					ok = false;
+					break;
+				}
+			}
+			const unsigned t = t0 + u;
+			int lo = 0, kind = kEmptyWindow;
+			unsigned wb = 0;
+			if (t < p.numTx && r < p.numRx) {
+				const float a = __fadd_rn(sm.minT[t], sm.minR[r]);
+				const float b = __fadd_rn(sm.maxT[t], sm.maxR[r]);
+				const float lof = fmaxf(floorf(a) - margin, 0.0f);
+				const float hif = fminf(floorf(b) + 1.0f + margin, static_cast<float>(L - 1));
+				if (lof <= static_cast<float>(L - 2) && hif >= 1.0f && hif >= lof) {
+					lo = static_cast<int>(lof) & ~(SP::kAlign - 1);
+					const unsigned cnt = static_cast<unsigned>(static_cast<int>(hif) - lo + 1);
+					wb = (cnt * static_cast<unsigned>(sizeof(T)) + 15u) & ~15u;
+					if (wb > winCap) {
+						kind = kGlobalWindow;
+						wb = 0;
+					} else {
+						kind = 0;
+					}
+				}
+			}
+			unsigned incl = wb;
+			for (int o = 1; o < 32; o <<= 1) {
+				const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+				if (lane >= o) incl += v;
+			}
+			// Bytes through the end of this lane's unit; the units that fit
+			// form a prefix (the first one always fits: winCap * kGroup <= cap).
+			const unsigned unitEnd = __shfl_sync(0xffffffffu, incl, u * kGroup + kGroup - 1);
+			const bool fits = t < p.numTx && unitEnd <= capBytes;
+			const int n = __popc(__ballot_sync(0xffffffffu, fits && j == 0));
+			const unsigned globalBits = __ballot_sync(0xffffffffu, kind == kGlobalWindow && u < n);
+			const unsigned total = __shfl_sync(0xffffffffu, incl, n * kGroup - 1);
+			const unsigned excl = incl - wb;
+			GroupStage& m = sm.meta[s];
+			if (u < n) {
+				m.base[u][j] = (kind == 0) ? static_cast<int>(excl / sizeof(T)) - lo : 0;
+				if (j == 0) m.unit[u] = make_int2(static_cast<int>(t), static_cast<int>((globalBits >> (u * kGroup)) & 0xffu));
+			}
+			if (lane == 0) {
+				m.count = n;
+				m.lastOfGroup = (t0 + n >= p.numTx) ? 1 : 0;
+				m.anyGlobal = globalBits != 0u ? 1 : 0;
+			}
+			__threadfence_block();
+			__syncwarp();
+			if (lane == 0) mbar_arrive_expect_tx(&sm.full[s], total);
+			__syncwarp();
+			if (u < n && wb > 0) {
+				const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
+				bulk_copy_g2s(sm.stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &sm.full[s]);
+			}
+			t0 += static_cast<unsigned>(n);
+			++it;
+			if (++s == nst) {
+				s = 0;
+				phase ^= 1u;
+			}
+		}
+	}
+	if (lane == 0) {
+		const int from = (it - nst > itStart) ? it - nst : itStart;
+		for (int q = from; q < it; ++q) {
+			if (!mbar_wait_bounded(&sm.full[q % nst], (q / nst) & 1, kWaitLimitNs)) {
+				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+				ok = false;
+				break;
+			}
+		}
+	}
+	return ok;
+}
+
+// ------------------------------------------------------------- consumers
+// The group's gathers of one unit into `acc` (the accumulators of the unit's
+// transmitter parity). FULL: every receiver of the group exists.
+template<typename SP, bool Q, bool FULL>
+__device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un, const int* base,
+		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg, float txv,
+		const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+{
+	using T = typename SP::T;
+	if (!anyGlobal) {
+#pragma unroll
+		for (int j = 0; j < kGroup; ++j) {
+			if (FULL || static_cast<unsigned>(j) < nrg) gather_staged<SP, Q>(buf, base[j], txv, rxd[j], lastIdx, fx, zero, acc[j]);
+		}
+	} else {
+		const T* sig = reinterpret_cast<const T*>(p.sig) + static_cast<size_t>(un.x) * p.numRx * p.sigStride;
+#pragma unroll
+		for (int j = 0; j < kGroup; ++j) {
+			if (FULL || static_cast<unsigned>(j) < nrg) {
+				if ((un.y >> j) & 1) {
+					gather_global<SP, Q>(sig + static_cast<size_t>(g * kGroup + j) * p.sigStride, txv, rxd[j], lastIdx,
+							fx, acc[j]);
+				} else {
+					gather_staged<SP, Q>(buf, base[j], txv, rxd[j], lastIdx, fx, zero, acc[j]);
+				}
+			}
+		}
+	}
+}
+
+// One unit u of stage m: its transmitter's delay once, then the group's gathers.
+template<typename SP, bool Q, bool FULL>
+__device__ __forceinline__ void group_unit(const DasParams& p, const GroupSmem& sm, const GroupStage& m, int u,
+		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
+		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+{
+	const int2 un = m.unit[u];
+	const float txv = Delay<Q>::tx(p, sm.txinfo[un.x], px, py, pz, fx);
+	const int4 b0 = *reinterpret_cast<const int4*>(&m.base[u][0]);
+	const int4 b1 = *reinterpret_cast<const int4*>(&m.base[u][4]);
+	const int base[kGroup] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+	group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, acc);
+}
+
+template<typename SP, int CF, bool Q>
+__device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, float px, float py, float pz,
+		bool active, unsigned pix, const Fixed& fx)
+{
+	using T = typename SP::T;
+	const int nst = static_cast<int>(sm.nst);
+	const unsigned capBytes = sm.capBytes;
+	const unsigned lastIdx = p.L - 2;
+	const T* zero = reinterpret_cast<const T*>(sm.zero);
+	const unsigned numGroups = (p.numRx + kGroup - 1) / kGroup;
+	float2 total = make_float2(0.f, 0.f);
+	CFState<CF> cf;
+	int s = it % nst;
+	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
+	for (unsigned g = 0; g < numGroups; ++g) {
+		const unsigned nrg = min(static_cast<unsigned>(kGroup), p.numRx - g * kGroup);
+		float rxd[kGroup];
+		float2 acc[kGroup];  // receiver g * kGroup + j's terms, in transmitter order
+#pragma unroll
+		for (int j = 0; j < kGroup; ++j) {
+			rxd[j] = (static_cast<unsigned>(j) < nrg) ? Delay<Q>::rx(p, sm.rxinfo[g * kGroup + j], px, py, pz, fx) : 0.0f;
+			acc[j] = make_float2(0.f, 0.f);
+		}
+		bool last = false;
+		while (!last) {
+			if (!mbar_wait_bounded(&sm.full[s], phase, kWaitLimitNs)) {
+				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+				return false;
+			}
+			const GroupStage& m = sm.meta[s];
+			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
+			const int4 head = *reinterpret_cast<const int4*>(&m.count);
+			if (nrg == static_cast<unsigned>(kGroup)) {
+				for (int u = 0; u < head.x; ++u) {
+					group_unit<SP, Q, true>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
+							acc);
+				}
+			} else {
+				for (int u = 0; u < head.x; ++u) {
+					group_unit<SP, Q, false>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
+							acc);
+				}
+			}
+			last = head.y != 0;
+			__syncwarp();
+			if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.empty[s]);
+			++it;
+			if (++s == nst) {
+				s = 0;
+				phase ^= 1u;
+			}
+		}
+#pragma unroll
+		for (int j = 0; j < kGroup; ++j) {
+			if (static_cast<unsigned>(j) < nrg) {
+				const float2 rs = receiver_sum(acc[j], sm.rxinfo[g * kGroup + j].z);
+				total.x += rs.x;
+				total.y += rs.y;
+				cf.add(rs);
+			}
+		}
+	}
+	if (active) {
+		const float v = SP::kAnalytic ? magnitude(total) : total.x;
+		p.value[pix] = v * p.valueCoef;
+		p.factor[pix] = cf.result(p.numRx, p, total);
+	}
+	return true;
+}
+
+// One tile (bx, by) of one frame; `it` is the block's running stage counter.
+template<int S, int CF, bool ANALYTIC, int TROWS>
+__device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx, unsigned by, int& it)
+{
+	using SP = Sample<ANALYTIC, S>;
+	const int warp = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
+	const bool producer = warp == TROWS;
+	const unsigned col = bx * 32 + lane;
+	const unsigned row = by * TROWS + warp;
+	const bool active = !producer && col < p.ncols && row < p.nrows;
+	const unsigned pix = col * p.nrows + row;
+	const unsigned nE = p.numTx + p.numRx;
+
+	// Threads beyond the grid's edge take the nearest grid point of the tile.
+	float px = 0.f, py = 0.f, pz = 0.f;
+	if (!producer) {
+		const unsigned q = min(col, p.ncols - 1) * p.nrows + min(row, p.nrows - 1);
+		px = p.grid[3 * q];
+		py = p.grid[3 * q + 1];
+		pz = p.grid[3 * q + 2];
+	}
+	if (threadIdx.x == 0) {
+		sm.tileMax[0] = 0;
+		sm.tileMax[1] = 0;
+	}
+	for (unsigned r = threadIdx.x; r < p.numRx; r += blockDim.x) {
+		sm.rxinfo[r] = make_float4(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), __ldg(&p.apod[r]) * p.invScale, 0.f);
+	}
+	for (unsigned t = threadIdx.x; t < p.numTx; t += blockDim.x) {
+		sm.txinfo[t] = make_float2(__ldg(&p.txXY[2 * t]), __ldg(&p.txXY[2 * t + 1]));
+	}
+	// Per-warp min/max of every element's FP32 delay over the tile.
+	if (!producer) {
+		for (unsigned e = 0; e < nE; ++e) {
+			float v;
+			if (e < p.numTx) {
+				v = __fadd_rn(p.signalOffset,
+						__fmul_rn(distance3d_z0(__ldg(&p.txXY[2 * e]), __ldg(&p.txXY[2 * e + 1]), px, py, pz), p.invCT));
+			} else {
+				const unsigned r = e - p.numTx;
+				v = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
+			}
+			float mn = v, mx = v;
+			for (int o = 16; o > 0; o >>= 1) {
+				mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+				mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+			}
+			if (lane == 0) {
+				sm.partMin[warp * sm.maxE + e] = mn;
+				sm.partMax[warp * sm.maxE + e] = mx;
+			}
+		}
+	}
+	__syncthreads();
+	float topT = 0.f, topR = 0.f;
+	for (unsigned e = threadIdx.x; e < nE; e += blockDim.x) {
+		float mn = sm.partMin[e], mx = sm.partMax[e];
+		for (int w = 1; w < TROWS; ++w) {
+			mn = fminf(mn, sm.partMin[w * sm.maxE + e]);
+			mx = fmaxf(mx, sm.partMax[w * sm.maxE + e]);
+		}
+		if (e < p.numTx) { sm.minT[e] = mn; sm.maxT[e] = mx; topT = fmaxf(topT, mx); }
+		else { sm.minR[e - p.numTx] = mn; sm.maxR[e - p.numTx] = mx; topR = fmaxf(topR, mx); }
+	}
+	if (topT > 0.f) atomicMax(&sm.tileMax[0], __float_as_int(topT));
+	if (topR > 0.f) atomicMax(&sm.tileMax[1], __float_as_int(topR));
+	__syncthreads();
+
+	const float topTx = __int_as_float(sm.tileMax[0]), topRx = __int_as_float(sm.tileMax[1]);
+	const bool q = p.delayMode == 2 || (p.delayMode == 0 && topTx + topRx > kDeepDelaySamples);
+	const Fixed fx = fixed_format(fmaxf(fmaxf(topTx, topRx), fabsf(p.signalOffset)));
+	if (producer) return group_produce<SP>(p, sm, it, q ? 2.0f : 0.0f);
+	return q ? group_consume<SP, CF, true>(p, sm, it, px, py, pz, active, pix, fx)
+	         : group_consume<SP, CF, false>(p, sm, it, px, py, pz, active, pix, fx);
+}
+
+// Resident blocks per SM the register allocation is held to (shared memory
+// permitting): 5 for 4-row tiles (at most 81 registers a thread).
+template<int TROWS> constexpr int group_min_blocks() { return TROWS == 4 ? 5 : (TROWS == 8 ? 3 : 1); }
+
+template<int S, int CF, bool ANALYTIC, int TROWS>
+__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
+das_group_kernel(DasParams p)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	const GroupLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
+	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, TROWS, p.stages, p.stageBytes);
+	init_group_barriers(sm, TROWS);
+	int it = 0;
+	group_tile<S, CF, ANALYTIC, TROWS>(p, sm, blockIdx.x, blockIdx.y, it);
+}
+
+template<int S, int CF, bool ANALYTIC, int TROWS>
+cudaError_t launch_group_one(const DasParams& p, cudaStream_t stream)
+{
+	const GroupLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
+	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TROWS>,
+			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
+	if (e != cudaSuccess) return e;
+	const dim3 grid((p.ncols + 31) / 32, (p.nrows + TROWS - 1) / TROWS);
+	das_group_kernel<S, CF, ANALYTIC, TROWS><<<grid, (TROWS + 1) * 32, lay.total, stream>>>(p);
+	return cudaGetLastError();
+}
+
+template<int S, int CF, bool ANALYTIC>
+cudaError_t launch_group_rows(const DasParams& p, cudaStream_t stream)
+{
+	switch (p.tileRows) {
+	case 4: return launch_group_one<S, CF, ANALYTIC, 4>(p, stream);
+	case 16: return launch_group_one<S, CF, ANALYTIC, 16>(p, stream);
+	default: return launch_group_one<S, CF, ANALYTIC, 8>(p, stream);
+	}
+}
+
+template<int S>
+cudaError_t launch_group_cf(const DasParams& p, int cf, bool analytic, cudaStream_t stream)
+{
+	if (!analytic) {
+		return (cf == CF_SCF) ? launch_group_rows<S, CF_SCF, false>(p, stream) : launch_group_rows<S, CF_NONE, false>(p, stream);
+	}
+	switch (cf) {
+	case CF_PCF: return launch_group_rows<S, CF_PCF, true>(p, stream);
+	case CF_SCF: return launch_group_rows<S, CF_SCF, true>(p, stream);
+	case CF_MF: return launch_group_rows<S, CF_MF, true>(p, stream);
+	default: return launch_group_rows<S, CF_NONE, true>(p, stream);
+	}
+}
+
+template<int S, bool ANALYTIC, int TROWS>
+__device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, const GroupSmem& sm, unsigned bx,
+		unsigned by, int& it)
+{
+	if (!ANALYTIC) {
+		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TROWS>(p, sm, bx, by, it)
+		                      : group_tile<S, CF_NONE, false, TROWS>(p, sm, bx, by, it);
+	}
+	switch (cf) {
+	case CF_PCF: return group_tile<S, CF_PCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_SCF: return group_tile<S, CF_SCF, true, TROWS>(p, sm, bx, by, it);
+	case CF_MF: return group_tile<S, CF_MF, true, TROWS>(p, sm, bx, by, it);
+	default: return group_tile<S, CF_NONE, true, TROWS>(p, sm, bx, by, it);
+	}
+}
+
+// Many frames: persistent blocks walk the tiles of every frame in the batch.
+template<int S, bool ANALYTIC, int TROWS>
+__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
+das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
+		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
+{
+	extern __shared__ __align__(128) unsigned char smem[];
+	__shared__ DasParams sp;
+	__shared__ int sAbort;
+	const GroupLayout lay(maxTx, maxRx, TROWS, capBytes, stages);
+	const GroupSmem sm = carve_group(smem, lay, maxTx, maxRx, TROWS, stages, capBytes);
+	if (threadIdx.x == 0) sAbort = 0;
+	init_group_barriers(sm, TROWS);
+	const unsigned count = hdr->count;
+	const unsigned totalTiles = hdr->totalTiles;
+	int it = 0;
+	unsigned f = 0;
+	for (unsigned w = blockIdx.x; w < totalTiles; w += gridDim.x) {
+		while (f + 1 < count && frames[f + 1].tileBegin <= w) ++f;  // work items are visited in increasing order
+		__syncthreads();  // the previous tile is done with sp and the shared tables
+		if (threadIdx.x == 0) sp = frames[f].das;
+		__syncthreads();
+		if (sAbort) break;
+		const unsigned local = w - frames[f].tileBegin;
+		const unsigned tilesX = frames[f].tilesX;
+		const bool ok = group_tile_any_cf<S, ANALYTIC, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
+		if (!ok) sAbort = 1;
+	}
+}
+
+template<int S, bool ANALYTIC, int TROWS>
+cudaError_t launch_group_batch_one(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		cudaStream_t stream)
+{
+	const GroupLayout lay(c.maxTx, c.maxRx, TROWS, c.stageBytes, c.stages);
+	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TROWS>;
+	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
+	if (e != cudaSuccess) return e;
+	unsigned blocks = c.blocks;
+	if (blocks == 0) {  // as many resident blocks as the SMs hold
+		int perSM = 0, dev = 0, sms = 0;
+		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, (TROWS + 1) * 32, lay.total)) != cudaSuccess) return e;
+		if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+		if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+		blocks = static_cast<unsigned>(sms) * static_cast<unsigned>(perSM > 0 ? perSM : 1);
+	}
+	kernel<<<blocks, (TROWS + 1) * 32, lay.total, stream>>>(frames, hdr, c.maxTx, c.maxRx, c.stageBytes, c.stages);
+	return cudaGetLastError();
+}
+
+template<int S, bool ANALYTIC>
+cudaError_t group_batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
+		cudaStream_t stream)
+{
+	switch (c.tileRows) {
+	case 4: return launch_group_batch_one<S, ANALYTIC, 4>(frames, hdr, c, stream);
+	case 16: return launch_group_batch_one<S, ANALYTIC, 16>(frames, hdr, c, stream);
+	default: return launch_group_batch_one<S, ANALYTIC, 8>(frames, hdr, c, stream);
+	}
+}
+
+}  // namespace
+
+// The launchers of one storage type S (instantiated by one source file each).
+template<int S>
+cudaError_t launch_das_group_storage(const DasParams& p, int cf, bool analytic, cudaStream_t stream)
+{
+	return launch_group_cf<S>(p, cf, analytic, stream);
+}
+
+template<int S>
+cudaError_t launch_das_group_batch_storage(const BatchDasFrame* frames, const BatchHeader* hdr,
+		const BatchDasConfig& c, bool analytic, cudaStream_t stream)
+{
+	return analytic ? group_batch_rows<S, true>(frames, hdr, c, stream) : group_batch_rows<S, false>(frames, hdr, c, stream);
+}
+
+inline size_t group_layout_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages)
+{
+	return GroupLayout(numTx, numRx, tileRows, capBytes, stages).total;
+}
+
+}  // namespace usgb

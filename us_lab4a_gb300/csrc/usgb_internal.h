@@ -48,6 +48,9 @@ struct PrepParams {
 };
 
 size_t prep_smem_bytes(const PrepParams& p, bool analytic);
+// Threads per preparation block for `smem` bytes of shared memory a block:
+// 128 when four blocks fit on an SM, 256 when two fit, else 512.
+int prep_threads(size_t smem);
 // Envelope (|analytic signal|, no DC removal) of p.numSignals real sequences of
 // p.ns = p.L samples (U = 1, one FIR tap of 1), float output, p.outStride apart.
 cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream);

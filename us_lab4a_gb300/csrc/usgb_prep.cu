@@ -416,29 +416,80 @@ __device__ __forceinline__ float fir_one(const float* rfs, const float* taps, un
 }
 
 // Pass 1: x[n] for n < L into xs (float view), partial sum of [deadZone, L).
+// fir_outputs for two input positions b0 and b1 at once: each broadcast tap
+// load serves both windows (half the tap traffic of two single calls).
+template<int NT, int U>
+__device__ __forceinline__ void fir_outputs2(const float* rfs, const float* taps, unsigned b0, unsigned b1,
+		float* out0, float* out1)
+{
+	constexpr int NTP = (NT + 3) & ~3;
+	float w0[NTP], w1[NTP];
+#pragma unroll
+	for (int t = 0; t < NT; ++t) {
+		w0[t] = rfs[b0 + (NT - 1) - t];
+		w1[t] = rfs[b1 + (NT - 1) - t];
+	}
+#pragma unroll
+	for (int t = NT; t < NTP; ++t) w0[t] = w1[t] = 0.f;
+#pragma unroll
+	for (int r = 0; r < U; ++r) {
+		const float* h = taps + r * NTP;
+		float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+		for (int q = 0; q < NTP / 4; ++q) {
+			const float4 c = lds_taps(h + 4 * q);
+			a0 = fmaf(c.x, w0[4 * q], a0);
+			a1 = fmaf(c.x, w1[4 * q], a1);
+			if (4 * q + 1 < NT) { a0 = fmaf(c.y, w0[4 * q + 1], a0); a1 = fmaf(c.y, w1[4 * q + 1], a1); }
+			if (4 * q + 2 < NT) { a0 = fmaf(c.z, w0[4 * q + 2], a0); a1 = fmaf(c.z, w1[4 * q + 2], a1); }
+			if (4 * q + 3 < NT) { a0 = fmaf(c.w, w0[4 * q + 3], a0); a1 = fmaf(c.w, w1[4 * q + 3], a1); }
+		}
+		out0[r] = a0;
+		out1[r] = a1;
+	}
+}
+
+// The U outputs of input position b: into xs (the packed buffer read as
+// floats) and the running DC sum of [deadZone, L).
+template<int U>
+__device__ __forceinline__ void fir_keep(const PrepParams& p, unsigned b, const float* o, float* xs, float& part)
+{
+#pragma unroll
+	for (int r = 0; r < U; ++r) {
+		if (b * U + r >= p.deadZone) part += o[r];
+	}
+	if (xs) {
+		if constexpr (U % 4 == 0) {
+#pragma unroll
+			for (int r = 0; r < U; r += 4) {
+				*reinterpret_cast<float4*>(xs + b * U + r) = make_float4(o[r], o[r + 1], o[r + 2], o[r + 3]);
+			}
+		} else {
+#pragma unroll
+			for (int r = 0; r < U; ++r) xs[b * U + r] = o[r];
+		}
+	}
+}
+
 template<int NT, int U>
 __device__ float fir_pass(const PrepParams& p, const float* rfs, const float* taps, float* xs)
 {
 	float part = 0.f;
-	if constexpr (NT > 0) {
+	if constexpr (NT > 1) {
+		// Input positions b and b + blockDim.x together.
+		for (unsigned b = threadIdx.x; b < p.ns; b += 2 * blockDim.x) {
+			const unsigned b1 = b + blockDim.x;
+			const bool two = b1 < p.ns;
+			float o0[U], o1[U];
+			fir_outputs2<NT, U>(rfs, taps, b, two ? b1 : b, o0, o1);
+			fir_keep<U>(p, b, o0, xs, part);
+			if (two) fir_keep<U>(p, b1, o1, xs, part);
+		}
+	} else if constexpr (NT > 0) {
 		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
 			float o[U];
 			fir_outputs<NT, U>(rfs, taps, b, o);
-#pragma unroll
-			for (int r = 0; r < U; ++r) {
-				if (b * U + r >= p.deadZone) part += o[r];
-			}
-			if (xs) {
-				if constexpr (U % 4 == 0) {
-#pragma unroll
-					for (int r = 0; r < U; r += 4) {
-						*reinterpret_cast<float4*>(xs + b * U + r) = make_float4(o[r], o[r + 1], o[r + 2], o[r + 3]);
-					}
-				} else {
-#pragma unroll
-					for (int r = 0; r < U; ++r) xs[b * U + r] = o[r];
-				}
-			}
+			fir_keep<U>(p, b, o, xs, part);
 		}
 	} else {
 		for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
@@ -608,16 +659,19 @@ __device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
 	__syncthreads();
 }
 
-template<int S, int NT, int U>
-__global__ void __launch_bounds__(kPrepThreads, 1)
+// Blocks of T threads, 512 / T of them per SM at most 128 registers a thread
+// (short A-scans: several small blocks share an SM instead of one block of
+// 512 threads with most of them idle in the FFT stages).
+template<int S, int NT, int U, int T>
+__global__ void __launch_bounds__(T, kPrepThreads / T)
 prep_analytic_kernel(PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
 	prep_analytic_body<S, NT, U>(p, blockIdx.x, sm);
 }
 
-template<int S, int NT, int U>
-__global__ void __launch_bounds__(kPrepThreads, 1)
+template<int S, int NT, int U, int T>
+__global__ void __launch_bounds__(T, kPrepThreads / T)
 prep_real_kernel(PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
@@ -637,8 +691,8 @@ __host__ __device__ inline int fir_shape(unsigned tapsPerPhase, unsigned U)
 }
 
 // Many frames: persistent blocks walk the A-scans of every frame of the batch.
-template<int S, bool ANALYTIC>
-__global__ void __launch_bounds__(kPrepThreads, 1)
+template<int S, bool ANALYTIC, int T>
+__global__ void __launch_bounds__(T, kPrepThreads / T)
 prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr)
 {
 	extern __shared__ __align__(16) float sm[];
@@ -667,21 +721,31 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 	}
 }
 
+template<int S, int NT, int U, int T>
+cudaError_t launch_kernel_t(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
+{
+	const dim3 grid(p.numSignals), block(T);
+	cudaError_t e;
+	if (analytic) {
+		e = cudaFuncSetAttribute(prep_analytic_kernel<S, NT, U, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		prep_analytic_kernel<S, NT, U, T><<<grid, block, smem, stream>>>(p);
+	} else {
+		e = cudaFuncSetAttribute(prep_real_kernel<S, NT, U, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e != cudaSuccess) return e;
+		prep_real_kernel<S, NT, U, T><<<grid, block, smem, stream>>>(p);
+	}
+	return cudaGetLastError();
+}
+
 template<int S, int NT, int U>
 cudaError_t launch_kernel(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
 {
-	const dim3 grid(p.numSignals), block(kPrepThreads);
-	cudaError_t e;
-	if (analytic) {
-		e = cudaFuncSetAttribute(prep_analytic_kernel<S, NT, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		if (e != cudaSuccess) return e;
-		prep_analytic_kernel<S, NT, U><<<grid, block, smem, stream>>>(p);
-	} else {
-		e = cudaFuncSetAttribute(prep_real_kernel<S, NT, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-		if (e != cudaSuccess) return e;
-		prep_real_kernel<S, NT, U><<<grid, block, smem, stream>>>(p);
+	switch (prep_threads(smem)) {
+	case 128: return launch_kernel_t<S, NT, U, 128>(p, analytic, smem, stream);
+	case 256: return launch_kernel_t<S, NT, U, 256>(p, analytic, smem, stream);
+	default: return launch_kernel_t<S, NT, U, 512>(p, analytic, smem, stream);
 	}
-	return cudaGetLastError();
 }
 
 template<int S>
@@ -696,15 +760,26 @@ cudaError_t dispatch_fir(const PrepParams& p, bool analytic, size_t smem, cudaSt
 	}
 }
 
+template<int S, bool ANALYTIC, int T>
+cudaError_t launch_batch_t(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
+		cudaStream_t stream)
+{
+	cudaError_t e = cudaFuncSetAttribute(prep_batch_kernel<S, ANALYTIC, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	prep_batch_kernel<S, ANALYTIC, T><<<blocks, T, smem, stream>>>(frames, hdr);
+	return cudaGetLastError();
+}
+
 template<int S, bool ANALYTIC>
 cudaError_t launch_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
 		cudaStream_t stream)
 {
-	cudaError_t e = cudaFuncSetAttribute(prep_batch_kernel<S, ANALYTIC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			static_cast<int>(smem));
-	if (e != cudaSuccess) return e;
-	prep_batch_kernel<S, ANALYTIC><<<blocks, kPrepThreads, smem, stream>>>(frames, hdr);
-	return cudaGetLastError();
+	switch (prep_threads(smem)) {
+	case 128: return launch_batch_t<S, ANALYTIC, 128>(frames, hdr, smem, blocks, stream);
+	case 256: return launch_batch_t<S, ANALYTIC, 256>(frames, hdr, smem, blocks, stream);
+	default: return launch_batch_t<S, ANALYTIC, 512>(frames, hdr, smem, blocks, stream);
+	}
 }
 
 }  // namespace
@@ -731,21 +806,39 @@ cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* h
 	}
 }
 
+int prep_threads(size_t smem)
+{
+	// Shared memory of an SM (228 KiB, 1 KiB reserved per block) over the block's.
+	const size_t perSM = (228u * 1024u) / (smem + 1024u);
+	return perSM >= 4 ? 128 : (perSM >= 2 ? 256 : 512);
+}
+
 // Envelope of numSignals real columns of ns samples (U = 1, single tap).
-__global__ void __launch_bounds__(kPrepThreads, 1)
+template<int T>
+__global__ void __launch_bounds__(T, kPrepThreads / T)
 envelope_kernel(PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
 	prep_analytic_body<STORE_F32, 1, 1, true>(p, blockIdx.x, sm);
 }
 
+template<int T>
+cudaError_t launch_envelope_t(const PrepParams& p, size_t smem, cudaStream_t stream)
+{
+	cudaError_t e = cudaFuncSetAttribute(envelope_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	envelope_kernel<T><<<p.numSignals, T, smem, stream>>>(p);
+	return cudaGetLastError();
+}
+
 cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream)
 {
 	const size_t smem = prep_smem_bytes(p, true);
-	cudaError_t e = cudaFuncSetAttribute(envelope_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-	if (e != cudaSuccess) return e;
-	envelope_kernel<<<p.numSignals, kPrepThreads, smem, stream>>>(p);
-	return cudaGetLastError();
+	switch (prep_threads(smem)) {
+	case 128: return launch_envelope_t<128>(p, smem, stream);
+	case 256: return launch_envelope_t<256>(p, smem, stream);
+	default: return launch_envelope_t<512>(p, smem, stream);
+	}
 }
 
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream)
