@@ -8,4 +8,5 @@ from .oracle import (  # noqa: F401
     upsample, hilbert, envelope, linear_to_decibels, fft, remove_dc, scf, pcf, hilbert_fft_size,
     next_fast_even_size,
     kaiser_beta, kaiser_size,
+    SingleSpec, single, SINGLE_T1R1_SAFT, SINGLE_TNRN, SINGLE_SYNTH_Y_TNRN,
 )

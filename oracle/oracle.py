@@ -202,6 +202,101 @@ def das(spec: OracleSpec, signals: np.ndarray, grid_xyz: np.ndarray, dtype=np.fl
     return value.reshape(grid_xyz.shape[:-1]), factor.reshape(grid_xyz.shape[:-1])
 
 
+SINGLE_T1R1_SAFT, SINGLE_TNRN, SINGLE_SYNTH_Y_TNRN = 0, 1, 2
+
+
+def _single_desc_type(ct):
+    class SingleDesc(C.Structure):
+        _fields_ = [
+            ("mode", C.c_int), ("num_signals", C.c_uint), ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("sampling_frequency", ct), ("propagation_speed", ct), ("center_frequency", ct),
+            ("peak_offset", ct), ("dead_zone_m", ct),
+            ("tx_xy", C.POINTER(ct)), ("rx_xy", C.POINTER(ct)), ("rx_apod", C.POINTER(ct)),
+            ("focus_x", ct), ("focus_y", ct), ("focus_z", ct), ("first_tx_delay", ct),
+            ("num_acq", C.c_uint), ("acq_y", C.POINTER(ct)),
+            ("cf", C.c_int), ("pcf_gamma", ct), ("scf_p", ct), ("nthreads", C.c_int),
+        ]
+    return SingleDesc
+
+
+_Single32 = _single_desc_type(C.c_float)
+_Single64 = _single_desc_type(C.c_double)
+
+
+@dataclass
+class SingleSpec:
+    """One frame of a single-term 3D processor (Vectorial3DT1R1SAFTProcessor,
+    Vectorial3DTnRnProcessor or SynthYVectorial3DTnRnProcessor).
+
+    tx_xy: T1R1 -- (num_signals, 2) positions of the active transmit elements;
+    TnRn -- (>= 1, 2), row 0 = the first element of the group (txElemPos[base]).
+    rx_xy: (num_signals, 2). rx_apod: TnRn weights (num_signals).
+    first_tx_delay: txDelays[0] in s. acq_y: synthetic y, the y of each
+    acquisition of the window (num_acq)."""
+    mode: int
+    tx_xy: np.ndarray
+    rx_xy: np.ndarray
+    num_samples: int
+    upsampling: int
+    sampling_frequency: float
+    propagation_speed: float
+    center_frequency: float
+    peak_offset: float = 0.0
+    dead_zone_m: float = 0.0
+    rx_apod: Optional[np.ndarray] = None
+    focus: tuple = (0.0, 0.0, 0.0)
+    first_tx_delay: float = 0.0
+    acq_y: Optional[np.ndarray] = None
+    cf: int = CF_NONE
+    pcf_gamma: float = 1.0
+    scf_p: float = 1.0
+    nthreads: int = field(default_factory=lambda: os.cpu_count() or 1)
+
+    @property
+    def num_signals(self) -> int:
+        return int(self.rx_xy.shape[0])
+
+    @property
+    def num_acq(self) -> int:
+        return int(len(self.acq_y)) if self.mode == SINGLE_SYNTH_Y_TNRN else 1
+
+
+def single(spec: SingleSpec, rf: np.ndarray, grid_xyz: np.ndarray, dtype=np.float64, want_signals: bool = False):
+    """Run a single-term processor. rf: (num_acq, num_signals, num_samples) or
+    (num_signals, num_samples). Returns (value, factor, signals)."""
+    desc_t, ct = (_Single32, C.c_float) if dtype == np.float32 else (_Single64, C.c_double)
+    lib = _lib()
+    f = getattr(lib, "orc_single_" + ("f32" if dtype == np.float32 else "f64"))
+    p = C.POINTER(ct)
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(desc_t), p, p, C.c_size_t, p, p, p]
+    n = spec.num_signals
+    keep = {
+        "tx": np.ascontiguousarray(spec.tx_xy, dtype=dtype),
+        "rx": np.ascontiguousarray(spec.rx_xy, dtype=dtype),
+        "apod": None if spec.rx_apod is None else np.ascontiguousarray(spec.rx_apod, dtype=dtype),
+        "y": None if spec.acq_y is None else np.ascontiguousarray(spec.acq_y, dtype=dtype),
+    }
+    d = desc_t(spec.mode, n, spec.num_samples, spec.upsampling, spec.sampling_frequency, spec.propagation_speed,
+               spec.center_frequency, spec.peak_offset, spec.dead_zone_m,
+               _ptr(keep["tx"], ct), _ptr(keep["rx"], ct), _ptr(keep["apod"], ct),
+               spec.focus[0], spec.focus[1], spec.focus[2], spec.first_tx_delay,
+               spec.num_acq, _ptr(keep["y"], ct), spec.cf, spec.pcf_gamma, spec.scf_p, int(spec.nthreads))
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    assert rf.size == spec.num_acq * n * spec.num_samples, rf.shape
+    g = np.ascontiguousarray(grid_xyz, dtype=dtype).reshape(-1, 3)
+    npix = g.shape[0]
+    value = np.zeros(max(npix, 1), dtype=dtype)
+    factor = np.ones(max(npix, 1), dtype=dtype)
+    L = spec.num_samples * spec.upsampling
+    sig = np.zeros(spec.num_acq * n * L * 2, dtype=dtype) if want_signals else None
+    _err(f(C.byref(d), _ptr(rf, ct), _ptr(g, ct), npix, _ptr(value, ct), _ptr(factor, ct), _ptr(sig, ct)))
+    if sig is not None:
+        sig = sig.view(np.complex64 if dtype == np.float32 else np.complex128).reshape(spec.num_acq, n, L)
+    shape = grid_xyz.shape[:-1]
+    return value[:npix].reshape(shape), factor[:npix].reshape(shape), sig
+
+
 def interp_taps(U: int, half_transition: float = 0.2, dtype=np.float64) -> np.ndarray:
     cap = 8192
     ct = C.c_float if dtype == np.float32 else C.c_double

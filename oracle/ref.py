@@ -104,3 +104,72 @@ def process(*, rf: np.ndarray, grid_xyz: np.ndarray, num_samples: int, upsamplin
     if rc != 0:
         raise RuntimeError(lib.ref_last_error().decode())
     return value, factor
+
+
+def _single_desc(ct):
+    class RefSingleDesc(C.Structure):
+        _fields_ = [
+            ("mode", C.c_int), ("nx", C.c_uint), ("ny", C.c_uint), ("pitch_x", ct), ("pitch_y", ct),
+            ("num_active", C.c_uint), ("active", C.POINTER(C.c_uint)),
+            ("base_element", C.c_uint), ("num_elements", C.c_uint),
+            ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("sampling_frequency", ct), ("propagation_speed", ct), ("center_frequency", ct),
+            ("peak_offset", ct), ("dead_zone_m", ct), ("rx_apod", C.POINTER(ct)),
+            ("focus_x", ct), ("focus_y", ct), ("focus_z", ct),
+            ("num_acq", C.c_uint), ("acq_y", C.POINTER(ct)), ("first_acq", C.c_uint), ("last_acq", C.c_uint),
+            ("cf", C.c_int), ("pcf_gamma", ct), ("tx_delays_out", C.POINTER(ct)),
+        ]
+    return RefSingleDesc
+
+
+_S32, _S64 = _single_desc(C.c_float), _single_desc(C.c_double)
+
+
+def single(*, mode: int, rf: np.ndarray, grid_xyz: np.ndarray, matrix, num_samples: int, upsampling: int,
+           fs: float, c: float, fc: float, peak_offset: float = 0.0, dead_zone_m: float = 0.0,
+           active=None, base_element: int = 0, num_elements: int = 0, rx_apod=None, focus=(0.0, 0.0, 0.0),
+           acq_y=None, first_acq: int = 0, last_acq: int = 0, cf: int = 0, pcf_gamma: float = 1.0,
+           dtype=np.float32):
+    """Run the reference's Vectorial3DT1R1SAFTProcessor (mode 0),
+    Vectorial3DTnRnProcessor (1) or SynthYVectorial3DTnRnProcessor (2) on a
+    matrix array = (nx, ny, pitch_x, pitch_y) (tx = rx positions).
+    T1R1: rf (len(active), num_samples). TnRn: rf (num_elements, num_samples);
+    synthetic y: rf (len(acq_y), num_elements, num_samples), window
+    [first_acq, last_acq]. Returns (value, factor, tx_delays)."""
+    lib = _load()
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    D = _S32 if dtype == np.float32 else _S64
+    f = lib.ref_single_f32 if dtype == np.float32 else lib.ref_single_f64
+    p = C.POINTER(ct)
+    f.argtypes = [C.POINTER(D), p, p, C.c_uint, C.c_uint, p, p]
+    f.restype = C.c_int
+    d = D()
+    d.mode = mode
+    d.nx, d.ny, d.pitch_x, d.pitch_y = matrix
+    act = np.ascontiguousarray(np.arange(matrix[0] * matrix[1]) if active is None else active, dtype=np.uint32)
+    d.num_active = act.size
+    d.active = act.ctypes.data_as(C.POINTER(C.c_uint))
+    d.base_element, d.num_elements = base_element, num_elements
+    d.num_samples, d.upsampling = num_samples, upsampling
+    d.sampling_frequency, d.propagation_speed, d.center_frequency = fs, c, fc
+    d.peak_offset, d.dead_zone_m = peak_offset, dead_zone_m
+    apod = np.ascontiguousarray(np.ones(max(num_elements, 1)) if rx_apod is None else rx_apod, dtype=dtype)
+    d.rx_apod = apod.ctypes.data_as(p)
+    d.focus_x, d.focus_y, d.focus_z = focus
+    ys = np.ascontiguousarray(np.zeros(1) if acq_y is None else acq_y, dtype=dtype)
+    d.num_acq = ys.size if acq_y is not None else 0
+    d.acq_y = ys.ctypes.data_as(p)
+    d.first_acq, d.last_acq = first_acq, last_acq
+    d.cf, d.pcf_gamma = cf, pcf_gamma
+    txd = np.zeros(max(num_elements, 1), dtype)
+    d.tx_delays_out = txd.ctypes.data_as(p)
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    g = np.ascontiguousarray(grid_xyz, dtype=dtype)
+    n1, n2 = g.shape[0], g.shape[1]
+    value = np.zeros((n1, n2), dtype)
+    factor = np.zeros((n1, n2), dtype)
+    rc = f(C.byref(d), rf.ctypes.data_as(p), g.ctypes.data_as(p), n1, n2, value.ctypes.data_as(p),
+           factor.ctypes.data_as(p))
+    if rc != 0:
+        raise RuntimeError(lib.ref_last_error().decode())
+    return value, factor, txd[:num_elements]

@@ -1,6 +1,7 @@
-// Driver that runs the reference's own STA processors, compiled from their
+// Driver that runs the reference's own processors, compiled from their
 // unchanged sources (src/user/processor/{VectorialSTAProcessor,
-// Vectorial3DSTAProcessor,DefaultSTAProcessor}.h), on in-memory RF.
+// Vectorial3DSTAProcessor,DefaultSTAProcessor,Vectorial3DT1R1SAFTProcessor,
+// Vectorial3DTnRnProcessor,SynthYVectorial3DTnRnProcessor}.h), on in-memory RF.
 // TEST INFRASTRUCTURE ONLY: it produces golden outputs for the parity tests
 // and validates the oracle restatement; nothing in the product uses it.
 //
@@ -15,7 +16,12 @@
 #include <unistd.h>
 
 #include "DefaultSTAProcessor.h"
+#include "SynthYVectorial3DTnRnProcessor.h"
+#include "TnRnAcquisition.h"
+#include "TnRnConfiguration.h"
 #include "Vectorial3DSTAProcessor.h"
+#include "Vectorial3DT1R1SAFTProcessor.h"
+#include "Vectorial3DTnRnProcessor.h"
 #include "VectorialSTAProcessor.h"
 #include "XYZValueFactor.h"
 
@@ -42,6 +48,44 @@ public:
 private:
 	const T* rf_;
 	unsigned firstTx_, numRx_, ns_;
+};
+
+// STAAcquisition of a T1R1 SAFT scan: one A-scan per active element, row i of
+// `rf` for element active[i].
+template<typename T>
+class SaftAcquisition : public STAAcquisition<T> {
+public:
+	SaftAcquisition(const T* rf, const std::vector<unsigned>& active, unsigned ns) : rf_(rf), active_(active), ns_(ns) {}
+	void execute(unsigned int txElement, typename STAAcquisition<T>::AcquisitionDataType& acqData) override
+	{
+		unsigned row = 0;
+		while (row < active_.size() && active_[row] != txElement) ++row;
+		if (row == active_.size()) throw std::runtime_error("element not in the active list");
+		acqData.resize(1, ns_);
+		for (unsigned s = 0; s < ns_; ++s) acqData(0, s) = rf_[static_cast<std::size_t>(row) * ns_ + s];
+	}
+private:
+	const T* rf_;
+	std::vector<unsigned> active_;
+	unsigned ns_;
+};
+
+// TnRnAcquisition over a caller-owned (numElements, numSamples) RF block.
+template<typename T>
+class MemoryTnRnAcquisition : public TnRnAcquisition<T> {
+public:
+	MemoryTnRnAcquisition(const T* rf, unsigned numElements, unsigned ns) : rf_(rf), numElements_(numElements), ns_(ns) {}
+	void setData(const T* rf) { rf_ = rf; }
+	void execute(typename TnRnAcquisition<T>::AcquisitionDataType& acqData) override
+	{
+		acqData.resize(numElements_, ns_);
+		for (unsigned r = 0; r < numElements_; ++r) {
+			for (unsigned s = 0; s < ns_; ++s) acqData(r, s) = rf_[static_cast<std::size_t>(r) * ns_ + s];
+		}
+	}
+private:
+	const T* rf_;
+	unsigned numElements_, ns_;
 };
 
 // Temporary key=value file for ParameterMap.
@@ -189,6 +233,126 @@ int run(const RefDesc<T>* dp, const T* rf, const T* gridXYZ, unsigned n1, unsign
 	}
 }
 
+template<typename T>
+struct RefSingleDesc {
+	int mode;                  // 0 T1R1 SAFT, 1 TnRn, 2 synthetic-y TnRn
+	unsigned nx, ny;           // matrix array (ArrayUtil::calculateElementPositions, no offset); tx = rx
+	T pitch_x, pitch_y;
+	unsigned num_active;       // T1R1: active elements (tx list = rx list)
+	const unsigned* active;    // T1R1: the active element numbers
+	unsigned base_element;     // TnRn: base element of the group
+	unsigned num_elements;     // TnRn: group size
+	unsigned num_samples, upsampling;
+	T sampling_frequency, propagation_speed, center_frequency, peak_offset, dead_zone_m;
+	const T* rx_apod;          // TnRn: num_elements weights
+	T focus_x, focus_y, focus_z;
+	unsigned num_acq;          // synthetic y: acquisitions in rf (num_acq x num_elements x num_samples)
+	const T* acq_y;            // synthetic y: num_acq positions
+	unsigned first_acq, last_acq;
+	int cf;                    // 0 none, 1 PCF
+	T pcf_gamma;
+	T* tx_delays_out;          // TnRn: the group's focusing delays (s), num_elements; may be NULL
+};
+
+template<typename T>
+void fill_common(const RefSingleDesc<T>& d, T& fc, T& maxF, T& acqTime, T& minGain, T& maxGain, T& c, T& acqDelay, T& fs, T& dz, T& vs)
+{
+	fc = d.center_frequency;
+	maxF = d.center_frequency * 2;
+	acqTime = 1e-4;
+	minGain = 0;
+	maxGain = 0;
+	c = d.propagation_speed;
+	acqDelay = 0;
+	fs = d.sampling_frequency;
+	dz = d.dead_zone_m;
+	vs = 1;
+}
+
+template<typename T>
+int run_single(const RefSingleDesc<T>* dp, const T* rf, const T* gridXYZ, unsigned n1, unsigned n2, T* value, T* factor)
+{
+	try {
+		const RefSingleDesc<T>& d = *dp;
+		Matrix<XYZValueFactor<T>> grid(n1, n2);
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				grid(i, j).x = gridXYZ[3 * p];
+				grid(i, j).y = gridXYZ[3 * p + 1];
+				grid(i, j).z = gridXYZ[3 * p + 2];
+			}
+		}
+		std::string text = "analytic_signal_coherence_factor_method = none\n";
+		if (d.cf == 1) {
+			char buf[64];
+			std::snprintf(buf, sizeof buf, "%.17g", static_cast<double>(d.pcf_gamma));
+			text = std::string("analytic_signal_coherence_factor_method = phase_coherence_factor\n"
+					"phase_coherence_factor_gamma = ") + buf + "\n";
+		}
+		TempParamFile f(text);
+		ParameterMap pm(f.path);
+		AnalyticSignalCoherenceFactorProcessor<T> cf(pm);
+		if (d.mode == 0) {
+			SA3DConfiguration<T> c;
+			c.numElementsMux = 1024;
+			c.numPulses = 1;
+			fill_common(d, c.centerFrequency, c.maxFrequency, c.acquisitionTime, c.minGain, c.maxGain,
+					c.propagationSpeed, c.acquisitionDelay, c.samplingFrequency, c.deadZoneM, c.valueScale);
+			ArrayUtil::calculateElementPositions(d.pitch_x, d.nx, T(0), d.pitch_y, d.ny, T(0), c.txElemPos);
+			ArrayUtil::calculateElementPositions(d.pitch_x, d.nx, T(0), d.pitch_y, d.ny, T(0), c.rxElemPos);
+			c.activeTxElem.assign(d.active, d.active + d.num_active);
+			c.activeRxElem.assign(d.active, d.active + d.num_active);
+			SaftAcquisition<T> acq(rf, c.activeTxElem, d.num_samples);
+			Vectorial3DT1R1SAFTProcessor<T> proc(c, acq, d.upsampling, cf, d.peak_offset);
+			proc.prepare(0);
+			proc.process(grid);
+		} else {
+			TnRnConfiguration<T> c;
+			c.numElementsMux = d.nx * d.ny;
+			c.numElements = d.num_elements;
+			c.numPulses = 1;
+			fill_common(d, c.centerFrequency, c.maxFrequency, c.acquisitionTime, c.minGain, c.maxGain,
+					c.propagationSpeed, c.acquisitionDelay, c.samplingFrequency, c.deadZoneM, c.valueScale);
+			ArrayUtil::calculateElementPositions(d.pitch_x, d.nx, T(0), d.pitch_y, d.ny, T(0), c.txElemPos);
+			ArrayUtil::calculateElementPositions(d.pitch_x, d.nx, T(0), d.pitch_y, d.ny, T(0), c.rxElemPos);
+			std::vector<T> txDelays;
+			ArrayUtil::calculateTx3DFocusDelay(d.focus_x, d.focus_y, d.focus_z, c.propagationSpeed,
+					c.txElemPos, d.base_element, c.numElements, txDelays);
+			if (d.tx_delays_out) std::copy(txDelays.begin(), txDelays.end(), d.tx_delays_out);
+			std::vector<T> apod(d.rx_apod, d.rx_apod + d.num_elements);
+			MemoryTnRnAcquisition<T> acq(rf, d.num_elements, d.num_samples);
+			if (d.mode == 1) {
+				Vectorial3DTnRnProcessor<T> proc(c, acq, d.upsampling, cf, d.peak_offset, apod);
+				proc.setTxDelays(d.focus_x, d.focus_y, d.focus_z, txDelays);
+				proc.prepare(d.base_element);
+				proc.process(grid);
+			} else {
+				SynthYVectorial3DTnRnProcessor<T> proc(c, acq, d.upsampling, cf, d.peak_offset, apod);
+				proc.setTxDelays(d.focus_x, d.focus_y, d.focus_z, txDelays);
+				proc.prepare(d.base_element);
+				const std::size_t acqSize = static_cast<std::size_t>(d.num_elements) * d.num_samples;
+				for (unsigned a = 0; a < d.num_acq; ++a) {
+					acq.setData(rf + a * acqSize);
+					proc.getAcqData(d.acq_y[a]);
+				}
+				proc.process(d.first_acq, d.last_acq, grid);
+			}
+		}
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				value[p] = grid(i, j).value;
+				factor[p] = grid(i, j).factor;
+			}
+		}
+		return 0;
+	} catch (std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
+}
+
 }  // namespace
 
 extern "C" {
@@ -200,5 +364,13 @@ int ref_process_f32(const RefDesc<float>* d, const float* rf, const float* grid,
 int ref_process_f64(const RefDesc<double>* d, const double* rf, const double* grid, unsigned n1, unsigned n2, double* value, double* factor)
 {
 	return run<double>(d, rf, grid, n1, n2, value, factor);
+}
+int ref_single_f32(const RefSingleDesc<float>* d, const float* rf, const float* grid, unsigned n1, unsigned n2, float* value, float* factor)
+{
+	return run_single<float>(d, rf, grid, n1, n2, value, factor);
+}
+int ref_single_f64(const RefSingleDesc<double>* d, const double* rf, const double* grid, unsigned n1, unsigned n2, double* value, double* factor)
+{
+	return run_single<double>(d, rf, grid, n1, n2, value, factor);
 }
 }

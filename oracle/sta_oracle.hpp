@@ -737,6 +737,157 @@ void delay_and_sum(const StaDesc<T>& d, const std::complex<T>* analytic, const T
 	});
 }
 
+// ---------------------------------------------------------------------------
+// Single-term 3D processors: one prepared A-scan per term, one term per
+// signal (and per acquisition of the synthetic-y window) at each grid point.
+// ---------------------------------------------------------------------------
+enum SingleMode { SINGLE_T1R1_SAFT = 0, SINGLE_TNRN = 1, SINGLE_SYNTH_Y_TNRN = 2 };
+
+template<typename T>
+struct SingleDesc {
+	int mode = SINGLE_T1R1_SAFT;
+	unsigned numSignals = 0;     // T1R1: active elements; TnRn: numElements
+	unsigned numSamples = 0;
+	unsigned upsampling = 1;
+	T samplingFrequency = 0;
+	T propagationSpeed = 0;
+	T centerFrequency = 0;
+	T peakOffset = 0;
+	T deadZoneM = 0;
+	const T* txXY = nullptr;     // T1R1: numSignals tx positions; TnRn: [0] = first element of the group
+	const T* rxXY = nullptr;     // numSignals rx positions
+	const T* rxApod = nullptr;   // TnRn: numSignals weights
+	T focusX = 0, focusY = 0, focusZ = 0;
+	T firstTxDelay = 0;          // txDelays[0], s
+	unsigned numAcq = 1;         // synthetic y: acquisitions of the window
+	const T* acqY = nullptr;     // synthetic y: y of each acquisition of the window
+	int cf = CF_NONE;
+	T pcfGamma = 1;
+	T scfP = 1;
+	int nthreads = 1;
+};
+
+// Distance between two 3D points. Follows src/util/Geometry.h:67-75.
+template<typename T>
+T distance3d(T x0, T y0, T z0, T x1, T y1, T z1)
+{
+	const T dx = x1 - x0;
+	const T dy = y1 - y0;
+	const T dz = z1 - z0;
+	return std::sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// Preparation of numAcq * numSignals A-scans (acquisition-major), as the
+// STA preparation of one transmit event per signal.
+// Follows src/user/processor/Vectorial3DT1R1SAFTProcessor.h:141-173,
+// src/user/processor/Vectorial3DTnRnProcessor.h:173-205 and
+// src/user/processor/SynthYVectorial3DTnRnProcessor.h:171-205.
+template<typename T>
+void prepare_single(const SingleDesc<T>& s, const T* rf, std::vector<std::complex<T>>& analytic)
+{
+	StaDesc<T> d;
+	d.numTx = s.numAcq * s.numSignals;
+	d.numRx = 1;
+	d.numSamples = s.numSamples;
+	d.upsampling = s.upsampling;
+	d.samplingFrequency = s.samplingFrequency;
+	d.propagationSpeed = s.propagationSpeed;
+	d.centerFrequency = s.centerFrequency;
+	d.deadZoneM = s.deadZoneM;
+	d.nthreads = s.nthreads;
+	prepare_signals<T>(d, rf, &analytic, nullptr);
+}
+
+// Per-point single terms, coherence factor over them, value = |sum| scaled.
+// T1R1 SAFT follows src/user/processor/Vectorial3DT1R1SAFTProcessor.h:175-233,
+// TnRn src/user/processor/Vectorial3DTnRnProcessor.h:207-279, synthetic y
+// src/user/processor/SynthYVectorial3DTnRnProcessor.h:220-302.
+// analytic: numAcq * numSignals * L.
+template<typename T>
+void single_term_das(const SingleDesc<T>& d, const std::complex<T>* analytic, unsigned L,
+		const T* gridXYZ, std::size_t npix, T* value, T* factor)
+{
+	const T fsUp = d.samplingFrequency * d.upsampling;
+	const T invCT = fsUp / d.propagationSpeed;
+	const T signalOffset = (d.samplingFrequency * d.upsampling) * d.peakOffset / d.centerFrequency;
+	const bool tnrn = d.mode != SINGLE_T1R1_SAFT;
+	const bool synthY = d.mode == SINGLE_SYNTH_Y_TNRN;
+	const unsigned numAcq = synthY ? d.numAcq : 1U;
+	T d0 = 0, t0 = 0;
+	if (tnrn) {
+		d0 = d.firstTxDelay * fsUp;
+		t0 = distance3d_z0<T>(d.txXY[0], d.txXY[1], d.focusX, d.focusY, d.focusZ) * invCT;
+	}
+	// centerAcq = (firstAcq + lastAcq) / 2, relative to the window.
+	const T centerY = synthY ? d.acqY[(numAcq - 1U) / 2U] : T(0);
+	const T valueFactor = static_cast<T>(1.0 / numAcq);
+	T pcfFactor = 0;
+	if (d.cf == CF_PCF) {
+		const T sigma0 = kPi / std::sqrt(3.0);
+		pcfFactor = d.pcfGamma / sigma0;
+	}
+	const std::size_t numTerms = static_cast<std::size_t>(numAcq) * d.numSignals;
+	parallel_for(npix, d.nthreads, [&](std::size_t b, std::size_t e) {
+		std::vector<std::complex<T>> terms(numTerms);
+		std::vector<T> delayList(d.numSignals), realParts(numTerms), phi, phiAux;
+		for (std::size_t p = b; p < e; ++p) {
+			const T px = gridXYZ[3 * p], py = gridXYZ[3 * p + 1], pz = gridXYZ[3 * p + 2];
+			std::fill(terms.begin(), terms.end(), std::complex<T>(0));
+			for (unsigned a = 0; a < numAcq; ++a) {
+				const T yOffset = synthY ? d.acqY[a] - centerY : T(0);
+				const T qy = synthY ? py - yOffset : py;
+				const std::complex<T>* acqSig = analytic + static_cast<std::size_t>(a) * d.numSignals * L;
+				std::complex<T>* acqTerms = terms.data() + static_cast<std::size_t>(a) * d.numSignals;
+				if (tnrn) {
+					const T t1 = distance3d<T>(d.focusX, d.focusY, d.focusZ, px, qy, pz) * invCT;
+					const T txDelay = (d.focusZ > 0) ? t1 + t0 + d0 : t1 - (t0 - d0);
+					for (unsigned i = 0; i < d.numSignals; ++i) {
+						delayList[i] = distance3d_z0<T>(d.rxXY[2 * i], d.rxXY[2 * i + 1], px, qy, pz) * invCT;
+					}
+					for (unsigned i = 0; i < d.numSignals; ++i) {
+						const T delay = signalOffset + txDelay + delayList[i];
+						const std::size_t idx = static_cast<std::size_t>(delay);
+						const T k = delay - idx;
+						if (idx + 1U < L) {
+							const std::complex<T>* s = acqSig + static_cast<std::size_t>(i) * L + idx;
+							acqTerms[i] = d.rxApod[i] * ((1 - k) * s[0] + k * s[1]);
+						}
+					}
+				} else {
+					for (unsigned i = 0; i < d.numSignals; ++i) {
+						delayList[i] = distance3d_z0<T>(d.txXY[2 * i], d.txXY[2 * i + 1], px, py, pz) * invCT;
+					}
+					for (unsigned i = 0; i < d.numSignals; ++i) {
+						const T rxDelay = distance3d_z0<T>(d.rxXY[2 * i], d.rxXY[2 * i + 1], px, py, pz) * invCT;
+						const T delay = signalOffset + delayList[i] + rxDelay;
+						const std::size_t idx = static_cast<std::size_t>(delay);
+						const T k = delay - idx;
+						if (idx + 1U < L) {
+							const std::complex<T>* s = acqSig + static_cast<std::size_t>(i) * L + idx;
+							acqTerms[i] += (1 - k) * s[0] + k * s[1];
+						}
+					}
+				}
+			}
+			T f = 1;
+			if (d.cf == CF_PCF) {
+				f = pcf<T>(terms.data(), static_cast<unsigned>(numTerms), pcfFactor, phi, phiAux);
+			} else if (d.cf == CF_SCF) {
+				for (std::size_t i = 0; i < numTerms; ++i) realParts[i] = terms[i].real();
+				f = scf<T>(realParts.data(), static_cast<unsigned>(numTerms), d.scfP);
+			} else if (d.cf == CF_MF) {
+				f = mallart_fink_cf<T>(terms.data(), static_cast<unsigned>(numTerms));
+			}
+			std::complex<T> acc(0);
+			for (std::size_t i = 0; i < numTerms; ++i) acc += terms[i];
+			T v = std::abs(acc);
+			if (synthY) v = valueFactor * v;
+			value[p] = v * (T(1) / d.numSignals);
+			factor[p] = f;
+		}
+	});
+}
+
 }  // namespace orc
 
 #endif  // USGB_STA_ORACLE_HPP

@@ -91,6 +91,64 @@ int das_only(const CDesc<T>* c, const T* signals, const T* grid, std::size_t npi
 		return -1;
 	}
 }
+
+template<typename T>
+struct CSingleDesc {
+	int mode;
+	unsigned num_signals, num_samples, upsampling;
+	T sampling_frequency, propagation_speed, center_frequency, peak_offset, dead_zone_m;
+	const T* tx_xy;
+	const T* rx_xy;
+	const T* rx_apod;
+	T focus_x, focus_y, focus_z, first_tx_delay;
+	unsigned num_acq;
+	const T* acq_y;
+	int cf;
+	T pcf_gamma, scf_p;
+	int nthreads;
+};
+
+template<typename T>
+int single(const CSingleDesc<T>* c, const T* rf, const T* grid, std::size_t npix, T* value, T* factor, T* signalsOut)
+{
+	try {
+		orc::SingleDesc<T> d;
+		d.mode = c->mode;
+		d.numSignals = c->num_signals;
+		d.numSamples = c->num_samples;
+		d.upsampling = c->upsampling;
+		d.samplingFrequency = c->sampling_frequency;
+		d.propagationSpeed = c->propagation_speed;
+		d.centerFrequency = c->center_frequency;
+		d.peakOffset = c->peak_offset;
+		d.deadZoneM = c->dead_zone_m;
+		d.txXY = c->tx_xy;
+		d.rxXY = c->rx_xy;
+		d.rxApod = c->rx_apod;
+		d.focusX = c->focus_x;
+		d.focusY = c->focus_y;
+		d.focusZ = c->focus_z;
+		d.firstTxDelay = c->first_tx_delay;
+		d.numAcq = (c->mode == orc::SINGLE_SYNTH_Y_TNRN) ? c->num_acq : 1U;
+		d.acqY = c->acq_y;
+		d.cf = c->cf;
+		d.pcfGamma = c->pcf_gamma;
+		d.scfP = c->scf_p;
+		d.nthreads = c->nthreads;
+		if (d.numSignals == 0 || d.numAcq == 0) throw std::invalid_argument("no signals");
+		if (d.mode != orc::SINGLE_T1R1_SAFT && !d.rxApod) throw std::invalid_argument("missing rx apodization");
+		std::vector<std::complex<T>> analytic;
+		orc::prepare_single<T>(d, rf, analytic);
+		if (signalsOut) std::memcpy(signalsOut, analytic.data(), analytic.size() * sizeof(std::complex<T>));
+		if (grid && npix) {
+			orc::single_term_das<T>(d, analytic.data(), d.numSamples * d.upsampling, grid, npix, value, factor);
+		}
+		return 0;
+	} catch (const std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
+}
 }  // namespace
 
 extern "C" {
@@ -121,6 +179,19 @@ int orc_das_f32(const CDesc<float>* d, const float* signals, const float* grid, 
 int orc_das_f64(const CDesc<double>* d, const double* signals, const double* grid, std::size_t npix, double* value, double* factor)
 {
 	return das_only<double>(d, signals, grid, npix, value, factor);
+}
+
+// Single-term 3D processors (T1R1 SAFT, TnRn, synthetic-y TnRn): preparation
+// of num_acq * num_signals A-scans, then the single-term delay-and-sum.
+int orc_single_f32(const CSingleDesc<float>* d, const float* rf, const float* grid, std::size_t npix,
+		float* value, float* factor, float* signals_out)
+{
+	return single<float>(d, rf, grid, npix, value, factor, signals_out);
+}
+int orc_single_f64(const CSingleDesc<double>* d, const double* rf, const double* grid, std::size_t npix,
+		double* value, double* factor, double* signals_out)
+{
+	return single<double>(d, rf, grid, npix, value, factor, signals_out);
 }
 
 // Building blocks, for the golden-vector tests.

@@ -34,6 +34,11 @@ def golden_frames():
 
 
 @pytest.fixture(scope="session")
+def golden_single():
+    return np.load(os.path.join(GOLDEN, "reference_single.npz"))
+
+
+@pytest.fixture(scope="session")
 def cuda():
     """The GPU tests' device. On a machine with a GPU the native library must
     build and load (no fallback); without one the test is an error, not a skip."""

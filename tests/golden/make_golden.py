@@ -13,8 +13,12 @@ sources are present; the fixtures are committed and travel with the tests).
    (VectorialSTAProcessor, Vectorial3DSTAProcessor, DefaultSTAProcessor,
    compiled from their sources by oracle/refbuild) on small seeded frames,
    with the inputs (RF, grid, parameters) stored beside them.
+3. reference_single.npz: the same for the single-term 3D processors
+   (Vectorial3DT1R1SAFTProcessor, Vectorial3DTnRnProcessor,
+   SynthYVectorial3DTnRnProcessor) on a 6 x 5 matrix array, every input
+   parameter stored beside the outputs.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py [--reference /root/reference] [--vectors-only | --single-only]
 """
 from __future__ import annotations
 
@@ -145,11 +149,88 @@ def reference_frames() -> dict:
     return out
 
 
+SINGLE_ARRAY = (6, 5, 0.3e-3, 0.3e-3)   # nx, ny, pitch_x, pitch_y
+SINGLE_ACQ_Y = (-0.6e-3, -0.3e-3, 0.0, 0.3e-3, 0.6e-3)
+
+# name: (mode, parameters). T1R1: active elements; TnRn: base element, group
+# size, focus z; synthetic y: window of the five acquisitions.
+SINGLE_CASES = {
+    "t1r1_plain": (0, dict(active=(0, 2, 3, 5, 7, 11, 13, 17, 20, 29), upsampling=4, cf=0, peak_offset=1.5,
+                           dead_zone_m=1e-3)),
+    "t1r1_pcf": (0, dict(active=tuple(range(30)), upsampling=8, cf=1, pcf_gamma=1.0, peak_offset=1.0)),
+    "tnrn_focused_pcf": (1, dict(base_element=3, num_elements=20, focus_z=4e-3, upsampling=4, cf=1, pcf_gamma=1.0,
+                                 peak_offset=1.5, dead_zone_m=1e-3, apod="hann")),
+    "tnrn_diverging": (1, dict(base_element=0, num_elements=30, focus_z=-5e-3, upsampling=1, cf=0, peak_offset=0.5)),
+    "synthy_window_pcf": (2, dict(base_element=0, num_elements=30, focus_z=-3e-3, upsampling=4, cf=1, pcf_gamma=2.0,
+                                  peak_offset=1.5, first_acq=1, last_acq=3)),
+    "synthy_all": (2, dict(base_element=0, num_elements=30, focus_z=-3e-3, upsampling=4, cf=0, peak_offset=1.5,
+                           first_acq=0, last_acq=4, apod="hann")),
+}
+
+
+def reference_single_frames() -> dict:
+    from oracle import ref
+    from us_lab4a_gb300 import synth
+    from us_lab4a_gb300.config import element_positions_matrix
+    from us_lab4a_gb300.workloads import grid_xyz3
+    fs, c, fc, ns = 40e6, 1540.0, 5e6, 400
+    nx, ny, pitch_x, pitch_y = SINGLE_ARRAY
+    el = element_positions_matrix(pitch_x, nx, 0.0, pitch_y, ny, 0.0, np.float32)
+    grid = grid_xyz3(-2e-3, 2e-3, 5, -1e-3, 1e-3, 3, 3e-3, 7e-3, 32).astype(np.float32).reshape(15, 32, 3)
+    out = {}
+    for i, (name, (mode, p)) in enumerate(sorted(SINGLE_CASES.items())):
+        rng = np.random.default_rng(2000 + i)
+        scat = synth.point_scatterers(rng, 6, (-2e-3, 2e-3), (3.5e-3, 6.5e-3), y_range=(-1e-3, 1e-3))
+        kw = dict(grid_xyz=grid, matrix=SINGLE_ARRAY, num_samples=ns, upsampling=p["upsampling"], fs=fs, c=c, fc=fc,
+                  peak_offset=p.get("peak_offset", 0.0), dead_zone_m=p.get("dead_zone_m", 0.0), cf=p["cf"],
+                  pcf_gamma=p.get("pcf_gamma", 1.0), dtype=np.float32)
+        meta = dict(mode=mode, num_samples=ns, upsampling=p["upsampling"], fs=fs, c=c, fc=fc,
+                    peak_offset=kw["peak_offset"], dead_zone_m=kw["dead_zone_m"], cf=p["cf"],
+                    pcf_gamma=kw["pcf_gamma"], grid=grid)
+        if mode == 0:
+            act = np.asarray(p["active"], np.uint32)
+            full = synth.synth_rf_numpy(el[act], el[act], scat, fs, c, fc, ns, rng)
+            rf = np.stack([full[k, k] for k in range(act.size)]).astype(np.float16).astype(np.float32)
+            v, f, _ = ref.single(mode=0, rf=rf, active=act, **kw)
+            meta.update(tx_xy=el[act], rx_xy=el[act], active=act)
+        else:
+            b, n = p["base_element"], p["num_elements"]
+            grp = el[b:b + n]
+            focus = (float(np.float32(grp[:, 0].mean())), float(np.float32(grp[:, 1].mean())), p["focus_z"])
+            apod = (np.hanning(n + 2)[1:-1] if p.get("apod") == "hann" else np.ones(n)).astype(np.float32)
+            src = np.array([[focus[0], focus[1]]])
+            if mode == 1:
+                rf = synth.synth_rf_numpy(src, grp, scat, fs, c, fc, ns, rng)[0]
+                rf = rf.astype(np.float16).astype(np.float32)
+                v, f, txd = ref.single(mode=1, rf=rf, base_element=b, num_elements=n, rx_apod=apod, focus=focus, **kw)
+            else:
+                ys = np.asarray(SINGLE_ACQ_Y, np.float32)
+                rf = np.stack([synth.synth_rf_numpy(src, grp + np.array([0.0, y], np.float32), scat, fs, c, fc, ns, rng)[0]
+                               for y in ys]).astype(np.float16).astype(np.float32)
+                v, f, txd = ref.single(mode=2, rf=rf, base_element=b, num_elements=n, rx_apod=apod, focus=focus,
+                                       acq_y=ys, first_acq=p["first_acq"], last_acq=p["last_acq"], **kw)
+                meta.update(acq_y=ys, first_acq=p["first_acq"], last_acq=p["last_acq"])
+            meta.update(tx_xy=grp, rx_xy=grp, rx_apod=apod, focus=np.asarray(focus, np.float32), tx_delays=txd,
+                        base_element=b)
+        meta.update(rf=rf.astype(np.float16), value=v, factor=f)
+        for k, x in meta.items():
+            out[name + "/" + k] = np.asarray(x)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
+    ap.add_argument("--single-only", action="store_true", help="rewrite reference_single.npz only")
     args = ap.parse_args()
+    if args.single_only:
+        from oracle import ref
+        if not ref.available():
+            ref.build()
+        np.savez_compressed(os.path.join(HERE, "reference_single.npz"), **reference_single_frames())
+        print("reference_single.npz", os.path.getsize(os.path.join(HERE, "reference_single.npz")))
+        return
     vec = reference_vectors(os.path.join(args.reference, "test"))
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     if args.vectors_only:
@@ -160,7 +241,8 @@ def main():
         ref.build()
     frames = reference_frames()
     np.savez_compressed(os.path.join(HERE, "reference_frames.npz"), **frames)
-    for f in ("reference_vectors.npz", "reference_frames.npz"):
+    np.savez_compressed(os.path.join(HERE, "reference_single.npz"), **reference_single_frames())
+    for f in ("reference_vectors.npz", "reference_frames.npz", "reference_single.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 

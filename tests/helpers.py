@@ -55,3 +55,27 @@ def db_err(a, b) -> float:
     """Peak-relative error in dB: 20 log10(max |a - b| / max |b|)."""
     e = rel_err(a, b)
     return -np.inf if e == 0 else 20.0 * np.log10(e)
+
+
+SINGLE_CASE_NAMES = ("synthy_all", "synthy_window_pcf", "t1r1_pcf", "t1r1_plain", "tnrn_diverging", "tnrn_focused_pcf")
+
+
+def single_case(oracle_lib, d, name):
+    """(SingleSpec, rf (acquisitions of the window) float32, grid) of one case
+    of reference_single.npz."""
+    g = lambda k: d[name + "/" + k]
+    mode = int(g("mode"))
+    rf = g("rf").astype(np.float32)
+    kw = {}
+    if mode != 0:
+        kw = dict(rx_apod=g("rx_apod"), focus=tuple(float(x) for x in g("focus")), first_tx_delay=float(g("tx_delays")[0]))
+    if mode == 2:
+        a, b = int(g("first_acq")), int(g("last_acq"))
+        kw["acq_y"] = g("acq_y")[a:b + 1]
+        rf = rf[a:b + 1]
+    spec = oracle_lib.SingleSpec(mode=mode, tx_xy=g("tx_xy"), rx_xy=g("rx_xy"), num_samples=int(g("num_samples")),
+                                 upsampling=int(g("upsampling")), sampling_frequency=float(g("fs")),
+                                 propagation_speed=float(g("c")), center_frequency=float(g("fc")),
+                                 peak_offset=float(g("peak_offset")), dead_zone_m=float(g("dead_zone_m")),
+                                 cf=int(g("cf")), pcf_gamma=float(g("pcf_gamma")), **kw)
+    return spec, rf, g("grid")

@@ -175,3 +175,33 @@ def test_oracle_against_compiled_reference_extra_cases(oracle_lib):
         v, f, _ = oracle_lib.process(spec, rf, fr.grid_xyz, dtype=np.float32)
         assert np.abs(v - vr).max() <= 1e-5 * np.abs(vr).max()
         assert np.abs(f - fref).max() <= 1e-4
+
+
+@pytest.mark.parametrize("name", ["synthy_all", "synthy_window_pcf", "t1r1_pcf", "t1r1_plain", "tnrn_diverging",
+                                  "tnrn_focused_pcf"])
+def test_single_term_oracle_matches_reference_processor(oracle_lib, golden_single, name):
+    """The FP32 oracle of the single-term 3D processors reproduces the outputs
+    of Vectorial3DT1R1SAFTProcessor / Vectorial3DTnRnProcessor /
+    SynthYVectorial3DTnRnProcessor<float> (compiled from the reference's
+    sources) within 1e-5 of the image maximum and the coherence factor within
+    1e-4; grid points whose every term falls outside the signal are exactly 0
+    on both sides."""
+    from helpers import single_case
+    spec, rf, grid = single_case(oracle_lib, golden_single, name)
+    v, f, _ = oracle_lib.single(spec, rf, grid, dtype=np.float32)
+    vr, fr = golden_single[name + "/value"], golden_single[name + "/factor"]
+    assert np.abs(vr).max() > 0
+    assert np.abs(v - vr).max() <= 1e-5 * np.abs(vr).max()
+    assert np.abs(f - fr).max() <= 1e-4
+    assert np.array_equal(v == 0, vr == 0)
+
+
+def test_single_term_tx_focus_delays_match_reference(golden_single):
+    """ArrayUtil::calculateTx3DFocusDelay restated on the host (focused and
+    diverging) gives the reference's delays bit for bit."""
+    from us_lab4a_gb300.config import tx_3d_focus_delay
+    for name in ("tnrn_focused_pcf", "tnrn_diverging", "synthy_all"):
+        g = lambda k: golden_single[name + "/" + k]
+        fx, fy, fz = (float(x) for x in g("focus"))
+        got = tx_3d_focus_delay(fx, fy, fz, float(g("c")), g("tx_xy"))
+        assert np.array_equal(got, g("tx_delays").astype(np.float32)), name

@@ -5,6 +5,8 @@ this library unchanged:
   ParameterMap                         src/util/ParameterMap.h:30-120 (key = value files, range checks)
   STAConfiguration                     src/user/configuration/STAConfiguration.h:29-75
   SA3DConfiguration                    src/user/configuration/SA3DConfiguration.h:33-135
+  TnRnConfiguration                    src/user/configuration/TnRnConfiguration.h:32-81
+  ArrayUtil::calculateTx3DFocusDelay   src/util/ArrayUtil.h:100-144
   ArrayGeometry::getElementXCentered2D src/util/ArrayGeometry.h:37-49
   ArrayUtil::calculateElementPositions src/util/ArrayUtil.h:51-70
   WindowFunction::get                  src/util/WindowFunction.h:237-289
@@ -247,6 +249,71 @@ class SA3DConfiguration:
             dead_zone_m=sa_pm.value("dead_zone_m", float, 0.0, 50.0e-3),
             num_elements_mux=mux,
         )
+
+
+@dataclass
+class TnRnConfiguration:
+    """Imaging with every element of the active group in transmission and
+    reception (one medium): group size, element positions of the whole array."""
+    num_elements: int
+    tx_elem_pos: np.ndarray          # (n, 2)
+    rx_elem_pos: np.ndarray          # (n, 2)
+    center_frequency: float
+    sampling_frequency: float
+    propagation_speed: float
+    dead_zone_m: float = 0.0
+    num_elements_mux: int = 1024
+    max_frequency: Optional[float] = None
+    value_scale: float = 1.0
+
+    @classmethod
+    def from_parameter_maps(cls, img_pm: ParameterMap, array_pm: ParameterMap, dtype=np.float32) -> "TnRnConfiguration":
+        def pos(prefix):
+            return element_positions_matrix(
+                array_pm.value(prefix + "_pitch_x", float, 1.0e-6, 1000.0),
+                int(array_pm.value(prefix + "_num_elem_x", float, 1, 1024)),
+                array_pm.value(prefix + "_offset_x", float, -1000.0, 1000.0),
+                array_pm.value(prefix + "_pitch_y", float, 1.0e-6, 1000.0),
+                int(array_pm.value(prefix + "_num_elem_y", float, 1, 1024)),
+                array_pm.value(prefix + "_offset_y", float, -1000.0, 1000.0), dtype)
+        tx, rx = pos("tx"), pos("rx")
+        mux = img_pm.value("num_elements_mux", int, 1, 1024)
+        if tx.shape[0] > mux or rx.shape[0] > mux:
+            raise InvalidParameterException("Error: numElementsMux is less than the number of array elements.")
+        return cls(
+            num_elements=img_pm.value("num_elements", int, 1, mux),
+            tx_elem_pos=tx, rx_elem_pos=rx,
+            center_frequency=img_pm.value("center_frequency", float, 100.0, 100.0e6),
+            sampling_frequency=img_pm.value("sampling_frequency", float, 100.0, 200.0e6),
+            propagation_speed=img_pm.value("propagation_speed_1", float, 100.0, 10000.0),
+            dead_zone_m=img_pm.value("dead_zone_m", float, 0.0, 50.0e-3),
+            num_elements_mux=mux,
+        )
+
+
+def tx_3d_focus_delay(focus_x: float, focus_y: float, focus_z: float, propagation_speed: float,
+                      elem_pos: np.ndarray, base_element: int = 0, num_group_elements: Optional[int] = None,
+                      dtype=np.float32) -> np.ndarray:
+    """Transmit delays (s) of the group elements for a focus (focus_z > 0) or
+    a virtual source behind the array (focus_z <= 0): the element farthest
+    from the focus fires first (delay 0), resp. the nearest one; evaluated in
+    `dtype` in the reference's order (distance3DZ0(pos, focus) * (1 / c))."""
+    t = np.dtype(dtype).type
+    pos = np.asarray(elem_pos, dtype)
+    n = pos.shape[0] - base_element if num_group_elements is None else int(num_group_elements)
+    if base_element + n > pos.shape[0]:
+        raise InvalidParameterException(
+            f"Error: baseElement + numGroupElements > elemPos.size() ( baseElement={base_element} "
+            f"numGroupElements={n} elemPos.size()={pos.shape[0]}).")
+    grp = pos[base_element:base_element + n]
+    inv_c = t(t(1) / t(propagation_speed))
+    dx = t(focus_x) - grp[:, 0]
+    dy = t(focus_y) - grp[:, 1]
+    fz = t(focus_z)
+    dt = np.sqrt(dx * dx + dy * dy + fz * fz).astype(dtype) * inv_c
+    if focus_z > 0.0:
+        return (max(t(0), dt.max()) - dt).astype(dtype)
+    return (dt - dt.min()).astype(dtype)
 
 
 # ---------------------------------------------------------------------------
