@@ -270,6 +270,96 @@ int usgb_batch_set_das_variant(usgb_batch* batch, int variant);
 int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
 int usgb_batch_synchronize(usgb_batch* batch);
 
+/*
+ * Single-term 3D processors: one prepared A-scan per term, so each grid point
+ * sums one linearly interpolated sample per signal (per signal and
+ * acquisition for the synthetic-y array) instead of one per tx x rx pair.
+ * Drop-in for
+ *   Vectorial3DT1R1SAFTProcessor<float>    src/user/processor/Vectorial3DT1R1SAFTProcessor.h:51-236
+ *     (prepare/process :120-236; delays :200-220)
+ *   Vectorial3DTnRnProcessor<float>        src/user/processor/Vectorial3DTnRnProcessor.h:51-282
+ *     (setTxDelays :137-146, prepare :148-161, process :163-282)
+ *   SynthYVectorial3DTnRnProcessor<float>  src/user/processor/SynthYVectorial3DTnRnProcessor.h:51-305
+ *     (getAcqData :169-205, process(firstAcq, lastAcq, grid) :207-305)
+ * The signals go through the same preparation as the STA processors
+ * (upsampling, DC removal, analytic signal); value = |sum of terms| /
+ * num_signals (times 1 / number of acquisitions of the window for the
+ * synthetic-y array) and factor = the coherence factor over all terms.
+ */
+typedef enum usgb_single_mode {
+	USGB_SINGLE_T1R1_SAFT = 0,    /* per-signal tx and rx element: delay = offset + |tx - p| / c + |rx - p| / c */
+	USGB_SINGLE_TNRN = 1,         /* one focused or diverging transmit (virtual source), rx apodization */
+	USGB_SINGLE_SYNTH_Y_TNRN = 2  /* TnRn acquisitions at several y positions, summed as one array in y */
+} usgb_single_mode;
+
+/* Mirrors the constructor arguments (config, acquisition, upsamplingFactor,
+ * coherenceFactor, peakOffset[, rxApod]) with SA3DConfiguration /
+ * TnRnConfiguration's fields (src/user/configuration/SA3DConfiguration.h:37-57,
+ * TnRnConfiguration.h:34-53). */
+typedef struct usgb_single_params {
+	uint32_t mode;              /* usgb_single_mode */
+	uint32_t num_signals;       /* T1R1: active elements (activeTxElem.size() == activeRxElem.size()); TnRn: numElements */
+	uint32_t num_samples;       /* samples per A-scan at sampling_frequency */
+	uint32_t upsampling;        /* 1..64 */
+	float sampling_frequency;   /* Hz */
+	float propagation_speed;    /* m/s */
+	float center_frequency;     /* Hz */
+	float peak_offset;          /* periods of center_frequency */
+	float dead_zone_m;          /* m */
+	/* host (x, y) pairs, m. T1R1: num_signals pairs, txElemPos[base + activeTxElem[i]].
+	 * TnRn: at least one pair; pair 0 = txElemPos[baseElement], the first element of the group. */
+	const float* tx_xy;
+	/* host, num_signals (x, y) pairs: T1R1 rxElemPos[base + activeRxElem[i]]; TnRn rxElemPos[baseElement + i]. */
+	const float* rx_xy;
+	/* host, num_signals weights. TnRn: required (the reference rejects a list of
+	 * the wrong size); T1R1: must be NULL (no apodization). */
+	const float* rx_apod;
+	uint32_t coherence;         /* usgb_coherence (USGB_CF_NONE / PCF / SCF on Re / MF) */
+	float pcf_gamma;
+	float scf_p;
+	uint32_t storage;           /* usgb_storage of the prepared signals */
+	float storage_scale;        /* samples are multiplied by this before FP16/BF16 storage; 0 = 1 */
+	uint32_t max_acquisitions;  /* synthetic y: acquisitions kept on the device (a ring); others: 0 or 1 */
+} usgb_single_params;
+
+typedef struct usgb_single usgb_single;
+int usgb_single_create(const usgb_single_params* params, usgb_single** single);
+void usgb_single_destroy(usgb_single* single);
+const char* usgb_single_last_error(const usgb_single* single);  /* NULL: last failed create on this thread */
+int usgb_single_set_stream(usgb_single* single, void* cuda_stream);
+
+/* setTxDelays(focusX, focusY, focusZ, txDelays): the focus (focus_z <= 0: a
+ * virtual source behind the array) and the group's transmit delays in s
+ * (ArrayUtil::calculateTx3DFocusDelay, src/util/ArrayUtil.h:100-144); only
+ * tx_delays[0] enters the image. TnRn modes; processing without it is
+ * USGB_ERR_INVALID_STATE ("Empty tx delay list."), as the reference's prepare. */
+int usgb_single_set_tx_delays(usgb_single* single, float focus_x, float focus_y, float focus_z,
+		const float* tx_delays, uint32_t count);
+
+/* Grid, column-major as in usgb_set_grid (host or device pointer). */
+int usgb_single_set_grid(usgb_single* single, const float* xyz, uint32_t ncols, uint32_t nrows);
+int usgb_single_set_grid_device(usgb_single* single, const float* d_xyz, uint32_t ncols, uint32_t nrows);
+
+/* T1R1 / TnRn: forms the image of one acquisition, rf = num_signals rows of
+ * num_samples (host; synchronous) or d_rf (device; asynchronous on the stream). */
+int usgb_single_process(usgb_single* single, const float* rf, float* value, float* factor);
+int usgb_single_process_device(usgb_single* single, const float* d_rf, float* d_value, float* d_factor);
+
+/* Synthetic y. usgb_single_add_acquisition(_device) prepares one acquisition
+ * (num_signals rows of num_samples) taken at `y` and appends it as number
+ * count++ (getAcqData(y)); the device keeps the last max_acquisitions.
+ * usgb_single_process_window(_device) forms the image of acquisitions
+ * first_acq..last_acq (process(firstAcq, lastAcq, gridData)): the grid's y is
+ * taken relative to the y of acquisition (first_acq + last_acq) / 2, which the
+ * reference then writes into every grid point's y. */
+int usgb_single_add_acquisition(usgb_single* single, const float* rf, float y);
+int usgb_single_add_acquisition_device(usgb_single* single, const float* d_rf, float y);
+int usgb_single_num_acquisitions(const usgb_single* single, uint32_t* count);
+int usgb_single_process_window(usgb_single* single, uint32_t first_acq, uint32_t last_acq, float* value, float* factor);
+int usgb_single_process_window_device(usgb_single* single, uint32_t first_acq, uint32_t last_acq, float* d_value,
+		float* d_factor);
+int usgb_single_synchronize(usgb_single* single);
+
 /* Library version string. */
 const char* usgb_version(void);
 

@@ -104,3 +104,90 @@ def test_python_exceptions_map_status(lib):
     fr.spec.dead_zone_m = 1.0
     with pytest.raises(InvalidValueException, match="Invalid dead zone"):
         StaEngine(fr.spec)
+
+
+def _single_params(**kw):
+    from us_lab4a_gb300 import native
+    from us_lab4a_gb300.config import element_positions_matrix
+    el = element_positions_matrix(0.3e-3, 4, 0.0, 0.3e-3, 4, 0.0, np.float32)
+    apod = np.ones(16, np.float32)
+    keep = {"el": el, "apod": apod}
+    p = native.SingleParams()
+    p.mode = native.USGB_SINGLE_TNRN
+    p.num_signals, p.num_samples, p.upsampling = 16, 256, 4
+    p.sampling_frequency, p.propagation_speed, p.center_frequency = 40e6, 1540.0, 5e6
+    p.tx_xy = p.rx_xy = el.ctypes.data_as(C.POINTER(C.c_float))
+    p.rx_apod = apod.ctypes.data_as(C.POINTER(C.c_float))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, keep
+
+
+@pytest.mark.parametrize("field,value,status,msg", [
+    ("mode", 3, 1, "Invalid processor mode"),
+    ("num_signals", 0, 1, "number of elements is zero"),
+    ("num_signals", 1025, 1, "More than 1024 elements"),
+    ("num_samples", 0, 1, "number of samples is zero"),
+    ("upsampling", 65, 2, "Invalid upsampling factor"),
+    ("dead_zone_m", 0.1, 2, "Invalid dead zone: deadZoneSamplesUp_"),
+    ("coherence", 9, 1, "Invalid coherence factor"),
+    ("pcf_gamma", -1.0, 2, "Invalid phase_coherence_factor_gamma"),
+    ("storage", 7, 1, "Invalid storage"),
+    ("max_acquisitions", 4, 1, "Only the synthetic-y array"),
+    ("rx_apod", None, 2, "Wrong rx apodization size: 0 (should be 16)"),
+])
+def test_single_create_rejects_invalid_frames(lib, field, value, status, msg):
+    """usgb_single_create checks the frame on the host with the reference's
+    messages (Vectorial3DTnRnProcessor.h:131-134, :182-186) before any device work."""
+    if field == "rx_apod":
+        p, keep = _single_params()
+        p.rx_apod = C.cast(None, C.POINTER(C.c_float))
+    else:
+        p, keep = _single_params(**{field: value})
+    if field == "pcf_gamma":
+        p.coherence = 1
+    h = C.c_void_p()
+    rc = lib.usgb_single_create(C.byref(p), C.byref(h))
+    assert rc == status
+    assert msg in lib.usgb_single_last_error(None).decode()
+    assert not h.value
+
+
+def test_single_t1r1_rejects_apodization_and_synthy_needs_a_ring(lib):
+    from us_lab4a_gb300 import native
+    p, keep = _single_params(mode=native.USGB_SINGLE_T1R1_SAFT)
+    h = C.c_void_p()
+    assert lib.usgb_single_create(C.byref(p), C.byref(h)) == 1
+    assert b"no rx apodization" in lib.usgb_single_last_error(None)
+    p, keep = _single_params(mode=native.USGB_SINGLE_SYNTH_Y_TNRN, max_acquisitions=0)
+    assert lib.usgb_single_create(C.byref(p), C.byref(h)) == 1
+    assert b"max_acquisitions" in lib.usgb_single_last_error(None)
+
+
+def test_single_processor_mirrors_reference_checks():
+    """Constructor and prepare() checks of the TnRn processors, raised before
+    any device work (Vectorial3DTnRnProcessor.h:131-134, 152-157)."""
+    from us_lab4a_gb300 import (AnalyticSignalCoherenceFactorProcessor, InvalidParameterException,
+                                InvalidStateException, InvalidValueException, TnRnConfiguration,
+                                Vectorial3DTnRnGB300Processor)
+    from us_lab4a_gb300.config import element_positions_matrix
+    el = element_positions_matrix(0.3e-3, 4, 0.0, 0.3e-3, 4, 0.0, np.float32)
+    cfg = TnRnConfiguration(num_elements=8, tx_elem_pos=el, rx_elem_pos=el, center_frequency=5e6,
+                            sampling_frequency=40e6, propagation_speed=1540.0, num_elements_mux=16)
+    cf = AnalyticSignalCoherenceFactorProcessor(method="none")
+
+    class Acq:
+        def prepare(self, base, delays):
+            pass
+
+        def execute(self):
+            return np.zeros((8, 64), np.float32)
+
+    with pytest.raises(InvalidValueException, match="Wrong rx apodization size: 7"):
+        Vectorial3DTnRnGB300Processor(cfg, Acq(), 4, cf, 0.0, np.ones(7))
+    proc = Vectorial3DTnRnGB300Processor(cfg, Acq(), 4, cf, 0.0, np.ones(8))
+    with pytest.raises(InvalidStateException, match="Empty tx delay list"):
+        proc.prepare(0)
+    proc.set_tx_delays(0.0, 0.0, 0.01, np.zeros(8))
+    with pytest.raises(InvalidParameterException, match="Invalid base element: 9"):
+        proc.prepare(9)

@@ -17,7 +17,8 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libusgb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["usgb_api.cu", "usgb_prep.cu", "usgb_das.cu", "usgb_das_staged.cu", "usgb_das_group.cu",
-           "usgb_das_group_f32.cu", "usgb_das_group_f16.cu", "usgb_das_group_bf16.cu", "usgb_post.cu", "usgb_noalloc.cu"]
+           "usgb_das_group_f32.cu", "usgb_das_group_f16.cu", "usgb_das_group_bf16.cu", "usgb_post.cu", "usgb_noalloc.cu",
+           "usgb_single.cu"]
 
 
 def nvcc() -> str:

@@ -1,5 +1,6 @@
-// Per-grid-point coherence-factor state over the receivers, shared by the
-// delay-and-sum kernels.
+// Per-grid-point coherence-factor state over the terms (per-receiver sums of
+// the STA kernels, single terms of the T1R1 / TnRn kernel), shared by the
+// delay-and-sum kernels. P is any parameter block with pcfFactor and scfP.
 #pragma once
 
 #include "usgb_common.cuh"
@@ -27,7 +28,7 @@ __device__ __forceinline__ float magnitude(float2 v)
 
 template<int CF> struct CFState {
 	__device__ void add(float2) {}
-	__device__ float result(unsigned, const DasParams&, float2) const { return 1.0f; }
+	template<class P> __device__ float result(unsigned, const P&, float2) const { return 1.0f; }
 };
 
 // PCF (src/util/CoherenceFactor.h:267-286): population standard deviation of
@@ -49,7 +50,7 @@ template<> struct CFState<CF_PCF> {
 		m2 = __fmaf_rn(d, inv, m2);
 		s2 = __fmaf_rn(d, __fsub_rn(aux, m2), s2);
 	}
-	__device__ float result(unsigned N, const DasParams& p, float2) const
+	template<class P> __device__ float result(unsigned N, const P& p, float2) const
 	{
 		const float sd1 = __fsqrt_rn(__fdiv_rn(s1, static_cast<float>(N)));
 		const float sd2 = __fsqrt_rn(__fdiv_rn(s2, static_cast<float>(N)));
@@ -61,7 +62,7 @@ template<> struct CFState<CF_PCF> {
 template<> struct CFState<CF_SCF> {
 	int signSum = 0;
 	__device__ void add(float2 v) { signSum += (v.x >= 0.f) ? 1 : -1; }
-	__device__ float result(unsigned N, const DasParams& p, float2) const
+	template<class P> __device__ float result(unsigned N, const P& p, float2) const
 	{
 		const float k = __fdiv_rn(static_cast<float>(signSum), static_cast<float>(N));
 		const float m = __fsub_rn(1.f, __fsqrt_rn(__fsub_rn(1.f, __fmul_rn(k, k))));
@@ -73,7 +74,7 @@ template<> struct CFState<CF_SCF> {
 template<> struct CFState<CF_MF> {
 	float energy = 0.f;
 	__device__ void add(float2 v) { energy = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, energy)); }
-	__device__ float result(unsigned N, const DasParams&, float2 total) const
+	template<class P> __device__ float result(unsigned N, const P&, float2 total) const
 	{
 		if (energy == 0.f) return 0.f;
 		const float num = __fadd_rn(__fmul_rn(total.x, total.x), __fmul_rn(total.y, total.y));

@@ -18,6 +18,7 @@ USGB_PATH_ANALYTIC, USGB_PATH_REAL = 0, 1
 USGB_CF_NONE, USGB_CF_PCF, USGB_CF_SCF, USGB_CF_MF = 0, 1, 2, 3
 USGB_STORE_F32, USGB_STORE_F16, USGB_STORE_BF16 = 0, 1, 2
 USGB_DELAY_AUTO, USGB_DELAY_FP32, USGB_DELAY_FP64 = 0, 1, 2
+USGB_SINGLE_T1R1_SAFT, USGB_SINGLE_TNRN, USGB_SINGLE_SYNTH_Y_TNRN = 0, 1, 2
 
 _FP = C.POINTER(C.c_float)
 
@@ -32,6 +33,18 @@ class StaParams(C.Structure):
         ("tx_xy", _FP), ("rx_xy", _FP), ("rx_apod", _FP),
         ("coherence", C.c_uint32), ("pcf_gamma", C.c_float), ("scf_p", C.c_float),
         ("storage", C.c_uint32), ("storage_scale", C.c_float),
+    ]
+
+
+class SingleParams(C.Structure):
+    """Mirror of ``usgb_single_params``."""
+    _fields_ = [
+        ("mode", C.c_uint32), ("num_signals", C.c_uint32), ("num_samples", C.c_uint32), ("upsampling", C.c_uint32),
+        ("sampling_frequency", C.c_float), ("propagation_speed", C.c_float),
+        ("center_frequency", C.c_float), ("peak_offset", C.c_float), ("dead_zone_m", C.c_float),
+        ("tx_xy", _FP), ("rx_xy", _FP), ("rx_apod", _FP),
+        ("coherence", C.c_uint32), ("pcf_gamma", C.c_float), ("scf_p", C.c_float),
+        ("storage", C.c_uint32), ("storage_scale", C.c_float), ("max_acquisitions", C.c_uint32),
     ]
 
 
@@ -58,6 +71,21 @@ SIGNATURES = {
     "usgb_set_das_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
     "usgb_set_delay_precision": (C.c_int, [C.c_void_p, C.c_uint32]),
     "usgb_batch_set_das_variant": (C.c_int, [C.c_void_p, C.c_int]),
+    "usgb_single_create": (C.c_int, [C.POINTER(SingleParams), C.POINTER(C.c_void_p)]),
+    "usgb_single_destroy": (None, [C.c_void_p]),
+    "usgb_single_last_error": (C.c_char_p, [C.c_void_p]),
+    "usgb_single_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "usgb_single_set_tx_delays": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, _FP, C.c_uint32]),
+    "usgb_single_set_grid": (C.c_int, [C.c_void_p, _FP, C.c_uint32, C.c_uint32]),
+    "usgb_single_set_grid_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32]),
+    "usgb_single_process": (C.c_int, [C.c_void_p, _FP, _FP, _FP]),
+    "usgb_single_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "usgb_single_add_acquisition": (C.c_int, [C.c_void_p, _FP, C.c_float]),
+    "usgb_single_add_acquisition_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_float]),
+    "usgb_single_num_acquisitions": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32)]),
+    "usgb_single_process_window": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, _FP, _FP]),
+    "usgb_single_process_window_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "usgb_single_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_post_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
     "usgb_post_destroy": (None, [C.c_void_p]),
     "usgb_post_last_error": (C.c_char_p, [C.c_void_p]),
