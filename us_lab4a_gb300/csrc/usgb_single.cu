@@ -52,8 +52,9 @@ struct SingleParams {
 	const float2* txXY;          // T1R1: numSignals; TnRn: [0] = first element of the group
 	const float2* rxXY;          // numSignals
 	const float* apod;           // TnRn: numSignals
-	const float* grid;           // npix (x, y, z)
-	unsigned npix;
+	const float* grid;           // npix (x, y, z), point (col, row) at col * nrows + row
+	unsigned npix, ncols, nrows;
+	unsigned tileCols;           // grid columns across a warp (32, 8 or 1)
 	float fsUp;                  // fs * U
 	float invCT;                 // fs * U / c
 	float signalOffset;          // fs * U * peakOffset / fc
@@ -90,14 +91,64 @@ __device__ __forceinline__ float distance3d(float x0, float y0, float z0, float 
 	return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
 }
 
+// Phase coherence factor over single terms (src/util/CoherenceFactor.h:267-286:
+// population standard deviations of the phases phi and phi -+ pi). One
+// update per term, so the sums are kept shifted by the first term's phases
+// (sum d, sum d^2 with d = phi - phi_0), which needs no division per term and
+// keeps the cancellation of sum d^2 - (sum d)^2 / N small: the phases lie in
+// [-pi, pi], so for N terms the rounding of the sums moves the variance by
+// about sqrt(N) * 2^-24 * (2 pi)^2, below 1e-4 of the factor for N <= 2^16.
+struct SinglePcf {
+	unsigned n = 0;
+	float k1 = 0.f, k2 = 0.f, s1 = 0.f, q1 = 0.f, s2 = 0.f, q2 = 0.f;
+	__device__ __forceinline__ void add(float2 v)
+	{
+		const float phi = atan2f(v.y, v.x);
+		const float pi = 3.14159265358979323846f;
+		const float aux = phi + ((phi < 0.f) ? pi : -pi);
+		if (n == 0) {
+			k1 = phi;
+			k2 = aux;
+		}
+		++n;
+		const float d1 = __fsub_rn(phi, k1);
+		const float d2 = __fsub_rn(aux, k2);
+		s1 = __fadd_rn(s1, d1);
+		q1 = __fmaf_rn(d1, d1, q1);
+		s2 = __fadd_rn(s2, d2);
+		q2 = __fmaf_rn(d2, d2, q2);
+	}
+	template<class P> __device__ float result(unsigned N, const P& p, float2) const
+	{
+		const float invN = __frcp_rn(static_cast<float>(N));
+		const float m1 = __fmul_rn(s1, invN), m2 = __fmul_rn(s2, invN);
+		const float v1 = fmaxf(0.f, __fsub_rn(__fmul_rn(q1, invN), __fmul_rn(m1, m1)));
+		const float v2 = fmaxf(0.f, __fsub_rn(__fmul_rn(q2, invN), __fmul_rn(m2, m2)));
+		const float sd = fminf(__fsqrt_rn(v1), __fsqrt_rn(v2));
+		return fmaxf(0.f, __fsub_rn(1.f, __fmul_rn(p.pcfFactor, sd)));
+	}
+};
+
+template<int CF> struct SingleCF { using T = CFState<CF>; };
+template<> struct SingleCF<usgb::CF_PCF> { using T = SinglePcf; };
+
 // MODE 0: T1R1 with separate tx and rx positions; 1: T1R1 with every tx
 // position equal to its rx position (one distance per term); 2: TnRn.
+//
+// A warp covers tileCols neighbouring grid columns at 32 / tileCols
+// consecutive depths: the delays of neighbouring columns at one depth differ
+// by a few samples, so a warp's gathers of one signal fall into a few
+// sectors, where 32 consecutive depths would spread them over one sector
+// each (a depth step is tens of upsampled samples).
 template<int S, int CF, int MODE>
 __global__ void __launch_bounds__(kSingleThreads)
 das_single_kernel(const __grid_constant__ SingleParams p)
 {
-	const unsigned pix = blockIdx.x * blockDim.x + threadIdx.x;
-	if (pix >= p.npix) return;
+	const unsigned tileRows = kSingleThreads / p.tileCols;
+	const unsigned col = blockIdx.x * p.tileCols + threadIdx.x % p.tileCols;
+	const unsigned row = blockIdx.y * tileRows + threadIdx.x / p.tileCols;
+	if (col >= p.ncols || row >= p.nrows) return;
+	const unsigned pix = col * p.nrows + row;
 	using CT = typename Complex<S>::T;
 	const float px = p.grid[3 * pix];
 	const float py = p.grid[3 * pix + 1];
@@ -115,7 +166,7 @@ das_single_kernel(const __grid_constant__ SingleParams p)
 	}
 
 	float2 total = make_float2(0.f, 0.f);
-	CFState<CF> cf;
+	typename SingleCF<CF>::T cf;
 	for (unsigned a = 0; a < p.numAcq; ++a) {
 		unsigned slot = p.firstSlot + a;
 		if (slot >= p.numSlots) slot -= p.numSlots;
@@ -173,7 +224,8 @@ das_single_kernel(const __grid_constant__ SingleParams p)
 template<int S, int CF>
 cudaError_t launch_mode(const SingleParams& p, int mode, cudaStream_t st)
 {
-	const unsigned blocks = (p.npix + kSingleThreads - 1) / kSingleThreads;
+	const unsigned tileRows = kSingleThreads / p.tileCols;
+	const dim3 blocks((p.ncols + p.tileCols - 1) / p.tileCols, (p.nrows + tileRows - 1) / tileRows);
 	switch (mode) {
 	case 0: das_single_kernel<S, CF, 0><<<blocks, kSingleThreads, 0, st>>>(p); break;
 	case 1: das_single_kernel<S, CF, 1><<<blocks, kSingleThreads, 0, st>>>(p); break;
@@ -500,6 +552,15 @@ void run_das(usgb_single* c, uint64_t first, uint64_t last, float* d_value, floa
 	p.apod = c->d_apod;
 	p.grid = c->d_grid;
 	p.npix = c->npix;
+	p.ncols = c->ncols;
+	p.nrows = c->nrows;
+	p.tileCols = c->ncols >= 32 ? 32U : (c->ncols >= 8 ? 8U : 1U);
+	while (p.tileCols > 1 && (c->nrows + kSingleThreads / p.tileCols - 1) / (kSingleThreads / p.tileCols) > 65535U) {
+		p.tileCols = p.tileCols == 32 ? 8U : 1U;
+	}
+	if ((c->nrows + kSingleThreads - 1) / kSingleThreads > 65535U) {
+		SINGLE_FAIL(USGB_ERR_UNSUPPORTED, "Grids of more than " << 65535U * kSingleThreads << " rows are not supported.");
+	}
 	p.fsUp = c->fsUp;
 	p.invCT = c->invCT;
 	p.signalOffset = c->signalOffset;
