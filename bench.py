@@ -328,6 +328,11 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         mixed = run_mixed(dev)
 
+    single = None
+    if world == 1 and not args.no_single:
+        torch.cuda.empty_cache()
+        single = run_single(dev)
+
     if rank == 0:
         fps = world * args.steps / (total_ms * 1e-3)
         line = {
@@ -349,7 +354,7 @@ def run_gpu(args):
                          "algorithmic_bytes": top[2]},
             "das_gathers_per_s": gathers / (das_ms * 1e-3),
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
-            "mixed": mixed,
+            "mixed": mixed, "single": single,
         }
         print(json.dumps(line), flush=True)
     eng.close()
@@ -507,6 +512,124 @@ def run_serving(dev, frames, rfs, refs, small, das_config, rates=(50.0, 200.0, 2
     return out
 
 
+SINGLE_GRID = (96, 96, 192)   # x, y, z points over x, y in +-4 mm and z in 5-25 mm
+
+
+def _single_case(dev, name: str, storage: str, reps: int, threads: int):
+    """One single-term 3D workload: frames/s with the RF resident, terms/s,
+    error against the FP64 oracle on three grid columns, and the FP32 oracle
+    on those columns scaled to the frame (CPU baseline)."""
+    import oracle
+    import torch
+    from us_lab4a_gb300 import SingleEngine, native, synth
+    from us_lab4a_gb300.config import element_positions_matrix, tx_3d_focus_delay
+    from us_lab4a_gb300.workloads import grid_xyz3
+    fs, c, fc, ns, U = 40e6, 1540.0, 5e6, 2048, 4
+    nx = 16 if name == "synthy" else 32
+    el = element_positions_matrix(0.3e-3, nx, 0.0, 0.3e-3, nx, 0.0, np.float32)
+    n = el.shape[0]
+    gx, gy, gz = SINGLE_GRID
+    grid = grid_xyz3(-4e-3, 4e-3, gx, -4e-3, 4e-3, gy, 5e-3, 25e-3, gz).astype(np.float32).reshape(gx * gy, gz, 3)
+    rng = np.random.default_rng(2024)
+    scat = synth.point_scatterers(rng, 40, (-4e-3, 4e-3), (6e-3, 24e-3), y_range=(-4e-3, 4e-3))
+    nacq = 16 if name == "synthy" else 1
+    mode = {"t1r1": native.USGB_SINGLE_T1R1_SAFT, "tnrn": native.USGB_SINGLE_TNRN,
+            "synthy": native.USGB_SINGLE_SYNTH_Y_TNRN}[name]
+    focus = (0.0, 0.0, -10e-3)
+    if name == "t1r1":
+        rfs = [synth.synth_rf_pairs_torch(el, el, scat, fs, c, fc, ns, 5, device=dev)]
+        tx, apod, ys = el, None, [0.0]
+    else:
+        src = np.array([[focus[0], focus[1]]], np.float32)
+        ys = [0.2e-3 * (a - (nacq - 1) / 2) for a in range(nacq)]
+        rfs = [synth.synth_rf_torch(src, el + np.array([0.0, y], np.float32), scat, fs, c, fc, ns, 5 + a,
+                                    device=dev)[0] for a, y in enumerate(ys)]
+        tx, apod = el[:1], np.hanning(n + 2)[1:-1].astype(np.float32)
+    delays = tx_3d_focus_delay(*focus, c, el) if name != "t1r1" else None
+    eng = SingleEngine(mode, tx, el, ns, U, fs, c, fc, 1.5, 0.0, rx_apod=apod, coherence="pcf", pcf_gamma=1.0,
+                       storage=storage, max_acquisitions=nacq if name == "synthy" else 0)
+    if delays is not None:
+        eng.set_tx_delays(*focus, delays)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream)
+    eng.set_grid_device(torch.as_tensor(grid, device=dev))
+    value = torch.empty(grid.shape[:2], device=dev)
+    factor = torch.empty_like(value)
+
+    added = []  # RF index of every acquisition added, in order
+
+    def add(k):
+        eng.add_acquisition_device(rfs[k % nacq], ys[k % nacq])
+        added.append(k % nacq)
+
+    def frame(k):
+        if name == "synthy":
+            # A new acquisition arrives and the window of the last nacq is imaged.
+            add(k)
+            last = len(added) - 1
+            eng.process_window_device(last - nacq + 1, last, value, factor)
+        else:
+            eng.process_device(rfs[0], value, factor)
+
+    with torch.cuda.stream(stream):
+        if name == "synthy":
+            for k in range(nacq):
+                add(k)
+        for k in range(3):
+            frame(k)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(reps):
+            frame(k)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    order = added[-nacq:] if name == "synthy" else [0]   # RF of each acquisition of the last window
+    img = value.cpu().numpy()
+    eng.close()
+    cols = np.array([gx * gy // 2 + gy // 2, gx * gy // 3, 7 * gx * gy // 8])
+    pts = grid[cols]
+    rf_host = np.stack([rfs[a].cpu().numpy() for a in order])
+    kw = dict(tx_xy=tx, rx_xy=el, num_samples=ns, upsampling=U, sampling_frequency=fs, propagation_speed=c,
+              center_frequency=fc, peak_offset=1.5, rx_apod=apod, cf=1, pcf_gamma=1.0, nthreads=threads)
+    if name != "t1r1":
+        kw.update(focus=focus, first_tx_delay=float(delays[0]))
+    if name == "synthy":
+        kw["acq_y"] = np.asarray([ys[a] for a in order], np.float32)
+    spec = oracle.SingleSpec(mode=mode, **kw)
+    v64, _, _ = oracle.single(spec, rf_host, pts, dtype=np.float64)
+    err_db = _db(float(np.abs(img[cols] - v64).max()), float(np.abs(v64).max()))
+    t0 = time.perf_counter()
+    oracle.single(spec, rf_host, pts[:, :1], dtype=np.float32)        # preparation (+ 3 points)
+    t_prep = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.single(spec, rf_host, pts, dtype=np.float32)
+    t_das = max(time.perf_counter() - t0 - t_prep, 1e-9) / (pts.shape[0] * (pts.shape[1] - 1))
+    npix = grid.shape[0] * grid.shape[1]
+    # One frame of the CPU form prepares one acquisition and images the window.
+    cpu_frame = t_prep / nacq + t_das * npix
+    terms = npix * n * nacq
+    return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "terms_per_s": terms / (ms * 1e-3),
+            "err_db_vs_fp64": err_db,
+            "cpu_oracle": {"frames_per_s": 1.0 / cpu_frame, "cores": threads, "kind": "port",
+                           "sample": f"FP32 oracle: preparation of {n * nacq} A-scans and {pts.shape[0] * pts.shape[1]}"
+                                     f" grid points, scaled to {npix} points"}}
+
+
+def run_single(dev, reps: int = 20):
+    """The single-term 3D processors (T1R1 SAFT, TnRn, synthetic-y TnRn), PCF."""
+    threads = os.cpu_count() or 1
+    out = {"workload": ("T1R1 SAFT and TnRn (diverging, focus z = -10 mm): 32 x 32 matrix array (1024 elements); "
+                        "synthetic y: 16 x 16 array, window of 16 acquisitions 0.2 mm apart in y; 2048 samples "
+                        f"@40 MHz, 4x, PCF, grid {SINGLE_GRID[0]}x{SINGLE_GRID[1]}x{SINGLE_GRID[2]}; RF resident; "
+                        "the prepared signals (<= 67 MB) stay in L2 between preparation and delay-and-sum")}
+    for name in ("t1r1", "tnrn", "synthy"):
+        for storage in ("f32", "f16"):
+            out[f"{name}_{storage}"] = _single_case(dev, name, storage, reps, threads)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -524,6 +647,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the 48-frame mixed-size / serving section")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-term 3D processor section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

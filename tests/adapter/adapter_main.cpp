@@ -1,6 +1,8 @@
-// Compiles the drop-in processors of include/usgb_sta_processor.hpp inside the
-// reference's own headers and runs them through the reference's plugin
-// interface (ArrayProcessor::prepare/process). Prints one line per case.
+// Compiles the drop-in processors of include/usgb_sta_processor.hpp and
+// include/usgb_single_processor.hpp inside the reference's own headers and
+// runs them through the reference's plugin interface
+// (ArrayProcessor::prepare/process, setTxDelays, getAcqData). Prints one line
+// per case.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -13,8 +15,11 @@
 #include "SA3DConfiguration.h"
 #include "STAAcquisition.h"
 #include "STAConfiguration.h"
+#include "TnRnAcquisition.h"
+#include "TnRnConfiguration.h"
 #include "Util.h"
 #include "XYZValueFactor.h"
+#include "usgb_single_processor.hpp"
 #include "usgb_sta_processor.hpp"
 
 using namespace Lab;
@@ -30,6 +35,49 @@ public:
 private:
 	unsigned nrx_, ns_;
 };
+
+class ZeroTnRnAcquisition : public TnRnAcquisition<float> {
+public:
+	ZeroTnRnAcquisition(unsigned n, unsigned ns) : n_(n), ns_(ns) {}
+	void execute(AcquisitionDataType& m) override
+	{
+		m.resize(n_, ns_);
+		for (auto& v : m) v = 0.0f;
+	}
+private:
+	unsigned n_, ns_;
+};
+
+static void matrix_positions(std::vector<XY<float>>& pos)
+{
+	ArrayUtil::calculateElementPositions(0.3e-3f, 4U, 0.0f, 0.3e-3f, 4U, 0.0f, pos);
+}
+
+static TnRnConfiguration<float> tnrn_config(float deadZone)
+{
+	TnRnConfiguration<float> c;
+	c.numElementsMux = 16;
+	c.numElements = 8;
+	c.numPulses = 1;
+	c.centerFrequency = 5e6f;
+	c.maxFrequency = 10e6f;
+	c.acquisitionTime = 1e-4f;
+	c.minGain = c.maxGain = 0;
+	c.propagationSpeed = 1540.0f;
+	c.acquisitionDelay = 0;
+	c.samplingFrequency = 40e6f;
+	c.deadZoneM = deadZone;
+	c.valueScale = 1;
+	matrix_positions(c.txElemPos);
+	matrix_positions(c.rxElemPos);
+	return c;
+}
+
+static void fill_grid(Matrix<XYZValueFactor<float>>& grid)
+{
+	for (unsigned i = 0; i < grid.n1(); ++i)
+		for (unsigned j = 0; j < grid.n2(); ++j) { grid(i, j).x = 1e-3f * i; grid(i, j).z = 5e-3f + 1e-3f * j; }
+}
 
 static STAConfiguration<float> config(float deadZone)
 {
@@ -92,6 +140,81 @@ int main()
 		float s = 0;
 		for (auto& pt : grid) s += pt.value;
 		std::printf("frame sum %g\n", s);
+	});
+	// Single-term 3D processors.
+	run_case("saft_frame", [&] {
+		SA3DConfiguration<float> c;
+		c.numElementsMux = 16;
+		c.numPulses = 1;
+		c.centerFrequency = 5e6f;
+		c.maxFrequency = 10e6f;
+		c.acquisitionTime = 1e-4f;
+		c.minGain = c.maxGain = 0;
+		c.propagationSpeed = 1540.0f;
+		c.acquisitionDelay = 0;
+		c.samplingFrequency = 40e6f;
+		c.deadZoneM = 0;
+		c.valueScale = 1;
+		matrix_positions(c.txElemPos);
+		matrix_positions(c.rxElemPos);
+		for (unsigned e = 0; e < 16; e += 2) {
+			c.activeTxElem.push_back(e);
+			c.activeRxElem.push_back(e);
+		}
+		ZeroAcquisition acq(1, 256);
+		Vectorial3DT1R1SAFTGB300Processor p(c, acq, 4, noCF, 0.0f);
+		Matrix<XYZValueFactor<float>> grid(4, 4);
+		fill_grid(grid);
+		p.prepare(0);
+		p.process(grid);
+	});
+	run_case("tnrn_apod", [&] {
+		auto c = tnrn_config(0.0f);
+		ZeroTnRnAcquisition acq(8, 256);
+		Vectorial3DTnRnGB300Processor p(c, acq, 4, noCF, 0.0f, std::vector<float>(7, 1.0f));
+	});
+	run_case("tnrn_no_delays", [&] {
+		auto c = tnrn_config(0.0f);
+		ZeroTnRnAcquisition acq(8, 256);
+		Vectorial3DTnRnGB300Processor p(c, acq, 4, noCF, 0.0f, apod);
+		p.prepare(0);
+	});
+	run_case("tnrn_dead_zone", [&] {
+		auto c = tnrn_config(0.05f);
+		ZeroTnRnAcquisition acq(8, 256);
+		Vectorial3DTnRnGB300Processor p(c, acq, 4, noCF, 0.0f, apod);
+		std::vector<float> delays;
+		ArrayUtil::calculateTx3DFocusDelay(0.0f, 0.0f, -5e-3f, c.propagationSpeed, c.txElemPos, 0U, 8U, delays);
+		p.setTxDelays(0.0f, 0.0f, -5e-3f, delays);
+		Matrix<XYZValueFactor<float>> grid(4, 4);
+		p.prepare(0);
+		p.process(grid);
+	});
+	run_case("tnrn_frame", [&] {
+		auto c = tnrn_config(0.0f);
+		ZeroTnRnAcquisition acq(8, 256);
+		Vectorial3DTnRnGB300Processor p(c, acq, 4, noCF, 0.0f, apod);
+		std::vector<float> delays;
+		ArrayUtil::calculateTx3DFocusDelay(0.0f, 0.0f, -5e-3f, c.propagationSpeed, c.txElemPos, 0U, 8U, delays);
+		p.setTxDelays(0.0f, 0.0f, -5e-3f, delays);
+		Matrix<XYZValueFactor<float>> grid(4, 4);
+		fill_grid(grid);
+		p.prepare(0);
+		p.process(grid);
+	});
+	run_case("synthy_frame", [&] {
+		auto c = tnrn_config(0.0f);
+		ZeroTnRnAcquisition acq(8, 256);
+		SynthYVectorial3DTnRnGB300Processor p(c, acq, 4, noCF, 0.0f, apod, 4);
+		std::vector<float> delays;
+		ArrayUtil::calculateTx3DFocusDelay(0.0f, 0.0f, -5e-3f, c.propagationSpeed, c.txElemPos, 0U, 8U, delays);
+		p.setTxDelays(0.0f, 0.0f, -5e-3f, delays);
+		p.prepare(0);
+		for (int a = 0; a < 3; ++a) p.getAcqData(1e-4f * a);
+		Matrix<XYZValueFactor<float>> grid(4, 4);
+		fill_grid(grid);
+		p.process(0, 2, grid);
+		if (grid(0, 0).y != 1e-4f) throw std::runtime_error("center y not written");
 	});
 	return 0;
 }

@@ -1,4 +1,5 @@
-"""The C++ drop-in processors (include/usgb_sta_processor.hpp) compile inside
+"""The C++ drop-in processors (include/usgb_sta_processor.hpp,
+include/usgb_single_processor.hpp) compile inside
 the reference's own headers, link libusgb.so, run through the reference's
 ArrayProcessor interface and rethrow library errors as the reference's
 exception types. Needs the reference sources (present where the fixtures are
@@ -34,9 +35,13 @@ def test_adapter_compiles_in_reference_tree_and_maps_errors(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120).stdout
     # Parameter checks run before any device work: the reference's exception type.
     assert "dead_zone InvalidValueException" in out and "Invalid dead zone" in out
+    assert "tnrn_apod InvalidValueException Wrong rx apodization size: 7 (should be 8)." in out
+    assert "tnrn_no_delays InvalidStateException Empty tx delay list." in out
+    assert "tnrn_dead_zone InvalidValueException" in out and "deadZoneSamplesUp_" in out
     import torch
-    if torch.cuda.is_available():
-        assert "frame ok" in out
-    else:
-        # No device here: the CUDA failure surfaces as Lab::Exception.
-        assert "frame Exception" in out
+    for case in ("frame", "saft_frame", "tnrn_frame", "synthy_frame"):
+        if torch.cuda.is_available():
+            assert f"\n{case} ok" in "\n" + out, out
+        else:
+            # No device here: the CUDA failure surfaces as Lab::Exception.
+            assert f"\n{case} Exception" in "\n" + out, out

@@ -126,3 +126,37 @@ def synth_rf_torch(tx_xy, rx_xy, scat: Scatterers, fs: float, c: float, fc: floa
         g.manual_seed(seed)
         rf += noise_std * torch.randn(rf.shape, generator=g, device=dev, dtype=torch.float32)
     return rf
+
+
+def synth_rf_pairs_torch(tx_xy, rx_xy, scat: Scatterers, fs: float, c: float, fc: float, num_samples: int,
+                         seed: int, noise_std: float = 0.01, bw: float = 0.6, device="cpu", chunk: int = 64):
+    """(n, num_samples) float32 RF of the n (tx_xy[i], rx_xy[i]) pairs (one
+    A-scan per pair: the T1R1 / SAFT acquisition when tx = rx), same echo
+    model as synth_rf_numpy."""
+    import torch
+    dev = torch.device(device)
+    tx = torch.as_tensor(np.asarray(tx_xy, np.float32), device=dev)
+    rx = torch.as_tensor(np.asarray(rx_xy, np.float32), device=dev)
+    n = tx.shape[0]
+    a = gauss_coefficient(fc, bw)
+    hw = _half_width(a, fs)
+    rf = torch.zeros(n * num_samples, dtype=torch.float32, device=dev)
+    offs = torch.arange(-hw, hw + 1, device=dev)
+    base = torch.arange(n, device=dev)[:, None, None] * num_samples
+    S = torch.as_tensor(np.stack([scat.x, scat.y, scat.z, scat.amp]).astype(np.float32), device=dev)
+    for s0 in range(0, len(scat), chunk):
+        sx, sy, sz, sa = S[:, s0:s0 + chunk]
+        dtx = torch.sqrt((sx[None] - tx[:, 0:1]) ** 2 + (sy[None] - tx[:, 1:2]) ** 2 + sz[None] ** 2)
+        drx = torch.sqrt((sx[None] - rx[:, 0:1]) ** 2 + (sy[None] - rx[:, 1:2]) ** 2 + sz[None] ** 2)
+        tau = (dtx + drx) / c                                            # (n, S)
+        nidx = torch.floor(tau * fs).to(torch.int64)[..., None] + offs   # (n, S, W)
+        t = nidx.to(torch.float32) / fs - tau[..., None]
+        v = sa[None, :, None] * torch.exp(-a * t * t) * torch.cos(2.0 * math.pi * fc * t)
+        ok = (nidx >= 0) & (nidx < num_samples)
+        rf.index_add_(0, (base + nidx)[ok], v[ok])
+    rf = rf.view(n, num_samples)
+    if noise_std > 0:
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        rf += noise_std * torch.randn(rf.shape, generator=g, device=dev, dtype=torch.float32)
+    return rf
