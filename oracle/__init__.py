@@ -9,4 +9,5 @@ from .oracle import (  # noqa: F401
     next_fast_even_size,
     kaiser_beta, kaiser_size,
     SingleSpec, single, SINGLE_T1R1_SAFT, SINGLE_TNRN, SINGLE_SYNTH_Y_TNRN,
+    TwoMediumSpec, two_medium,
 )

@@ -297,6 +297,74 @@ def single(spec: SingleSpec, rf: np.ndarray, grid_xyz: np.ndarray, dtype=np.floa
     return value[:npix].reshape(shape), factor[:npix].reshape(shape), sig
 
 
+def _two_medium_desc_type(ct):
+    class TwoMediumDesc(C.Structure):
+        _fields_ = [
+            ("num_elements", C.c_uint), ("num_elements_mux", C.c_uint),
+            ("pitch", ct), ("center_frequency", ct), ("propagation_speed_1", ct), ("propagation_speed_2", ct),
+            ("sampling_frequency", ct), ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("max_fermat_block_size", ct), ("peak_offset", ct), ("signal_start_offset", C.c_uint),
+            ("num_acq", C.c_uint), ("num_tx", C.c_uint), ("num_steps", C.c_uint), ("steps", C.POINTER(C.c_uint)),
+            ("num_interface", C.c_uint), ("interface_xz", C.POINTER(ct)), ("rx_apod", C.POINTER(ct)),
+            ("cf", C.c_int), ("pcf_gamma", ct), ("nthreads", C.c_int),
+        ]
+    return TwoMediumDesc
+
+
+_TwoMedium32 = _two_medium_desc_type(C.c_float)
+_TwoMedium64 = _two_medium_desc_type(C.c_double)
+
+
+@dataclass
+class TwoMediumSpec:
+    """TwoMediumSTAConfiguration fields plus the processor's constructor and
+    process() arguments (VectorialCombinedTwoMediumImagingProcessor).
+    steps: (n, 4) (baseElemIdx, baseElem, firstTxElem, lastTxElem);
+    interface_xz: (m, 2); rx_apod: (num_elements,)."""
+    num_elements: int
+    num_elements_mux: int
+    pitch: float
+    center_frequency: float
+    propagation_speed_1: float
+    propagation_speed_2: float
+    sampling_frequency: float
+    num_samples: int
+    upsampling: int
+    steps: np.ndarray
+    interface_xz: np.ndarray
+    rx_apod: np.ndarray
+    max_fermat_block_size: float = 2.0
+    peak_offset: float = 0.0
+    signal_start_offset: int = 0
+    cf: int = CF_NONE
+    pcf_gamma: float = 1.0
+    nthreads: int = field(default_factory=lambda: os.cpu_count() or 1)
+
+
+def two_medium(spec: TwoMediumSpec, rf: np.ndarray, grid_xz: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """rf: (num_acq, num_tx, num_elements, num_samples); grid_xz: (ncols, nrows, 2).
+    Returns the complex image (ncols, nrows)."""
+    desc_t, ct = (_TwoMedium32, C.c_float) if dtype == np.float32 else (_TwoMedium64, C.c_double)
+    lib = _lib()
+    f = getattr(lib, "orc_two_medium_" + ("f32" if dtype == np.float32 else "f64"))
+    p = C.POINTER(ct)
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(desc_t), p, p, C.c_uint, C.c_uint, p]
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    steps = np.ascontiguousarray(spec.steps, dtype=np.uint32).reshape(-1, 4)
+    ifxz = np.ascontiguousarray(spec.interface_xz, dtype=dtype).reshape(-1, 2)
+    apod = np.ascontiguousarray(spec.rx_apod, dtype=dtype)
+    d = desc_t(spec.num_elements, spec.num_elements_mux, spec.pitch, spec.center_frequency,
+               spec.propagation_speed_1, spec.propagation_speed_2, spec.sampling_frequency, spec.num_samples,
+               spec.upsampling, spec.max_fermat_block_size, spec.peak_offset, spec.signal_start_offset,
+               rf.shape[0], rf.shape[1], steps.shape[0], steps.ctypes.data_as(C.POINTER(C.c_uint)),
+               ifxz.shape[0], _ptr(ifxz, ct), _ptr(apod, ct), spec.cf, spec.pcf_gamma, int(spec.nthreads))
+    g = np.ascontiguousarray(grid_xz, dtype=dtype)
+    out = np.zeros(g.shape[0] * g.shape[1] * 2, dtype=dtype)
+    _err(f(C.byref(d), _ptr(rf, ct), _ptr(g, ct), g.shape[0], g.shape[1], _ptr(out, ct)))
+    return out.view(np.complex64 if dtype == np.float32 else np.complex128).reshape(g.shape[0], g.shape[1])
+
+
 def interp_taps(U: int, half_transition: float = 0.2, dtype=np.float64) -> np.ndarray:
     cap = 8192
     ct = C.c_float if dtype == np.float32 else C.c_double

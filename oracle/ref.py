@@ -173,3 +173,48 @@ def single(*, mode: int, rf: np.ndarray, grid_xyz: np.ndarray, matrix, num_sampl
     if rc != 0:
         raise RuntimeError(lib.ref_last_error().decode())
     return value, factor, txd[:num_elements]
+
+
+def _two_medium_desc(ct):
+    class RefTwoMediumDesc(C.Structure):
+        _fields_ = [
+            ("num_elements", C.c_uint), ("num_elements_mux", C.c_uint),
+            ("pitch", ct), ("center_frequency", ct), ("propagation_speed_1", ct), ("propagation_speed_2", ct),
+            ("sampling_frequency", ct), ("num_samples", C.c_uint), ("upsampling", C.c_uint),
+            ("max_fermat_block_size", ct), ("peak_offset", ct), ("signal_start_offset", C.c_uint),
+            ("num_acq", C.c_uint), ("num_tx", C.c_uint), ("num_steps", C.c_uint), ("steps", C.POINTER(C.c_uint)),
+            ("num_interface", C.c_uint), ("interface_xz", C.POINTER(ct)), ("rx_apod", C.POINTER(ct)),
+            ("cf", C.c_int), ("pcf_gamma", ct),
+        ]
+    return RefTwoMediumDesc
+
+
+_TM32, _TM64 = _two_medium_desc(C.c_float), _two_medium_desc(C.c_double)
+
+
+def two_medium(spec, rf: np.ndarray, grid_xz: np.ndarray, dtype=np.float32) -> np.ndarray:
+    """Run the reference's VectorialCombinedTwoMediumImagingProcessor on an
+    oracle.TwoMediumSpec; rf (num_acq, num_tx, num_elements, num_samples),
+    grid_xz (ncols, nrows, 2). Returns the complex image (ncols, nrows)."""
+    lib = _load()
+    ct = C.c_float if dtype == np.float32 else C.c_double
+    D = _TM32 if dtype == np.float32 else _TM64
+    f = lib.ref_two_medium_f32 if dtype == np.float32 else lib.ref_two_medium_f64
+    p = C.POINTER(ct)
+    f.argtypes = [C.POINTER(D), p, p, C.c_uint, C.c_uint, p]
+    f.restype = C.c_int
+    rf = np.ascontiguousarray(rf, dtype=dtype)
+    steps = np.ascontiguousarray(spec.steps, dtype=np.uint32).reshape(-1, 4)
+    ifxz = np.ascontiguousarray(spec.interface_xz, dtype=dtype).reshape(-1, 2)
+    apod = np.ascontiguousarray(spec.rx_apod, dtype=dtype)
+    d = D(spec.num_elements, spec.num_elements_mux, spec.pitch, spec.center_frequency, spec.propagation_speed_1,
+          spec.propagation_speed_2, spec.sampling_frequency, spec.num_samples, spec.upsampling,
+          spec.max_fermat_block_size, spec.peak_offset, spec.signal_start_offset, rf.shape[0], rf.shape[1],
+          steps.shape[0], steps.ctypes.data_as(C.POINTER(C.c_uint)), ifxz.shape[0], ifxz.ctypes.data_as(p),
+          apod.ctypes.data_as(p), spec.cf, spec.pcf_gamma)
+    g = np.ascontiguousarray(grid_xz, dtype=dtype)
+    out = np.zeros(g.shape[0] * g.shape[1] * 2, dtype=dtype)
+    rc = f(C.byref(d), rf.ctypes.data_as(p), g.ctypes.data_as(p), g.shape[0], g.shape[1], out.ctypes.data_as(p))
+    if rc != 0:
+        raise RuntimeError(lib.ref_last_error().decode())
+    return out.view(np.complex64 if dtype == np.float32 else np.complex128).reshape(g.shape[0], g.shape[1])

@@ -1,7 +1,8 @@
 // Driver that runs the reference's own processors, compiled from their
 // unchanged sources (src/user/processor/{VectorialSTAProcessor,
 // Vectorial3DSTAProcessor,DefaultSTAProcessor,Vectorial3DT1R1SAFTProcessor,
-// Vectorial3DTnRnProcessor,SynthYVectorial3DTnRnProcessor}.h), on in-memory RF.
+// Vectorial3DTnRnProcessor,SynthYVectorial3DTnRnProcessor,
+// VectorialCombinedTwoMediumImagingProcessor}.h), on in-memory RF.
 // TEST INFRASTRUCTURE ONLY: it produces golden outputs for the parity tests
 // and validates the oracle restatement; nothing in the product uses it.
 //
@@ -22,6 +23,7 @@
 #include "Vectorial3DSTAProcessor.h"
 #include "Vectorial3DT1R1SAFTProcessor.h"
 #include "Vectorial3DTnRnProcessor.h"
+#include "VectorialCombinedTwoMediumImagingProcessor.h"
 #include "VectorialSTAProcessor.h"
 #include "XYZValueFactor.h"
 
@@ -353,6 +355,97 @@ int run_single(const RefSingleDesc<T>* dp, const T* rf, const T* gridXYZ, unsign
 	}
 }
 
+template<typename T>
+struct RefTwoMediumDesc {
+	unsigned num_elements, num_elements_mux;
+	T pitch, center_frequency, propagation_speed_1, propagation_speed_2, sampling_frequency;
+	unsigned num_samples;        // samples per A-scan of every acquisition tensor
+	unsigned upsampling;
+	T max_fermat_block_size, peak_offset;
+	unsigned signal_start_offset;
+	unsigned num_acq, num_tx;    // acqDataList: num_acq tensors of (num_tx, num_elements, num_samples)
+	unsigned num_steps;
+	const unsigned* steps;       // num_steps x (baseElemIdx, baseElem, firstTxElem, lastTxElem)
+	unsigned num_interface;
+	const T* interface_xz;       // num_interface (x, z)
+	const T* rx_apod;            // num_elements
+	int cf;                      // 0 none, 1 PCF
+	T pcf_gamma;
+};
+
+// VectorialCombinedTwoMediumImagingProcessor<T>::process on a grid of n1
+// columns x n2 rows (x, z); out: n1 x n2 complex (re, im).
+template<typename T>
+int run_two_medium(const RefTwoMediumDesc<T>* dp, const T* rf, const T* gridXZ, unsigned n1, unsigned n2, T* out)
+{
+	try {
+		const RefTwoMediumDesc<T>& d = *dp;
+		TwoMediumSTAConfiguration<T> c;
+		c.numElements = d.num_elements;
+		c.numElementsMux = d.num_elements_mux;
+		c.pitch = d.pitch;
+		c.centerFrequency = d.center_frequency;
+		c.acquisitionTime = 1e-4;
+		c.minGain = 0;
+		c.maxGain = 0;
+		c.propagationSpeed1 = d.propagation_speed_1;
+		c.propagationSpeed2 = d.propagation_speed_2;
+		c.acquisitionDelay = 0;
+		c.samplingFrequency = d.sampling_frequency;
+		c.deadZoneM = 0;
+		std::vector<Tensor3<T>> acqDataList(d.num_acq);
+		const std::size_t acqSize = static_cast<std::size_t>(d.num_tx) * d.num_elements * d.num_samples;
+		for (unsigned a = 0; a < d.num_acq; ++a) {
+			acqDataList[a].resize(d.num_tx, d.num_elements, d.num_samples);
+			std::copy(rf + a * acqSize, rf + (a + 1) * acqSize, &acqDataList[a](0, 0, 0));
+		}
+		std::string text = "analytic_signal_coherence_factor_method = none\n";
+		if (d.cf == 1) {
+			char buf[64];
+			std::snprintf(buf, sizeof buf, "%.17g", static_cast<double>(d.pcf_gamma));
+			text = std::string("analytic_signal_coherence_factor_method = phase_coherence_factor\n"
+					"phase_coherence_factor_gamma = ") + buf + "\n";
+		}
+		TempParamFile f(text);
+		ParameterMap pm(f.path);
+		AnalyticSignalCoherenceFactorProcessor<T> cf(pm);
+		VectorialCombinedTwoMediumImagingProcessor<T> proc(c, acqDataList, d.upsampling, cf, d.max_fermat_block_size,
+				d.peak_offset, d.signal_start_offset);
+		std::vector<typename VectorialCombinedTwoMediumImagingProcessor<T>::StepConfiguration> steps;
+		for (unsigned i = 0; i < d.num_steps; ++i) {
+			const unsigned* s = d.steps + 4 * i;
+			steps.push_back({s[0], s[1], s[2], s[3]});
+		}
+		std::vector<XZ<T>> interfacePoints(d.num_interface);
+		for (unsigned i = 0; i < d.num_interface; ++i) {
+			interfacePoints[i].x = d.interface_xz[2 * i];
+			interfacePoints[i].z = d.interface_xz[2 * i + 1];
+		}
+		std::vector<T> apod(d.rx_apod, d.rx_apod + d.num_elements);
+		Matrix<XZ<T>> grid(n1, n2);
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				grid(i, j).x = gridXZ[2 * p];
+				grid(i, j).z = gridXZ[2 * p + 1];
+			}
+		}
+		Matrix<std::complex<T>> value(n1, n2);
+		proc.process(steps, interfacePoints, apod, grid, value);
+		for (unsigned i = 0; i < n1; ++i) {
+			for (unsigned j = 0; j < n2; ++j) {
+				const std::size_t p = static_cast<std::size_t>(i) * n2 + j;
+				out[2 * p] = value(i, j).real();
+				out[2 * p + 1] = value(i, j).imag();
+			}
+		}
+		return 0;
+	} catch (std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
+}
+
 }  // namespace
 
 extern "C" {
@@ -372,5 +465,15 @@ int ref_single_f32(const RefSingleDesc<float>* d, const float* rf, const float* 
 int ref_single_f64(const RefSingleDesc<double>* d, const double* rf, const double* grid, unsigned n1, unsigned n2, double* value, double* factor)
 {
 	return run_single<double>(d, rf, grid, n1, n2, value, factor);
+}
+int ref_two_medium_f32(const RefTwoMediumDesc<float>* d, const float* rf, const float* grid, unsigned n1, unsigned n2,
+		float* out)
+{
+	return run_two_medium<float>(d, rf, grid, n1, n2, out);
+}
+int ref_two_medium_f64(const RefTwoMediumDesc<double>* d, const double* rf, const double* grid, unsigned n1, unsigned n2,
+		double* out)
+{
+	return run_two_medium<double>(d, rf, grid, n1, n2, out);
 }
 }

@@ -888,6 +888,282 @@ void single_term_das(const SingleDesc<T>& d, const std::complex<T>* analytic, un
 	});
 }
 
+// ---------------------------------------------------------------------------
+// Two-medium imaging (linear array in medium 1 over an interface sampled as a
+// list of (x, z) points, image in medium 2): refracted delays by Fermat's
+// principle, then a tx x rx delay-and-sum per step of a sliding
+// sub-aperture, summed as complex values.
+// ---------------------------------------------------------------------------
+
+// FermatPrinciple::calcBlockSizeForTwoStepSearch (src/util/FermatPrinciple.h:106-115);
+// the maximum block size arrives as an unsigned number of wavelengths.
+template<typename T>
+unsigned fermat_block_size(unsigned n, T interfaceStep, T wavelength, unsigned maxBlockSizeInWavelengths)
+{
+	const T idealBlockSize = std::sqrt(n / 2.0) + 0.5;
+	const T maxBlockSize = (wavelength * maxBlockSizeInWavelengths) / interfaceStep;
+	const T blockSize = std::min(idealBlockSize, maxBlockSize);
+	return std::max(2U, static_cast<unsigned>(blockSize));
+}
+
+// Travel time element (x1, z1) -> interface point -> (x2, z2), minimised in
+// two steps (every blockSize-th point, then the points around the best one).
+// Follows src/util/FermatPrinciple.h:117-165.
+template<typename T>
+void fermat_min_time_two_steps(unsigned blockSize, T c1, T c2, const T* ifXZ, unsigned n, T x1, T z1, T x2, T z2,
+		T& tMin, unsigned& idxMin)
+{
+	const T invC1 = 1 / c1;
+	const T invC2 = 1 / c2;
+	auto time = [&](unsigned i) {
+		const T px = ifXZ[2 * i], pz = ifXZ[2 * i + 1];
+		const T dx1 = px - x1;
+		const T dz1 = pz - z1;
+		const T dx2 = x2 - px;
+		const T dz2 = z2 - pz;
+		return std::sqrt(dx1 * dx1 + dz1 * dz1) * invC1 + std::sqrt(dx2 * dx2 + dz2 * dz2) * invC2;
+	};
+	tMin = std::numeric_limits<T>::max();
+	idxMin = std::numeric_limits<unsigned>::max();
+	for (unsigned i = 0; i < n; i += blockSize) {
+		const T t = time(i);
+		if (t < tMin) {
+			tMin = t;
+			idxMin = i;
+		}
+	}
+	const unsigned iBegin = (idxMin > (blockSize - 1)) ? idxMin - (blockSize - 1) : 0;
+	const unsigned iEnd = std::min<unsigned>(idxMin + blockSize, n);
+	for (unsigned i = iBegin; i < iEnd; ++i) {
+		const T t = time(i);
+		if (t < tMin) {
+			tMin = t;
+			idxMin = i;
+		}
+	}
+}
+
+// Interface point nearest in x, in two steps. Follows src/util/FermatPrinciple.h:210-238.
+template<typename T>
+void fermat_nearest_x_two_steps(unsigned blockSize, const T* ifXZ, unsigned n, T x, T& zIdxMin, unsigned& idxMin)
+{
+	T dxMin = std::numeric_limits<T>::max();
+	idxMin = 0;
+	for (unsigned i = 0; i < n; i += blockSize) {
+		const T dx = std::abs(ifXZ[2 * i] - x);
+		if (dx < dxMin) {
+			dxMin = dx;
+			idxMin = i;
+		}
+	}
+	const unsigned iBegin = (idxMin > (blockSize - 1)) ? idxMin - (blockSize - 1) : 0;
+	const unsigned iEnd = std::min<unsigned>(idxMin + blockSize, n);
+	for (unsigned i = iBegin; i < iEnd; ++i) {
+		const T dx = std::abs(ifXZ[2 * i] - x);
+		if (dx < dxMin) {
+			dxMin = dx;
+			idxMin = i;
+		}
+	}
+	zIdxMin = ifXZ[2 * idxMin + 1];
+}
+
+template<typename T>
+struct TwoMediumDesc {
+	unsigned numElements = 0, numElementsMux = 0;
+	T pitch = 0, centerFrequency = 0, c1 = 0, c2 = 0, samplingFrequency = 0;
+	unsigned numSamples = 0, upsampling = 1;
+	T maxFermatBlockSize = 0, peakOffset = 0;
+	unsigned signalStartOffset = 0;
+	unsigned numAcq = 0, numTx = 0;       // acquisitions: numAcq x numTx x numElements x numSamples
+	unsigned numSteps = 0;
+	const unsigned* steps = nullptr;      // numSteps x (baseElemIdx, baseElem, firstTxElem, lastTxElem)
+	unsigned numInterface = 0;
+	const T* interfaceXZ = nullptr;
+	const T* rxApod = nullptr;            // numElements
+	int cf = CF_NONE;
+	T pcfGamma = 1;
+	int nthreads = 1;
+};
+
+// VectorialCombinedTwoMediumImagingProcessor<T>::process
+// (src/user/processor/VectorialCombinedTwoMediumImagingProcessor.h:230-401, with
+// CalculateDelays :403-484, PrepareData(WithOneTxElem) :486-570 and
+// ProcessColumn(WithOneTxElem) :572-790). gridXZ: ncols x nrows (x, z), rows
+// evenly spaced in z; out: ncols x nrows complex (rows above the interface 0).
+template<typename T>
+void two_medium_process(const TwoMediumDesc<T>& d, const T* rf, const T* gridXZ, unsigned ncols, unsigned nrows,
+		std::complex<T>* out)
+{
+	if (d.numSteps == 0) throw std::invalid_argument("The list of step configurations is empty.");
+	if (d.numInterface < 2) throw std::invalid_argument("The interface needs at least two points.");
+	const unsigned U = d.upsampling;
+	const unsigned L = d.numSamples * U;
+	const T lambda2 = d.c2 / d.centerFrequency;
+	const T signalOffset = (d.samplingFrequency * U) * (d.peakOffset / d.centerFrequency) - d.signalStartOffset * U;
+	const T* ifXZ = d.interfaceXZ;
+	const unsigned nIf = d.numInterface;
+	auto gx = [&](unsigned col, unsigned row) { return gridXZ[2 * (static_cast<std::size_t>(col) * nrows + row)]; };
+	auto gz = [&](unsigned col, unsigned row) { return gridXZ[2 * (static_cast<std::size_t>(col) * nrows + row) + 1]; };
+
+	const T dxI = ifXZ[2] - ifXZ[0];
+	const T dzI = ifXZ[3] - ifXZ[1];
+	const T r = std::sqrt(dxI * dxI + dzI * dzI);
+	const unsigned blockSize = fermat_block_size<T>(nIf, r, lambda2, static_cast<unsigned>(d.maxFermatBlockSize));
+
+	// First imaged row of every column (the first one below the interface).
+	std::vector<unsigned> minRow(ncols);
+	const T zStep = gz(0, 1) - gz(0, 0);
+	for (unsigned col = 0; col < ncols; ++col) {
+		T zIdxMin;
+		unsigned idxMin;
+		fermat_nearest_x_two_steps<T>(blockSize, ifXZ, nIf, gx(col, 0), zIdxMin, idxMin);
+		if (zIdxMin <= gz(col, 0)) {
+			minRow[col] = 1;
+		} else if (zIdxMin >= gz(col, nrows - 1)) {
+			minRow[col] = nrows;
+		} else {
+			minRow[col] = static_cast<unsigned>(std::ceil((zIdxMin - gz(col, 0)) / zStep)) + 1;
+		}
+	}
+
+	// Element x (ArrayGeometry::getElementX2D, src/util/ArrayGeometry.h:51-63) and
+	// medium-1 paths element -> interface point, in medium-2 length units.
+	const T c2ByC1 = d.c2 / d.c1;
+	std::vector<T> xArray(d.numElementsMux);
+	const T xCenter = ((d.numElementsMux - 1) * d.pitch) / 2 - T(0);
+	for (unsigned e = 0; e < d.numElementsMux; ++e) xArray[e] = e * d.pitch - xCenter;
+	std::vector<T> medium1(static_cast<std::size_t>(d.numElementsMux) * nIf);
+	for (unsigned e = 0; e < d.numElementsMux; ++e) {
+		for (unsigned i = 0; i < nIf; ++i) {
+			const T dx = ifXZ[2 * i] - xArray[e];
+			const T z = ifXZ[2 * i + 1];
+			medium1[static_cast<std::size_t>(e) * nIf + i] = std::sqrt(dx * dx + z * z) * c2ByC1;
+		}
+	}
+
+	// Delays in samples, (col, row, element): a Fermat search for the first
+	// imaged row, then a walk along the interface from the previous row's point.
+	const T fs = d.samplingFrequency * U;
+	const T fsInvC2 = d.samplingFrequency * U / d.c2;
+	const std::size_t mux = d.numElementsMux;
+	std::vector<T> delay(static_cast<std::size_t>(ncols) * nrows * mux, T(0));
+	parallel_for(ncols, d.nthreads, [&](std::size_t b, std::size_t e) {
+		for (std::size_t col = b; col < e; ++col) {
+			if (minRow[col] >= nrows) continue;
+			for (unsigned elem = 0; elem < d.numElementsMux; ++elem) {
+				unsigned last = 0;
+				{
+					const unsigned row = minRow[col];
+					T tMin;
+					unsigned idxMin;
+					fermat_min_time_two_steps<T>(blockSize, d.c1, d.c2, ifXZ, nIf, xArray[elem], T(0),
+							gx(static_cast<unsigned>(col), row), gz(static_cast<unsigned>(col), row), tMin, idxMin);
+					delay[(col * nrows + row) * mux + elem] = tMin * fs;
+					last = idxMin;
+				}
+				const T* m1 = &medium1[static_cast<std::size_t>(elem) * nIf];
+				for (unsigned row = minRow[col] + 1; row < nrows; ++row) {
+					const T px = gx(static_cast<unsigned>(col), row), pz = gz(static_cast<unsigned>(col), row);
+					auto tc2 = [&](unsigned i) {
+						const T dx = px - ifXZ[2 * i];
+						const T dz = pz - ifXZ[2 * i + 1];
+						return m1[i] + std::sqrt(dx * dx + dz * dz);
+					};
+					unsigned idxMin = last;
+					T tC2Min = tc2(idxMin);
+					for (unsigned i = idxMin + 1; i < nIf; ++i) {
+						const T t = tc2(i);
+						if (t >= tC2Min) break;
+						tC2Min = t;
+						idxMin = i;
+					}
+					if (idxMin == last) {
+						for (int i = static_cast<int>(idxMin) - 1; i >= 0; --i) {
+							const T t = tc2(static_cast<unsigned>(i));
+							if (t >= tC2Min) break;
+							tC2Min = t;
+							idxMin = static_cast<unsigned>(i);
+						}
+					}
+					delay[(col * nrows + row) * mux + elem] = tC2Min * fsInvC2;
+					last = idxMin;
+				}
+			}
+		}
+	});
+
+	// Signals: the STA preparation (upsampling, DC removal over the whole
+	// A-scan, analytic signal) of every acquisition, (acq, tx, rx, L).
+	StaDesc<T> pd;
+	pd.numTx = d.numAcq * d.numTx;
+	pd.numRx = d.numElements;
+	pd.numSamples = d.numSamples;
+	pd.upsampling = U;
+	pd.samplingFrequency = d.samplingFrequency;
+	pd.propagationSpeed = d.c1;
+	pd.centerFrequency = d.centerFrequency;
+	pd.deadZoneM = 0;
+	pd.nthreads = d.nthreads;
+	std::vector<std::complex<T>> sig;
+	prepare_signals<T>(pd, rf, &sig, nullptr);
+
+	T pcfFactor = 0;
+	if (d.cf == CF_PCF) {
+		const T sigma0 = kPi / std::sqrt(3.0);
+		pcfFactor = d.pcfGamma / sigma0;
+	}
+	const bool oneTx = d.steps[2] == d.steps[3];
+	const unsigned maxPosition = L - 2;
+	const std::size_t acqStride = static_cast<std::size_t>(d.numTx) * d.numElements * L;
+	parallel_for(ncols, d.nthreads, [&](std::size_t b, std::size_t e) {
+		std::vector<std::complex<T>> rxSum(d.numElements);
+		std::vector<T> phi, phiAux;
+		for (std::size_t col = b; col < e; ++col) {
+			for (unsigned row = 0; row < nrows; ++row) out[col * nrows + row] = std::complex<T>(0);
+			for (unsigned row = minRow[col]; row < nrows; ++row) {
+				std::complex<T> pointSum(0);
+				for (unsigned si = 0; si < d.numSteps; ++si) {
+					const unsigned* st = d.steps + 4 * si;
+					const unsigned baseElemIdx = st[0], baseElem = st[1], firstTx = st[2], lastTx = st[3];
+					const T* delays = &delay[(col * nrows + row) * mux + baseElem];
+					std::fill(rxSum.begin(), rxSum.end(), std::complex<T>(0));
+					for (unsigned tx = firstTx; tx <= lastTx; ++tx) {
+						const T txOffset = signalOffset + delays[tx];
+						// One transmit element: the signals of acquisition baseElemIdx, row 0.
+						const std::complex<T>* p = sig.data() + baseElemIdx * acqStride +
+								static_cast<std::size_t>(oneTx ? 0 : tx - firstTx) * d.numElements * L;
+						for (unsigned rx = 0; rx < d.numElements; ++rx, p += L) {
+							const T position = txOffset + delays[rx];
+							if (position >= 0.0f) {
+								const unsigned idx = static_cast<unsigned>(position);
+								if (idx <= maxPosition) {
+									const T k = position - idx;
+									const std::complex<T> v0 = p[idx], v1 = p[idx + 1];
+									if (oneTx) rxSum[rx] = v0 + k * (v1 - v0); else rxSum[rx] += v0 + k * (v1 - v0);
+								} else if (oneTx) {
+									rxSum[rx] = 0;
+								}
+							} else if (oneTx) {
+								rxSum[rx] = 0;
+							}
+						}
+					}
+					std::complex<T> sum(0);
+					for (unsigned rx = 0; rx < d.numElements; ++rx) sum += rxSum[rx] * d.rxApod[rx];
+					if (d.cf == CF_PCF) {
+						const T f = pcf<T>(rxSum.data(), d.numElements, pcfFactor, phi, phiAux);
+						if (oneTx) pointSum += sum * f; else out[col * nrows + row] += sum * f;
+					} else {
+						if (oneTx) pointSum += sum; else out[col * nrows + row] += sum;
+					}
+				}
+				if (oneTx) out[col * nrows + row] = pointSum;
+			}
+		}
+	});
+}
+
 }  // namespace orc
 
 #endif  // USGB_STA_ORACLE_HPP

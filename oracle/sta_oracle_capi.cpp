@@ -149,6 +149,58 @@ int single(const CSingleDesc<T>* c, const T* rf, const T* grid, std::size_t npix
 		return -1;
 	}
 }
+
+template<typename T>
+struct CTwoMediumDesc {
+	unsigned num_elements, num_elements_mux;
+	T pitch, center_frequency, propagation_speed_1, propagation_speed_2, sampling_frequency;
+	unsigned num_samples, upsampling;
+	T max_fermat_block_size, peak_offset;
+	unsigned signal_start_offset;
+	unsigned num_acq, num_tx, num_steps;
+	const unsigned* steps;
+	unsigned num_interface;
+	const T* interface_xz;
+	const T* rx_apod;
+	int cf;
+	T pcf_gamma;
+	int nthreads;
+};
+
+template<typename T>
+int two_medium(const CTwoMediumDesc<T>* c, const T* rf, const T* grid, unsigned ncols, unsigned nrows, T* out)
+{
+	try {
+		orc::TwoMediumDesc<T> d;
+		d.numElements = c->num_elements;
+		d.numElementsMux = c->num_elements_mux;
+		d.pitch = c->pitch;
+		d.centerFrequency = c->center_frequency;
+		d.c1 = c->propagation_speed_1;
+		d.c2 = c->propagation_speed_2;
+		d.samplingFrequency = c->sampling_frequency;
+		d.numSamples = c->num_samples;
+		d.upsampling = c->upsampling;
+		d.maxFermatBlockSize = c->max_fermat_block_size;
+		d.peakOffset = c->peak_offset;
+		d.signalStartOffset = c->signal_start_offset;
+		d.numAcq = c->num_acq;
+		d.numTx = c->num_tx;
+		d.numSteps = c->num_steps;
+		d.steps = c->steps;
+		d.numInterface = c->num_interface;
+		d.interfaceXZ = c->interface_xz;
+		d.rxApod = c->rx_apod;
+		d.cf = c->cf;
+		d.pcfGamma = c->pcf_gamma;
+		d.nthreads = c->nthreads;
+		orc::two_medium_process<T>(d, rf, grid, ncols, nrows, reinterpret_cast<std::complex<T>*>(out));
+		return 0;
+	} catch (const std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
+}
 }  // namespace
 
 extern "C" {
@@ -192,6 +244,20 @@ int orc_single_f64(const CSingleDesc<double>* d, const double* rf, const double*
 		double* value, double* factor, double* signals_out)
 {
 	return single<double>(d, rf, grid, npix, value, factor, signals_out);
+}
+
+// Two-medium imaging (VectorialCombinedTwoMediumImagingProcessor): rf =
+// num_acq x num_tx x num_elements x num_samples, grid = ncols x nrows (x, z),
+// out = ncols x nrows complex (re, im).
+int orc_two_medium_f32(const CTwoMediumDesc<float>* d, const float* rf, const float* grid, unsigned ncols, unsigned nrows,
+		float* out)
+{
+	return two_medium<float>(d, rf, grid, ncols, nrows, out);
+}
+int orc_two_medium_f64(const CTwoMediumDesc<double>* d, const double* rf, const double* grid, unsigned ncols,
+		unsigned nrows, double* out)
+{
+	return two_medium<double>(d, rf, grid, ncols, nrows, out);
 }
 
 // Building blocks, for the golden-vector tests.

@@ -39,6 +39,11 @@ def golden_single():
 
 
 @pytest.fixture(scope="session")
+def golden_two_medium():
+    return np.load(os.path.join(GOLDEN, "reference_two_medium.npz"))
+
+
+@pytest.fixture(scope="session")
 def cuda():
     """The GPU tests' device. On a machine with a GPU the native library must
     build and load (no fallback); without one the test is an error, not a skip."""

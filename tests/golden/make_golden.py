@@ -17,8 +17,12 @@ sources are present; the fixtures are committed and travel with the tests).
    (Vectorial3DT1R1SAFTProcessor, Vectorial3DTnRnProcessor,
    SynthYVectorial3DTnRnProcessor) on a 6 x 5 matrix array, every input
    parameter stored beside the outputs.
+4. reference_two_medium.npz: the same for VectorialCombinedTwoMediumImagingProcessor
+   (one transmit element per step and STA steps, with and without PCF) on
+   small two-medium scenes (noise-free RF, stored as FP16 values).
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference] [--vectors-only | --single-only]
+Usage: python tests/golden/make_golden.py [--reference /root/reference]
+           [--vectors-only | --single-only | --two-medium-only]
 """
 from __future__ import annotations
 
@@ -218,12 +222,62 @@ def reference_single_frames() -> dict:
     return out
 
 
+# name: (one transmit element per step, steps, upsampling, CF, PCF gamma, max Fermat block size)
+TWO_MEDIUM_CASES = {
+    "onetx_plain": (True, 4, 4, 0, 1.0, 2.0),
+    "onetx_pcf": (True, 3, 4, 1, 1.0, 2.0),
+    "sta_plain": (False, 3, 2, 0, 1.0, 2.0),
+    "sta_pcf": (False, 3, 4, 1, 2.0, 3.5),
+}
+
+
+def two_medium_spec(oracle_mod, sc, cf, gamma):
+    return oracle_mod.TwoMediumSpec(
+        num_elements=sc.num_elements, num_elements_mux=sc.num_elements_mux, pitch=sc.pitch,
+        center_frequency=sc.center_frequency, propagation_speed_1=sc.propagation_speed_1,
+        propagation_speed_2=sc.propagation_speed_2, sampling_frequency=sc.sampling_frequency,
+        num_samples=sc.num_samples, upsampling=sc.upsampling, steps=sc.steps, interface_xz=sc.interface_xz,
+        rx_apod=sc.rx_apod, max_fermat_block_size=sc.max_fermat_block_size, peak_offset=sc.peak_offset,
+        signal_start_offset=sc.signal_start_offset, cf=cf, pcf_gamma=gamma)
+
+
+def reference_two_medium_frames() -> dict:
+    import oracle
+    from oracle import ref
+    from us_lab4a_gb300 import workloads
+    out = {}
+    for i, (name, (one_tx, nsteps, U, cf, gamma, mfbs)) in enumerate(sorted(TWO_MEDIUM_CASES.items())):
+        sc = workloads.two_medium_scene(one_tx, num_elements=8, num_elements_mux=16, num_steps=nsteps,
+                                        num_samples=1000, upsampling=U, grid=(24, 64), tx_element=3,
+                                        sampling_frequency=20e6, num_scatterers=8, noise_std=0.0, seed=3000 + i)
+        sc.rf = sc.rf.astype(np.float16).astype(np.float32)
+        sc.max_fermat_block_size = mfbs
+        img = ref.two_medium(two_medium_spec(oracle, sc, cf, gamma), sc.rf, sc.grid_xz, dtype=np.float32)
+        meta = dict(num_elements=sc.num_elements, num_elements_mux=sc.num_elements_mux, pitch=sc.pitch,
+                    fc=sc.center_frequency, c1=sc.propagation_speed_1, c2=sc.propagation_speed_2,
+                    fs=sc.sampling_frequency, upsampling=U, steps=sc.steps, interface_xz=sc.interface_xz,
+                    rx_apod=sc.rx_apod, grid_xz=sc.grid_xz, rf=sc.rf.astype(np.float16), max_fermat_block_size=mfbs,
+                    peak_offset=sc.peak_offset, signal_start_offset=sc.signal_start_offset, cf=cf, pcf_gamma=gamma,
+                    image=img)
+        for k, x in meta.items():
+            out[name + "/" + k] = np.asarray(x)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
     ap.add_argument("--single-only", action="store_true", help="rewrite reference_single.npz only")
+    ap.add_argument("--two-medium-only", action="store_true", help="rewrite reference_two_medium.npz only")
     args = ap.parse_args()
+    if args.two_medium_only:
+        from oracle import ref
+        if not ref.available():
+            ref.build()
+        np.savez_compressed(os.path.join(HERE, "reference_two_medium.npz"), **reference_two_medium_frames())
+        print("reference_two_medium.npz", os.path.getsize(os.path.join(HERE, "reference_two_medium.npz")))
+        return
     if args.single_only:
         from oracle import ref
         if not ref.available():
@@ -242,7 +296,8 @@ def main():
     frames = reference_frames()
     np.savez_compressed(os.path.join(HERE, "reference_frames.npz"), **frames)
     np.savez_compressed(os.path.join(HERE, "reference_single.npz"), **reference_single_frames())
-    for f in ("reference_vectors.npz", "reference_frames.npz", "reference_single.npz"):
+    np.savez_compressed(os.path.join(HERE, "reference_two_medium.npz"), **reference_two_medium_frames())
+    for f in ("reference_vectors.npz", "reference_frames.npz", "reference_single.npz", "reference_two_medium.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 

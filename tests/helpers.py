@@ -79,3 +79,21 @@ def single_case(oracle_lib, d, name):
                                  peak_offset=float(g("peak_offset")), dead_zone_m=float(g("dead_zone_m")),
                                  cf=int(g("cf")), pcf_gamma=float(g("pcf_gamma")), **kw)
     return spec, rf, g("grid")
+
+
+TWO_MEDIUM_CASE_NAMES = ("onetx_pcf", "onetx_plain", "sta_pcf", "sta_plain")
+
+
+def two_medium_case(oracle_lib, d, name):
+    """(TwoMediumSpec, rf float32 (num_acq, num_tx, num_elements, num_samples), grid_xz)
+    of one case of reference_two_medium.npz."""
+    g = lambda k: d[name + "/" + k]
+    rf = g("rf").astype(np.float32)
+    spec = oracle_lib.TwoMediumSpec(
+        num_elements=int(g("num_elements")), num_elements_mux=int(g("num_elements_mux")), pitch=float(g("pitch")),
+        center_frequency=float(g("fc")), propagation_speed_1=float(g("c1")), propagation_speed_2=float(g("c2")),
+        sampling_frequency=float(g("fs")), num_samples=rf.shape[3], upsampling=int(g("upsampling")),
+        steps=g("steps"), interface_xz=g("interface_xz"), rx_apod=g("rx_apod"),
+        max_fermat_block_size=float(g("max_fermat_block_size")), peak_offset=float(g("peak_offset")),
+        signal_start_offset=int(g("signal_start_offset")), cf=int(g("cf")), pcf_gamma=float(g("pcf_gamma")))
+    return spec, rf, g("grid_xz")

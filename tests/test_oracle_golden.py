@@ -205,3 +205,30 @@ def test_single_term_tx_focus_delays_match_reference(golden_single):
         fx, fy, fz = (float(x) for x in g("focus"))
         got = tx_3d_focus_delay(fx, fy, fz, float(g("c")), g("tx_xy"))
         assert np.array_equal(got, g("tx_delays").astype(np.float32)), name
+
+
+@pytest.mark.parametrize("name", ["onetx_pcf", "onetx_plain", "sta_pcf", "sta_plain"])
+def test_two_medium_oracle_matches_reference_processor(oracle_lib, golden_two_medium, name):
+    """The FP32 oracle of the two-medium imaging reproduces
+    VectorialCombinedTwoMediumImagingProcessor<float> (compiled from the
+    reference's sources): Fermat delays, minimum rows, one-transmit and STA
+    steps, PCF; within 1e-5 of the image maximum, the same points zero."""
+    from helpers import two_medium_case
+    spec, rf, grid = two_medium_case(oracle_lib, golden_two_medium, name)
+    img = oracle_lib.two_medium(spec, rf, grid, dtype=np.float32)
+    ref = golden_two_medium[name + "/image"]
+    assert np.abs(ref).max() > 0
+    assert np.abs(img - ref).max() <= 1e-5 * np.abs(ref).max()
+    assert np.array_equal(img == 0, ref == 0)
+
+
+def test_two_medium_fermat_block_size_rule(oracle_lib, golden_two_medium):
+    """FermatPrinciple::calcBlockSizeForTwoStepSearch takes the maximum block
+    size as an unsigned number of wavelengths: 3.5 acts as 3."""
+    from helpers import two_medium_case
+    spec, rf, grid = two_medium_case(oracle_lib, golden_two_medium, "sta_pcf")
+    spec.max_fermat_block_size = 3.0
+    a = oracle_lib.two_medium(spec, rf, grid, dtype=np.float32)
+    spec.max_fermat_block_size = 3.5
+    b = oracle_lib.two_medium(spec, rf, grid, dtype=np.float32)
+    assert np.array_equal(a, b)

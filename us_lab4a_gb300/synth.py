@@ -160,3 +160,45 @@ def synth_rf_pairs_torch(tx_xy, rx_xy, scat: Scatterers, fs: float, c: float, fc
         g.manual_seed(seed)
         rf += noise_std * torch.randn(rf.shape, generator=g, device=dev, dtype=torch.float32)
     return rf
+
+
+def two_medium_travel_times(elem_x: np.ndarray, interface_xz: np.ndarray, points_xz: np.ndarray, c1: float,
+                            c2: float) -> np.ndarray:
+    """(num_elements, num_points) one-way travel time from elements at
+    (x, 0) in medium 1 to points in medium 2 through the sampled interface:
+    the minimum over the interface points (Fermat's principle, brute force)."""
+    ex = np.asarray(elem_x, np.float64)[:, None, None]
+    ix = np.asarray(interface_xz, np.float64)[None, :, 0:1]
+    iz = np.asarray(interface_xz, np.float64)[None, :, 1:2]
+    px = np.asarray(points_xz, np.float64)[None, None, :, 0]
+    pz = np.asarray(points_xz, np.float64)[None, None, :, 1]
+    t = np.sqrt((ix - ex) ** 2 + iz ** 2) / c1 + np.sqrt((px - ix) ** 2 + (pz - iz) ** 2) / c2   # (E, I, P)
+    return t.min(axis=1)
+
+
+def synth_rf_two_medium_numpy(tx_x: np.ndarray, rx_x: np.ndarray, interface_xz: np.ndarray, scat_xz: np.ndarray,
+                              amp: np.ndarray, fs: float, c1: float, c2: float, fc: float, num_samples: int,
+                              rng: np.random.Generator, noise_std: float = 0.0, bw: float = 0.6,
+                              start_offset: int = 0) -> np.ndarray:
+    """(num_tx, num_rx, num_samples) float32 RF of point scatterers in medium 2
+    seen through the interface; samples before `start_offset` are dropped
+    (the dead zone cut of the two-medium method)."""
+    ttx = two_medium_travel_times(tx_x, interface_xz, scat_xz, c1, c2)   # (T, S)
+    trx = two_medium_travel_times(rx_x, interface_xz, scat_xz, c1, c2)   # (R, S)
+    a = gauss_coefficient(fc, bw)
+    hw = _half_width(a, fs)
+    ntx, nrx = ttx.shape[0], trx.shape[0]
+    rf = np.zeros(ntx * nrx * num_samples, np.float64)
+    offs = np.arange(-hw, hw + 1)
+    base = (np.arange(ntx)[:, None] * nrx + np.arange(nrx)[None, :]) * num_samples
+    tau = ttx[:, None, :] + trx[None, :, :] - start_offset / fs                  # (T, R, S)
+    n0 = np.floor(tau * fs).astype(np.int64)
+    n = n0[..., None] + offs
+    t = n / fs - tau[..., None]
+    v = np.asarray(amp, np.float64)[None, None, :, None] * np.exp(-a * t * t) * np.cos(2.0 * math.pi * fc * t)
+    ok = (n >= 0) & (n < num_samples)
+    np.add.at(rf, (base[:, :, None, None] + n)[ok], v[ok])
+    rf = rf.reshape(ntx, nrx, num_samples)
+    if noise_std > 0:
+        rf += rng.normal(0.0, noise_std, rf.shape)
+    return rf.astype(np.float32)

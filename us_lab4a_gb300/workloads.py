@@ -13,6 +13,12 @@
   mixed        frames drawn from {32,64,96,128} elements x {1024,2048,4096}
                samples x {128x128, 256x256, 512x1024} grids x CF on/off,
                16 scatterers each, 4x upsampling (the mixed-size batch).
+  two_medium   linear array in water (c1 1480 m/s) over a cylinder of a
+               second medium (c2 2700 m/s, radius 15 mm, top at 15 mm): the
+               interface is the upper arc (-170..-10 degrees) sampled every
+               lambda2 / 4, a sub-aperture stepped across the array, one
+               transmit element or every element per step (STA), scatterers
+               inside the cylinder, grid below the top of the cylinder.
 Grid extents and upsampling of the mixed frames are not fixed by the
 workload descriptions; the values above are this library's choice.
 Each workload also has a reduced "small" form for CPU-oracle parity tests.
@@ -185,3 +191,69 @@ def large_serving_frame(seed: int = 1004, storage: str = "f16") -> Frame:
 
 def with_storage(frame: Frame, storage: str) -> Frame:
     return replace(frame, spec=replace(frame.spec, storage=storage))
+
+
+@dataclass
+class TwoMediumScene:
+    """Inputs of VectorialCombinedTwoMediumImagingProcessor: configuration
+    fields, per-step acquisitions, steps, interface, apodization and grid."""
+    num_elements: int
+    num_elements_mux: int
+    pitch: float
+    center_frequency: float
+    propagation_speed_1: float
+    propagation_speed_2: float
+    sampling_frequency: float
+    upsampling: int
+    steps: np.ndarray            # (num_steps, 4) uint32: baseElemIdx, baseElem, firstTxElem, lastTxElem
+    interface_xz: np.ndarray     # (m, 2) float32
+    rx_apod: np.ndarray          # (num_elements,) float32
+    grid_xz: np.ndarray          # (ncols, nrows, 2) float32
+    rf: np.ndarray               # (num_steps, num_tx, num_elements, num_samples) float32
+    max_fermat_block_size: float = 2.0
+    peak_offset: float = 1.5
+    signal_start_offset: int = 0
+
+    @property
+    def num_samples(self) -> int:
+        return int(self.rf.shape[3])
+
+
+def two_medium_scene(one_tx: bool, num_elements: int = 32, num_elements_mux: int = 64, num_steps: int = 8,
+                     num_samples: int = 2000, upsampling: int = 4, grid=(128, 256), tx_element: int = 0,
+                     sampling_frequency: float = 40e6, num_scatterers: int = 24, noise_std: float = 0.01,
+                     seed: int = 1005) -> TwoMediumScene:
+    pitch, fc, c1, c2, fs = 0.6e-3, 5e6, 1480.0, 2700.0, sampling_frequency
+    rng = np.random.default_rng(seed)
+    R, cz = 15e-3, 30e-3
+    lam2 = c2 / fc
+    a1, a2 = np.deg2rad(-170.0), np.deg2rad(-10.0)
+    m = int(np.ceil((a2 - a1) / (lam2 / (4 * R)))) + 1
+    ang = np.linspace(a1, a2, m)
+    ifxz = np.stack([R * np.cos(ang), cz + R * np.sin(ang)], axis=1).astype(np.float32)
+    xs = np.linspace(-8e-3, 8e-3, grid[0])
+    zs = np.linspace(14e-3, 40e-3, grid[1])
+    grid_xz = np.stack(np.meshgrid(xs, zs, indexing="ij"), axis=-1).astype(np.float32)
+    base = np.round(np.linspace(0, num_elements_mux - num_elements, num_steps)).astype(np.uint32)
+    steps = np.array([[i, b, tx_element, tx_element] if one_tx else [i, b, 0, num_elements - 1]
+                      for i, b in enumerate(base)], np.uint32)
+    x = (np.arange(num_elements_mux) * pitch - (num_elements_mux - 1) * pitch / 2).astype(np.float64)
+    # Scatterers inside the cylinder (a disc of radius 12 mm around the axis).
+    rr = 12e-3 * np.sqrt(rng.uniform(0.0, 1.0, num_scatterers))
+    th = rng.uniform(0.0, 2 * np.pi, num_scatterers)
+    scat = np.stack([rr * np.cos(th), cz + rr * np.sin(th)], axis=1)
+    amp = rng.uniform(0.5, 1.0, num_scatterers)
+    start = 7
+    ntx = 1 if one_tx else num_elements
+    rf = np.zeros((num_steps, ntx, num_elements, num_samples), np.float32)
+    for i, b in enumerate(base):
+        sub = x[b:b + num_elements]
+        tx = sub[tx_element:tx_element + 1] if one_tx else sub
+        rf[i] = synth.synth_rf_two_medium_numpy(tx, sub, ifxz, scat, amp, fs, c1, c2, fc, num_samples, rng,
+                                                noise_std=noise_std, start_offset=start)
+    apod = np.hanning(num_elements + 2)[1:-1].astype(np.float32)
+    return TwoMediumScene(num_elements=num_elements, num_elements_mux=num_elements_mux, pitch=pitch,
+                          center_frequency=fc, propagation_speed_1=c1, propagation_speed_2=c2,
+                          sampling_frequency=fs, upsampling=upsampling, steps=steps, interface_xz=ifxz,
+                          rx_apod=apod, grid_xz=grid_xz, rf=rf, max_fermat_block_size=2.0, peak_offset=1.5,
+                          signal_start_offset=start)
