@@ -360,6 +360,73 @@ int usgb_single_process_window_device(usgb_single* single, uint32_t first_acq, u
 		float* d_factor);
 int usgb_single_synchronize(usgb_single* single);
 
+/*
+ * Two-medium imaging: a linear array in medium 1 (speed c1) images medium 2
+ * (speed c2) through an interface given as a list of (x, z) points. Delays
+ * follow Fermat's principle (the fastest path through an interface point);
+ * each step of a sub-aperture moved across the array adds its delay-and-sum
+ * (one transmit element, or STA over several) to a complex image. Drop-in for
+ *   VectorialCombinedTwoMediumImagingProcessor<float>
+ *     src/user/processor/VectorialCombinedTwoMediumImagingProcessor.h:59-401
+ *     (constructor :192-228, process(stepConfigList, interfacePointList,
+ *     rxApod, gridXZ, gridValue) :230-401)
+ * and the work of VectorialCombinedTwoMediumImagingCUDAProcessor{,2}
+ * (src/user/processor/VectorialCombinedTwoMediumImagingCUDAProcessor.h), with
+ * the delay search, the signal preparation and every gather on the GPU.
+ */
+typedef struct usgb_two_medium_params {
+	uint32_t num_elements;          /* numElements: elements of one step (receive; and transmit in STA steps) */
+	uint32_t num_elements_mux;      /* numElementsMux: elements of the array, pitch apart, centred on x = 0 */
+	float pitch;                    /* m */
+	float center_frequency;         /* Hz */
+	float propagation_speed_1;      /* medium of the array, m/s */
+	float propagation_speed_2;      /* imaged medium, m/s */
+	float sampling_frequency;       /* Hz */
+	uint32_t num_samples;           /* samples per A-scan of the acquisitions (after the start offset cut) */
+	uint32_t upsampling;            /* 1..64 */
+	float max_fermat_block_size;    /* maxFermatBlockSize, wavelengths; used as an unsigned count, as the reference */
+	float peak_offset;              /* periods of center_frequency */
+	uint32_t signal_start_offset;   /* samples cut from the start of every A-scan before the acquisitions */
+	uint32_t num_acquisitions;      /* acqDataList.size() */
+	uint32_t num_tx;                /* transmit events per acquisition (acqDataList[i].n1()) */
+	uint32_t coherence;             /* usgb_coherence over the receive terms of a step (the reference: none or PCF) */
+	float pcf_gamma;
+	float scf_p;
+	uint32_t storage;               /* usgb_storage of the prepared signals */
+	float storage_scale;            /* samples are multiplied by this before FP16/BF16 storage; 0 = 1 */
+} usgb_two_medium_params;
+
+/* StepConfiguration: acquisition index, first element of the sub-aperture,
+ * transmit elements first..last relative to it (all steps one element, or
+ * all several). */
+typedef struct usgb_two_medium_step {
+	uint32_t base_elem_idx;
+	uint32_t base_elem;
+	uint32_t first_tx_elem;
+	uint32_t last_tx_elem;
+} usgb_two_medium_step;
+
+typedef struct usgb_two_medium usgb_two_medium;
+int usgb_two_medium_create(const usgb_two_medium_params* params, usgb_two_medium** tm);
+void usgb_two_medium_destroy(usgb_two_medium* tm);
+const char* usgb_two_medium_last_error(const usgb_two_medium* tm);  /* NULL: last failed create on this thread */
+int usgb_two_medium_set_stream(usgb_two_medium* tm, void* cuda_stream);
+
+/* process(): rf = the acquisitions (num_acquisitions x num_tx x num_elements x
+ * num_samples floats), interface_xz = num_interface (x, z) pairs, rx_apod =
+ * num_elements weights, grid_xz = ncols x nrows (x, z) pairs (column-major,
+ * rows evenly spaced in z), value = ncols x nrows complex (re, im) pairs;
+ * points above the interface are 0. Host pointers, synchronous; the _device
+ * form takes device pointers (steps stay on the host) and runs asynchronously
+ * on the stream. */
+int usgb_two_medium_process(usgb_two_medium* tm, const float* rf, const usgb_two_medium_step* steps, uint32_t num_steps,
+		const float* interface_xz, uint32_t num_interface, const float* rx_apod, const float* grid_xz, uint32_t ncols,
+		uint32_t nrows, float* value);
+int usgb_two_medium_process_device(usgb_two_medium* tm, const float* d_rf, const usgb_two_medium_step* steps,
+		uint32_t num_steps, const float* d_interface_xz, uint32_t num_interface, const float* d_rx_apod,
+		const float* d_grid_xz, uint32_t ncols, uint32_t nrows, float* d_value);
+int usgb_two_medium_synchronize(usgb_two_medium* tm);
+
 /* Library version string. */
 const char* usgb_version(void);
 

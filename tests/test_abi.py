@@ -191,3 +191,37 @@ def test_single_processor_mirrors_reference_checks():
     proc.set_tx_delays(0.0, 0.0, 0.01, np.zeros(8))
     with pytest.raises(InvalidParameterException, match="Invalid base element: 9"):
         proc.prepare(9)
+
+
+def _tm_params(**kw):
+    from us_lab4a_gb300 import native
+    p = native.TwoMediumParams()
+    p.num_elements, p.num_elements_mux, p.pitch = 16, 32, 0.6e-3
+    p.center_frequency, p.propagation_speed_1, p.propagation_speed_2 = 5e6, 1480.0, 2700.0
+    p.sampling_frequency, p.num_samples, p.upsampling = 40e6, 1000, 4
+    p.max_fermat_block_size, p.num_acquisitions, p.num_tx = 2.0, 3, 1
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+@pytest.mark.parametrize("field,value,status,msg", [
+    ("num_elements", 0, 1, "number of elements is zero"),
+    ("num_elements", 33, 1, "num_elements (33) > num_elements_mux (32)"),
+    ("num_elements_mux", 2000, 1, "More than 1024 elements"),
+    ("num_samples", 1, 1, "number of samples (1) is < 2"),
+    ("num_acquisitions", 0, 1, "No acquisition data"),
+    ("upsampling", 0, 2, "Invalid upsampling factor"),
+    ("propagation_speed_2", 0.0, 2, "must be > 0"),
+    ("coherence", 7, 1, "Invalid coherence factor"),
+    ("storage", 5, 1, "Invalid storage"),
+    ("num_samples", 300000, 1, "greater than 1048576"),
+])
+def test_two_medium_create_rejects_invalid_frames(lib, field, value, status, msg):
+    """usgb_two_medium_create checks the parameters on the host before any
+    device work."""
+    p = _tm_params(**{field: value})
+    h = C.c_void_p()
+    assert lib.usgb_two_medium_create(C.byref(p), C.byref(h)) == status
+    assert msg in lib.usgb_two_medium_last_error(None).decode()
+    assert not h.value

@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libusgb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["usgb_api.cu", "usgb_prep.cu", "usgb_das.cu", "usgb_das_staged.cu", "usgb_das_group.cu",
            "usgb_das_group_f32.cu", "usgb_das_group_f16.cu", "usgb_das_group_bf16.cu", "usgb_post.cu", "usgb_noalloc.cu",
-           "usgb_single.cu"]
+           "usgb_single.cu", "usgb_two_medium.cu"]
 
 
 def nvcc() -> str:
@@ -30,6 +30,7 @@ def nvcc() -> str:
 
 def _flags() -> list[str]:
     return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                   "-Xcompiler", "-ffp-contract=off",
                    "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 

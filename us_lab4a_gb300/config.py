@@ -6,6 +6,7 @@ this library unchanged:
   STAConfiguration                     src/user/configuration/STAConfiguration.h:29-75
   SA3DConfiguration                    src/user/configuration/SA3DConfiguration.h:33-135
   TnRnConfiguration                    src/user/configuration/TnRnConfiguration.h:32-81
+  TwoMediumSTAConfiguration            src/user/configuration/TwoMediumSTAConfiguration.h:29-67
   ArrayUtil::calculateTx3DFocusDelay   src/util/ArrayUtil.h:100-144
   ArrayGeometry::getElementXCentered2D src/util/ArrayGeometry.h:37-49
   ArrayUtil::calculateElementPositions src/util/ArrayUtil.h:51-70
@@ -288,6 +289,41 @@ class TnRnConfiguration:
             propagation_speed=img_pm.value("propagation_speed_1", float, 100.0, 10000.0),
             dead_zone_m=img_pm.value("dead_zone_m", float, 0.0, 50.0e-3),
             num_elements_mux=mux,
+        )
+
+
+@dataclass
+class TwoMediumSTAConfiguration:
+    """STA through an interface into a second medium (linear array)."""
+    num_elements: int
+    num_elements_mux: int
+    pitch: float
+    center_frequency: float
+    propagation_speed_1: float
+    propagation_speed_2: float
+    sampling_frequency: float
+    acquisition_time: float = 1e-4
+    min_gain: float = 0.0
+    max_gain: float = 0.0
+    acquisition_delay: float = 0.0
+    dead_zone_m: float = 0.0
+
+    @classmethod
+    def from_parameter_map(cls, pm: ParameterMap) -> "TwoMediumSTAConfiguration":
+        mux = pm.value("num_elements_mux", int, 1, 1024)
+        return cls(
+            num_elements_mux=mux,
+            num_elements=pm.value("num_elements", int, 1, mux),
+            pitch=pm.value("pitch", float, 0.01e-3, 10.0e-3),
+            center_frequency=pm.value("center_frequency", float, 100.0, 100.0e6),
+            acquisition_time=pm.value("acquisition_time", float, 1.0e-6, 1.0),
+            min_gain=pm.value("min_gain", float, 0.0, 48.0),
+            max_gain=pm.value("max_gain", float, 0.0, 48.0),
+            propagation_speed_1=pm.value("propagation_speed_1", float, 100.0, 10000.0),
+            propagation_speed_2=pm.value("propagation_speed_2", float, 100.0, 10000.0),
+            acquisition_delay=pm.value("acquisition_delay", float, 0.0, 1.0),
+            sampling_frequency=pm.value("sampling_frequency", float, 100.0, 200.0e6),
+            dead_zone_m=pm.value("dead_zone_m", float, 0.0, 50.0e-3),
         )
 
 

@@ -48,6 +48,24 @@ class SingleParams(C.Structure):
     ]
 
 
+class TwoMediumParams(C.Structure):
+    """Mirror of ``usgb_two_medium_params``."""
+    _fields_ = [
+        ("num_elements", C.c_uint32), ("num_elements_mux", C.c_uint32), ("pitch", C.c_float),
+        ("center_frequency", C.c_float), ("propagation_speed_1", C.c_float), ("propagation_speed_2", C.c_float),
+        ("sampling_frequency", C.c_float), ("num_samples", C.c_uint32), ("upsampling", C.c_uint32),
+        ("max_fermat_block_size", C.c_float), ("peak_offset", C.c_float), ("signal_start_offset", C.c_uint32),
+        ("num_acquisitions", C.c_uint32), ("num_tx", C.c_uint32), ("coherence", C.c_uint32),
+        ("pcf_gamma", C.c_float), ("scf_p", C.c_float), ("storage", C.c_uint32), ("storage_scale", C.c_float),
+    ]
+
+
+class TwoMediumStep(C.Structure):
+    """Mirror of ``usgb_two_medium_step``."""
+    _fields_ = [("base_elem_idx", C.c_uint32), ("base_elem", C.c_uint32), ("first_tx_elem", C.c_uint32),
+                ("last_tx_elem", C.c_uint32)]
+
+
 class BatchItem(C.Structure):
     """Mirror of ``usgb_batch_item``."""
     _fields_ = [("ctx", C.c_void_p), ("d_rf", C.c_void_p), ("d_value", C.c_void_p), ("d_factor", C.c_void_p)]
@@ -86,6 +104,16 @@ SIGNATURES = {
     "usgb_single_process_window": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, _FP, _FP]),
     "usgb_single_process_window_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]),
     "usgb_single_synchronize": (C.c_int, [C.c_void_p]),
+    "usgb_two_medium_create": (C.c_int, [C.POINTER(TwoMediumParams), C.POINTER(C.c_void_p)]),
+    "usgb_two_medium_destroy": (None, [C.c_void_p]),
+    "usgb_two_medium_last_error": (C.c_char_p, [C.c_void_p]),
+    "usgb_two_medium_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "usgb_two_medium_process": (C.c_int, [C.c_void_p, _FP, C.POINTER(TwoMediumStep), C.c_uint32, _FP, C.c_uint32,
+                                          _FP, _FP, C.c_uint32, C.c_uint32, _FP]),
+    "usgb_two_medium_process_device": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(TwoMediumStep), C.c_uint32,
+                                                 C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                                 C.c_uint32, C.c_void_p]),
+    "usgb_two_medium_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_post_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
     "usgb_post_destroy": (None, [C.c_void_p]),
     "usgb_post_last_error": (C.c_char_p, [C.c_void_p]),
