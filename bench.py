@@ -333,6 +333,11 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         single = run_single(dev)
 
+    two_medium = None
+    if world == 1 and not args.no_two_medium:
+        torch.cuda.empty_cache()
+        two_medium = run_two_medium(dev)
+
     if rank == 0:
         fps = world * args.steps / (total_ms * 1e-3)
         line = {
@@ -354,7 +359,7 @@ def run_gpu(args):
                          "algorithmic_bytes": top[2]},
             "das_gathers_per_s": gathers / (das_ms * 1e-3),
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
-            "mixed": mixed, "single": single,
+            "mixed": mixed, "single": single, "two_medium": two_medium,
         }
         print(json.dumps(line), flush=True)
     eng.close()
@@ -630,6 +635,87 @@ def run_single(dev, reps: int = 20):
     return out
 
 
+_TM_ORACLE = {}   # one_tx -> (FP64 oracle image of the sampled columns, CPU seconds per frame)
+
+
+def _two_medium_case(dev, one_tx: bool, storage: str, reps: int, threads: int):
+    """Two-medium imaging of the cylinder scene: GPU frames/s with the RF
+    resident, error against the FP64 oracle on 8 columns, and the FP32 oracle
+    (its fixed preparation cost plus the per-column cost scaled to the grid)
+    as the CPU baseline."""
+    import oracle
+    import torch
+    from us_lab4a_gb300 import TwoMediumEngine, TwoMediumSTAConfiguration, workloads
+    sc = workloads.two_medium_scene(one_tx)
+    cfg = TwoMediumSTAConfiguration(num_elements=sc.num_elements, num_elements_mux=sc.num_elements_mux,
+                                    pitch=sc.pitch, center_frequency=sc.center_frequency,
+                                    propagation_speed_1=sc.propagation_speed_1,
+                                    propagation_speed_2=sc.propagation_speed_2,
+                                    sampling_frequency=sc.sampling_frequency)
+    eng = TwoMediumEngine(cfg, sc.rf.shape[0], sc.rf.shape[1], sc.num_samples, sc.upsampling, coherence="pcf",
+                          max_fermat_block_size=sc.max_fermat_block_size, peak_offset=sc.peak_offset,
+                          signal_start_offset=sc.signal_start_offset, storage=storage)
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float32), device=dev)
+    rf, ifxz, apod, grid = t(sc.rf), t(sc.interface_xz), t(sc.rx_apod), t(sc.grid_xz)
+    ncols, nrows = sc.grid_xz.shape[:2]
+    out = torch.empty((ncols, nrows, 2), device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            eng.process_device(rf, sc.steps, ifxz, apod, grid, out)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            eng.process_device(rf, sc.steps, ifxz, apod, grid, out)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    img = out.cpu().numpy().view(np.complex64)[..., 0]
+    eng.close()
+    spec = oracle.TwoMediumSpec(
+        num_elements=sc.num_elements, num_elements_mux=sc.num_elements_mux, pitch=sc.pitch,
+        center_frequency=sc.center_frequency, propagation_speed_1=sc.propagation_speed_1,
+        propagation_speed_2=sc.propagation_speed_2, sampling_frequency=sc.sampling_frequency,
+        num_samples=sc.num_samples, upsampling=sc.upsampling, steps=sc.steps, interface_xz=sc.interface_xz,
+        rx_apod=sc.rx_apod, max_fermat_block_size=sc.max_fermat_block_size, peak_offset=sc.peak_offset,
+        signal_start_offset=sc.signal_start_offset, cf=1, pcf_gamma=1.0, nthreads=threads)
+    cols = np.linspace(0, ncols - 1, 8).astype(int)
+    sub = sc.grid_xz[cols]
+    if one_tx not in _TM_ORACLE:
+        ref64 = oracle.two_medium(spec, sc.rf, sub, dtype=np.float64)
+        t0 = time.perf_counter()
+        oracle.two_medium(spec, sc.rf, sc.grid_xz[:1, :2], dtype=np.float32)   # preparation (+ 2 points)
+        t_prep = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle.two_medium(spec, sc.rf, sub, dtype=np.float32)
+        t_cols = max(time.perf_counter() - t0 - t_prep, 1e-9) / len(cols)
+        _TM_ORACLE[one_tx] = (ref64, t_prep + t_cols * ncols)
+    ref64, cpu_frame = _TM_ORACLE[one_tx]
+    err_db = _db(float(np.abs(img[cols] - ref64).max()), float(np.abs(ref64).max()))
+    gathers = int(sum((s[3] - s[2] + 1) for s in sc.steps)) * sc.num_elements * ncols * nrows
+    return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "gathers_per_s": gathers / (ms * 1e-3),
+            "err_db_vs_fp64": err_db,
+            "cpu_oracle": {"frames_per_s": 1.0 / cpu_frame, "cores": threads, "kind": "port",
+                           "sample": f"FP32 oracle: preparation of the {int(np.prod(sc.rf.shape[:3]))} A-scans and "
+                                     f"{len(cols)} of {ncols} columns, scaled to the grid"}}
+
+
+def run_two_medium(dev, reps: int = 10):
+    """Two-medium imaging (VectorialCombinedTwoMediumImagingProcessor), PCF."""
+    threads = os.cpu_count() or 1
+    out = {"workload": ("cylinder scene: 64-element linear array (pitch 0.6 mm) in water (1480 m/s) over a "
+                        "2700 m/s cylinder (radius 15 mm, top at 15 mm, interface sampled every lambda/4 over "
+                        "-170..-10 degrees: 312 points); 32-element sub-aperture in 8 steps, one transmit element "
+                        "(onetx) or STA (32 x 32) per step; 2000 samples @40 MHz, 4x, PCF; grid 128 x 256 "
+                        "(x -8..8 mm, z 14..40 mm); RF resident; delay search, preparation and image per frame")}
+    for one_tx in (True, False):
+        for storage in ("f32", "f16"):
+            out[("onetx" if one_tx else "sta") + "_" + storage] = _two_medium_case(dev, one_tx, storage, reps, threads)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -648,6 +734,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the 48-frame mixed-size / serving section")
     ap.add_argument("--no-single", action="store_true", help="skip the single-term 3D processor section")
+    ap.add_argument("--no-two-medium", action="store_true", help="skip the two-medium imaging section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

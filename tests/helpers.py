@@ -48,7 +48,10 @@ def run_device(spec, rf, grid_xyz, device="cuda:0", variant=None):
 
 
 def rel_err(a, b) -> float:
-    return float(np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)).max() / np.abs(b).max())
+    """max |a - b| / max |b|, for real or complex images."""
+    a, b = np.asarray(a), np.asarray(b)
+    t = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    return float(np.abs(a.astype(t) - b.astype(t)).max() / np.abs(b.astype(t)).max())
 
 
 def db_err(a, b) -> float:

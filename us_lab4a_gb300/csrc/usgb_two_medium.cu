@@ -12,8 +12,9 @@
 // column, the medium-1 path table (element x interface point), the delay
 // table (one thread per column and element walks down the column, each row's
 // search starting at the previous row's interface point) and the image (one
-// thread per grid point, gathering over every step's transmit x receive pairs
-// from the table). Every delay is rounded as the reference's float arithmetic
+// thread per grid point and step, gathering over the step's transmit x
+// receive pairs from the table; the warps of a block take different steps of
+// the same 32 points). Every delay is rounded as the reference's float arithmetic
 // (no contraction, IEEE division and square root), so the searches pick the
 // same interface points and each gather reads the same samples with the same
 // weight; terms are summed in the reference's order.
@@ -203,7 +204,9 @@ __global__ void __launch_bounds__(kTmThreads) tm_delay_kernel(const __grid_const
 			}
 		}
 		out[r0] = __fmul_rn(tMin, p.fsUp);
-		last = idxMin;
+		// No finite travel time (NaN coordinates): walk from point 0 rather
+		// than from the search's "none" marker.
+		last = idxMin < p.nIf ? idxMin : 0U;
 	}
 	const float* m1 = p.medium1 + static_cast<size_t>(elem) * p.nIf;
 	for (unsigned row = r0 + 1U; row < p.nrows; ++row) {
@@ -249,78 +252,100 @@ __device__ __forceinline__ float2 interp(const typename Complex<S>::T* row, floa
 	return v;
 }
 
-// One thread per grid point (warps along the rows of a column, so the delay
-// table reads are coalesced). ONE_TX: every step transmits from one element
-// (ProcessColumnWithOneTxElem); else STA steps (ProcessColumn).
+// One step's contribution at one grid point: the apodized sum over the
+// receive elements (each the sum over the step's transmit elements, or the
+// single transmit element's term), weighted by the coherence factor of the
+// receive terms. ONE_TX: ProcessColumnWithOneTxElem; else ProcessColumn.
 template<int S, int CF, bool ONE_TX>
-__global__ void __launch_bounds__(kTmThreads) tm_image_kernel(const __grid_constant__ TmParams p)
+__device__ __forceinline__ float2 step_contribution(const TmParams& p, const uint4 st, const float* drow, size_t nr)
 {
 	using CT = typename Complex<S>::T;
-	const unsigned row = blockIdx.x * blockDim.x + threadIdx.x;
-	const unsigned col = blockIdx.y;
-	if (row >= p.nrows) return;
-	const size_t pix = static_cast<size_t>(col) * p.nrows + row;
-	if (row < p.minRow[col]) {
-		p.out[pix] = make_float2(0.f, 0.f);
-		return;
-	}
 	const unsigned maxPos = p.L - 2U;
+	const float* d = drow + st.y * nr;  // element baseElem + e at d[e * nr]
+	const CT* acq = static_cast<const CT*>(p.sig) + st.x * p.acqStride;
+	CFState<CF> cf;
+	float2 sum = make_float2(0.f, 0.f);
+	if (ONE_TX) {
+		const float txOffset = __fadd_rn(p.signalOffset, d[st.z * nr]);
+		for (unsigned rx = 0; rx < p.numElements; ++rx) {
+			const float2 term = interp<S>(acq + rx * p.sigStride, __fadd_rn(txOffset, d[rx * nr]), maxPos, p.invScale);
+			const float a = __ldg(&p.apod[rx]);
+			sum.x = __fadd_rn(sum.x, __fmul_rn(term.x, a));
+			sum.y = __fadd_rn(sum.y, __fmul_rn(term.y, a));
+			cf.add(term);
+		}
+	} else {
+		for (unsigned rx = 0; rx < p.numElements; ++rx) {
+			const float rxDelay = d[rx * nr];
+			float2 acc = make_float2(0.f, 0.f);
+			const CT* sigRx = acq + rx * p.sigStride;
+#pragma unroll 4
+			for (unsigned tx = st.z; tx <= st.w; ++tx) {
+				const float txOffset = __fadd_rn(p.signalOffset, d[tx * nr]);
+				const float2 term = interp<S>(sigRx + (tx - st.z) * p.txStride, __fadd_rn(txOffset, rxDelay), maxPos,
+						p.invScale);
+				acc.x = __fadd_rn(acc.x, term.x);
+				acc.y = __fadd_rn(acc.y, term.y);
+			}
+			const float a = __ldg(&p.apod[rx]);
+			sum.x = __fadd_rn(sum.x, __fmul_rn(acc.x, a));
+			sum.y = __fadd_rn(sum.y, __fmul_rn(acc.y, a));
+			cf.add(acc);
+		}
+	}
+	if (CF != usgb::CF_NONE) {
+		const float f = cf.result(p.numElements, p, sum);
+		return make_float2(__fmul_rn(sum.x, f), __fmul_rn(sum.y, f));
+	}
+	return sum;
+}
+
+// A block covers kTmRows consecutive rows of one column (the lanes of a
+// warp, so the delay-table reads are coalesced) for kTmStepLanes steps at a
+// time (one warp per step); the steps' contributions meet in shared memory
+// and are added in step order, as the reference adds them.
+constexpr unsigned kTmRows = 32;
+constexpr unsigned kTmStepLanes = 8;
+constexpr int kTmImageThreads = kTmRows * kTmStepLanes;
+
+template<int S, int CF, bool ONE_TX>
+__global__ void __launch_bounds__(kTmImageThreads, 4) tm_image_kernel(const __grid_constant__ TmParams p)
+{
+	__shared__ float2 contrib[kTmStepLanes][kTmRows];
+	const unsigned lane = threadIdx.x % kTmRows, sl = threadIdx.x / kTmRows;
+	const unsigned row = blockIdx.x * kTmRows + lane;
+	const unsigned col = blockIdx.y;
+	const bool inGrid = row < p.nrows;
+	const bool active = inGrid && row >= p.minRow[col];
 	const size_t nr = p.nrows;
 	const float* drow = p.delay + static_cast<size_t>(col) * p.mux * nr + row;
 	float2 v = make_float2(0.f, 0.f);
-	for (unsigned s = 0; s < p.numSteps; ++s) {
-		const uint4 st = p.steps[s];
-		const float* d = drow + st.y * nr;  // element baseElem + e at d[e * nr]
-		const CT* acq = static_cast<const CT*>(p.sig) + st.x * p.acqStride;
-		CFState<CF> cf;
-		float2 sum = make_float2(0.f, 0.f);
-		if (ONE_TX) {
-			const float txOffset = __fadd_rn(p.signalOffset, d[st.z * nr]);
-			for (unsigned rx = 0; rx < p.numElements; ++rx) {
-				const float2 term = interp<S>(acq + rx * p.sigStride, __fadd_rn(txOffset, d[rx * nr]), maxPos, p.invScale);
-				const float a = __ldg(&p.apod[rx]);
-				sum.x = __fadd_rn(sum.x, __fmul_rn(term.x, a));
-				sum.y = __fadd_rn(sum.y, __fmul_rn(term.y, a));
-				cf.add(term);
-			}
-		} else {
-			for (unsigned rx = 0; rx < p.numElements; ++rx) {
-				const float rxDelay = d[rx * nr];
-				float2 acc = make_float2(0.f, 0.f);
-				const CT* sigRx = acq + rx * p.sigStride;
-				for (unsigned tx = st.z; tx <= st.w; ++tx) {
-					const float txOffset = __fadd_rn(p.signalOffset, d[tx * nr]);
-					const float2 term = interp<S>(sigRx + (tx - st.z) * p.txStride, __fadd_rn(txOffset, rxDelay), maxPos,
-							p.invScale);
-					acc.x = __fadd_rn(acc.x, term.x);
-					acc.y = __fadd_rn(acc.y, term.y);
-				}
-				const float a = __ldg(&p.apod[rx]);
-				sum.x = __fadd_rn(sum.x, __fmul_rn(acc.x, a));
-				sum.y = __fadd_rn(sum.y, __fmul_rn(acc.y, a));
-				cf.add(acc);
+	for (unsigned s0 = 0; s0 < p.numSteps; s0 += kTmStepLanes) {
+		const unsigned s = s0 + sl;
+		float2 c = make_float2(0.f, 0.f);
+		if (active && s < p.numSteps) c = step_contribution<S, CF, ONE_TX>(p, p.steps[s], drow, nr);
+		contrib[sl][lane] = c;
+		__syncthreads();
+		if (sl == 0 && active) {
+			const unsigned n = min(kTmStepLanes, p.numSteps - s0);
+			for (unsigned k = 0; k < n; ++k) {
+				v.x = __fadd_rn(v.x, contrib[k][lane].x);
+				v.y = __fadd_rn(v.y, contrib[k][lane].y);
 			}
 		}
-		if (CF != usgb::CF_NONE) {
-			const float f = cf.result(p.numElements, p, sum);
-			v.x = __fadd_rn(v.x, __fmul_rn(sum.x, f));
-			v.y = __fadd_rn(v.y, __fmul_rn(sum.y, f));
-		} else {
-			v.x = __fadd_rn(v.x, sum.x);
-			v.y = __fadd_rn(v.y, sum.y);
-		}
+		__syncthreads();
 	}
-	p.out[pix] = v;
+	if (sl == 0 && inGrid) p.out[static_cast<size_t>(col) * nr + row] = active ? v : make_float2(0.f, 0.f);
 }
 
 template<int S, int CF>
 cudaError_t launch_image_cf(const TmParams& p, bool oneTx, cudaStream_t st)
 {
-	const dim3 grid((p.nrows + kTmThreads - 1) / kTmThreads, p.ncols);
+	const dim3 grid((p.nrows + kTmRows - 1) / kTmRows, p.ncols);
 	if (oneTx) {
-		tm_image_kernel<S, CF, true><<<grid, kTmThreads, 0, st>>>(p);
+		tm_image_kernel<S, CF, true><<<grid, kTmImageThreads, 0, st>>>(p);
 	} else {
-		tm_image_kernel<S, CF, false><<<grid, kTmThreads, 0, st>>>(p);
+		tm_image_kernel<S, CF, false><<<grid, kTmImageThreads, 0, st>>>(p);
 	}
 	return cudaGetLastError();
 }
