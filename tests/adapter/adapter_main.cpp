@@ -15,11 +15,15 @@
 #include "SA3DConfiguration.h"
 #include "STAAcquisition.h"
 #include "STAConfiguration.h"
+#include "Tensor3.h"
 #include "TnRnAcquisition.h"
 #include "TnRnConfiguration.h"
+#include "TwoMediumSTAConfiguration.h"
+#include "XZ.h"
 #include "Util.h"
 #include "XYZValueFactor.h"
 #include "usgb_single_processor.hpp"
+#include "usgb_two_medium_processor.hpp"
 #include "usgb_sta_processor.hpp"
 
 using namespace Lab;
@@ -216,5 +220,40 @@ int main()
 		p.process(0, 2, grid);
 		if (grid(0, 0).y != 1e-4f) throw std::runtime_error("center y not written");
 	});
+	// Two-medium imaging.
+	auto two_medium = [&](const char* name, unsigned firstTx, unsigned lastTx, std::size_t nIf) {
+		run_case(name, [&] {
+			TwoMediumSTAConfiguration<float> c;
+			c.numElements = 8;
+			c.numElementsMux = 16;
+			c.pitch = 0.6e-3f;
+			c.centerFrequency = 5e6f;
+			c.acquisitionTime = 1e-4f;
+			c.minGain = c.maxGain = 0;
+			c.propagationSpeed1 = 1480.0f;
+			c.propagationSpeed2 = 2700.0f;
+			c.acquisitionDelay = 0;
+			c.samplingFrequency = 20e6f;
+			c.deadZoneM = 0;
+			std::vector<Tensor3<float>> acq(2);
+			for (auto& t : acq) {
+				t.resize(lastTx - firstTx + 1, 8, 400);
+				for (auto& v : t) v = 0.0f;
+			}
+			VectorialCombinedTwoMediumImagingGB300Processor p(c, acq, 4, noCF, 2.0f, 1.5f, 0);
+			std::vector<VectorialCombinedTwoMediumImagingGB300Processor::StepConfiguration> steps = {
+				{0, 0, firstTx, lastTx}, {1, 8, firstTx, lastTx}};
+			std::vector<XZ<float>> iface;
+			for (std::size_t i = 0; i < nIf; ++i) iface.push_back(XZ<float>(-5e-3f + 1e-4f * i, 8e-3f));
+			std::vector<float> apodTm(8, 1.0f);
+			Matrix<XZ<float>> grid(4, 8);
+			for (unsigned i = 0; i < 4; ++i)
+				for (unsigned j = 0; j < 8; ++j) { grid(i, j).x = 1e-3f * i; grid(i, j).z = 6e-3f + 1e-3f * j; }
+			Matrix<std::complex<float>> value(4, 8);
+			p.process(steps, iface, apodTm, grid, value);
+		});
+	};
+	two_medium("two_medium_frame", 0, 7, 100);
+	two_medium("two_medium_onetx_frame", 3, 3, 100);
 	return 0;
 }

@@ -1,5 +1,5 @@
 """The C++ drop-in processors (include/usgb_sta_processor.hpp,
-include/usgb_single_processor.hpp) compile inside
+include/usgb_single_processor.hpp, include/usgb_two_medium_processor.hpp) compile inside
 the reference's own headers, link libusgb.so, run through the reference's
 ArrayProcessor interface and rethrow library errors as the reference's
 exception types. Needs the reference sources (present where the fixtures are
@@ -39,7 +39,7 @@ def test_adapter_compiles_in_reference_tree_and_maps_errors(tmp_path):
     assert "tnrn_no_delays InvalidStateException Empty tx delay list." in out
     assert "tnrn_dead_zone InvalidValueException" in out and "deadZoneSamplesUp_" in out
     import torch
-    for case in ("frame", "saft_frame", "tnrn_frame", "synthy_frame"):
+    for case in ("frame", "saft_frame", "tnrn_frame", "synthy_frame", "two_medium_frame", "two_medium_onetx_frame"):
         if torch.cuda.is_available():
             assert f"\n{case} ok" in "\n" + out, out
         else:
