@@ -427,6 +427,26 @@ int usgb_two_medium_process_device(usgb_two_medium* tm, const float* d_rf, const
 		const float* d_grid_xz, uint32_t ncols, uint32_t nrows, float* d_value);
 int usgb_two_medium_synchronize(usgb_two_medium* tm);
 
+/*
+ * Saved acquisitions and images: the HDF5 files the reference reads and
+ * writes through HDF5Util::load / HDF5Util::save (src/util/HDF5Util.h:181-287):
+ * SavedSTAAcquisition's "signal" datasets (FileUtil::txElemSignalsPath,
+ * src/util/FileUtil.cpp:58-65: <dir>/signals-base%04u-tx%04u.h5, num_rx rows of
+ * num_samples) and Project::saveImageToHDF5 / saveFactorToHDF5 images
+ * (image_value.h5 "value", image_factor.h5 "factor", src/Project.h:106-113).
+ * Reads HDF5 files of superblock versions 0 and 1 (what libhdf5 writes by
+ * default) with one rank-1 or rank-2 32/64-bit floating-point dataset per
+ * name, contiguous, compact or chunked, with the shuffle, deflate, LZF and
+ * Fletcher-32 filters; writes one contiguous IEEE 64-bit little-endian
+ * rank-2 dataset per file. Values are row-major (n1 rows of n2); a rank-1
+ * dataset reads as n1 = 1. Host only; no GPU needed. Errors: the message is
+ * in usgb_h5_last_error() (this thread).
+ */
+const char* usgb_h5_last_error(void);
+int usgb_h5_dataset_info(const char* path, const char* dataset, uint32_t* rank, uint64_t* n1, uint64_t* n2);
+int usgb_h5_read_f64(const char* path, const char* dataset, double* out, size_t capacity, uint64_t* n1, uint64_t* n2);
+int usgb_h5_write_f64(const char* path, const char* dataset, const double* data, uint64_t n1, uint64_t n2);
+
 /* Library version string. */
 const char* usgb_version(void);
 

@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libusgb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["usgb_api.cu", "usgb_prep.cu", "usgb_das.cu", "usgb_das_staged.cu", "usgb_das_group.cu",
            "usgb_das_group_f32.cu", "usgb_das_group_f16.cu", "usgb_das_group_bf16.cu", "usgb_post.cu", "usgb_noalloc.cu",
-           "usgb_single.cu", "usgb_two_medium.cu"]
+           "usgb_single.cu", "usgb_two_medium.cu", "usgb_h5.cpp"]
 
 
 def nvcc() -> str:

@@ -114,6 +114,12 @@ SIGNATURES = {
                                                  C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
                                                  C.c_uint32, C.c_void_p]),
     "usgb_two_medium_synchronize": (C.c_int, [C.c_void_p]),
+    "usgb_h5_last_error": (C.c_char_p, []),
+    "usgb_h5_dataset_info": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint64)]),
+    "usgb_h5_read_f64": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.c_size_t,
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "usgb_h5_write_f64": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), C.c_uint64, C.c_uint64]),
     "usgb_post_create": (C.c_int, [C.c_uint32, C.POINTER(C.c_void_p)]),
     "usgb_post_destroy": (None, [C.c_void_p]),
     "usgb_post_last_error": (C.c_char_p, [C.c_void_p]),
