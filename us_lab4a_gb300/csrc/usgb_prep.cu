@@ -25,7 +25,9 @@
 //   pass over digit-reversed pairs (k, M-k), and the inverse is an in-place
 //   decimation-in-time FFT that consumes the digit-reversed order and returns
 //   the imaginary part y[n] in natural order. The real part of the analytic
-//   signal is the DC-free input itself, recomputed at store time.
+//   signal is the DC-free input itself: the DC-removal pass writes it to the
+//   output (before the FFT overwrites it in shared memory), the last pass the
+//   imaginary part.
 // * Each butterfly reads one twiddle W_Ms^j and forms its powers in
 //   registers: the first stage from a two-level table (W^m = hi[m / 128] *
 //   lo[m % 128]), later stages from per-stage tables indexed by j, so that
@@ -202,20 +204,6 @@ template<int SIGN> struct SmallDFT<6, SIGN> {
 template<int SIGN> struct SmallDFT<9, SIGN> {
 	static __device__ __forceinline__ void run(float2* v) { composite_dft<3, 3, SIGN>(v); }
 };
-
-// Bit patterns of one stored complex sample as 32-bit words (no address-of,
-// so the values stay in registers).
-__device__ __forceinline__ void sample_words(float2 c, unsigned* w) { w[0] = __float_as_uint(c.x); w[1] = __float_as_uint(c.y); }
-__device__ __forceinline__ void sample_words(__half2 c, unsigned* w)
-{
-	w[0] = static_cast<unsigned>(__half_as_ushort(__low2half(c))) |
-			(static_cast<unsigned>(__half_as_ushort(__high2half(c))) << 16);
-}
-__device__ __forceinline__ void sample_words(__nv_bfloat162 c, unsigned* w)
-{
-	w[0] = static_cast<unsigned>(__bfloat16_as_ushort(__low2bfloat16(c))) |
-			(static_cast<unsigned>(__bfloat16_as_ushort(__high2bfloat16(c))) << 16);
-}
 
 // W^m from the two-level table in shared memory.
 __device__ __forceinline__ float2 twiddle(const float2* lo, const float2* hi, unsigned m)
@@ -501,73 +489,49 @@ __device__ float fir_pass(const PrepParams& p, const float* rfs, const float* ta
 	return part;
 }
 
-// Store pass: (x[n] - mean, y[n] / M) for n < L (analytic), or x[n] - mean (real).
-template<int S, bool ANALYTIC, int NT, int U>
-__device__ void store_pass(const PrepParams& p, const float* rfs, const float* taps, const float* ys, float mean,
-		unsigned a)
+// One component (c = 0: real, 1: imaginary) of complex output sample n,
+// rounded as Complex<S>::pack rounds it.
+template<int S>
+__device__ __forceinline__ void store_component(typename Complex<S>::T* out, size_t n, int c, float v)
 {
-	const float invM = ANALYTIC ? 1.0f / static_cast<float>(p.M) : 0.f;
+	if constexpr (S == STORE_F16) {
+		reinterpret_cast<__half*>(out)[2 * n + c] = __float2half_rn(v);
+	} else if constexpr (S == STORE_BF16) {
+		reinterpret_cast<__nv_bfloat16*>(out)[2 * n + c] = __float2bfloat16_rn(v);
+	} else {
+		reinterpret_cast<float*>(out)[2 * n + c] = v;
+	}
+}
+
+// Imaginary parts y[n] / M of the analytic output (the real parts were
+// written by the DC-removal pass).
+template<int S>
+__device__ void store_imag_pass(const PrepParams& p, const float* ys, unsigned a)
+{
+	using CT = typename Complex<S>::T;
+	CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+	const float invM = 1.0f / static_cast<float>(p.M);
 	const float sc = p.outScale;
-	if (ANALYTIC) {
-		using CT = typename Complex<S>::T;
-		CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
-		if constexpr (NT > 0) {
-			for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
-				float o[U];
-				fir_outputs<NT, U>(rfs, taps, b, o);
-				// y[bU .. bU + U) as 16-byte loads (scalar loads at the U-float
-				// lane stride would conflict U-fold in the banks).
-				float y[U];
-				if constexpr (U % 4 == 0) {
+	for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) store_component<S>(out, n, 1, ys[n] * invM * sc);
+}
+
+// Store pass of the real-RF path: x[n] - mean, with x recomputed from the A-scan.
+template<int S, int NT, int U>
+__device__ void store_real_pass(const PrepParams& p, const float* rfs, const float* taps, float mean, unsigned a)
+{
+	const float sc = p.outScale;
+	using RT = typename Real<S>::T;
+	RT* out = reinterpret_cast<RT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+	if constexpr (NT > 0) {
+		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
+			float o[U];
+			fir_outputs<NT, U>(rfs, taps, b, o);
 #pragma unroll
-					for (int r = 0; r < U; r += 4) {
-						const float4 t = *reinterpret_cast<const float4*>(ys + b * U + r);
-						y[r] = t.x;
-						y[r + 1] = t.y;
-						y[r + 2] = t.z;
-						y[r + 3] = t.w;
-					}
-				} else {
-#pragma unroll
-					for (int r = 0; r < U; ++r) y[r] = ys[b * U + r];
-				}
-				constexpr int perVec = 16 / static_cast<int>(sizeof(CT));  // samples per 16-byte store
-				if constexpr (U % perVec == 0) {
-#pragma unroll
-					for (int r0 = 0; r0 < U; r0 += perVec) {
-						unsigned w[4];
-#pragma unroll
-						for (int j = 0; j < perVec; ++j) {
-							const CT c = Complex<S>::pack((o[r0 + j] - mean) * sc, y[r0 + j] * invM * sc);
-							sample_words(c, w + j * (sizeof(CT) / 4));
-						}
-						*reinterpret_cast<uint4*>(out + b * U + r0) = make_uint4(w[0], w[1], w[2], w[3]);
-					}
-				} else {
-#pragma unroll
-					for (int r = 0; r < U; ++r) out[b * U + r] = Complex<S>::pack((o[r] - mean) * sc, y[r] * invM * sc);
-				}
-			}
-		} else {
-			for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
-				const float x = fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride);
-				out[n] = Complex<S>::pack((x - mean) * sc, ys[n] * invM * sc);
-			}
+			for (int r = 0; r < U; ++r) out[b * U + r] = Real<S>::pack((o[r] - mean) * sc);
 		}
 	} else {
-		using RT = typename Real<S>::T;
-		RT* out = reinterpret_cast<RT*>(p.out) + static_cast<size_t>(a) * p.outStride;
-		if constexpr (NT > 0) {
-			for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
-				float o[U];
-				fir_outputs<NT, U>(rfs, taps, b, o);
-#pragma unroll
-				for (int r = 0; r < U; ++r) out[b * U + r] = Real<S>::pack((o[r] - mean) * sc);
-			}
-		} else {
-			for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
-				out[n] = Real<S>::pack((fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride) - mean) * sc);
-			}
+		for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) {
+			out[n] = Real<S>::pack((fir_one(rfs, taps, n, p.U, p.tapsPerPhase, p.tapsStride) - mean) * sc);
 		}
 	}
 }
@@ -597,10 +561,19 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	const float part = fir_pass<NT, U>(p, rfs, taps, xs);
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
 	//    (block_sum's barriers also order the writes above).
+	//    The real parts of the output, (x[n] - mean) * scale, are stored here
+	//    (the FFT overwrites x); the imaginary parts follow in step 6.
 	float mean = 0.f;
 	if constexpr (!ENV) {
 		mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
-		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) xs[n] -= mean;
+		using CT = typename Complex<S>::T;
+		CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+		const float sc = p.outScale;
+		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) {
+			const float d = xs[n] - mean;
+			xs[n] = d;
+			store_component<S>(out, n, 0, d * sc);
+		}
 	}
 	__syncthreads();
 
@@ -631,7 +604,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	// 5. Inverse FFT (natural-order output: y[n] * M at float index n).
 	fft_run<true>(data, p, twLo, twHi, stw);
 
-	// 6. Store (x[n] - mean, y[n]) for n < L; x is recomputed from the A-scan.
+	// 6. Store y[n] / M for n < L (the real parts were stored in step 2).
 	if constexpr (ENV) {
 		// |x[n] + i y[n]| (the input itself is the real part).
 		const float invM = 1.0f / static_cast<float>(p.M);
@@ -642,7 +615,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 			out[n] = sqrtf(x * x + y * y);
 		}
 	} else {
-		store_pass<S, true, NT, U>(p, rfs, taps, xs, mean, a);
+		store_imag_pass<S>(p, xs, a);
 	}
 	__syncthreads();  // shared memory is reused by the next A-scan of a batch
 }
@@ -655,7 +628,7 @@ __device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
 	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
 	const float part = fir_pass<NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr);
 	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
-	store_pass<S, false, NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr, mean, a);
+	store_real_pass<S, NT, U>(p, sm + lay.rfs, sm + lay.taps, mean, a);
 	__syncthreads();
 }
 
