@@ -426,9 +426,14 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	         : group_consume<SP, CF, false>(p, sm, it, px, py, pz, active, pix, fx);
 }
 
-// Resident blocks per SM the register allocation is held to (shared memory
-// permitting): 5 for 4-row tiles (at most 81 registers a thread).
+// Resident blocks per SM the register allocation is held to. One frame: 5
+// for 4-row tiles (at most 81 registers a thread; measured fastest on the
+// 64-element frames even though 32 KiB stages let only 3 blocks in). Batches
+// (every coherence factor in one kernel, more live state): 3 for 4-row tiles
+// and 2 for 8-row tiles, which removes their spills (2-3 KiB a thread at 5
+// and 3).
 template<int TROWS> constexpr int group_min_blocks() { return TROWS == 4 ? 5 : (TROWS == 8 ? 3 : 1); }
+template<int TROWS> constexpr int group_batch_min_blocks() { return TROWS == 4 ? 3 : (TROWS == 8 ? 2 : 1); }
 
 template<int S, int CF, bool ANALYTIC, int TROWS>
 __global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
@@ -496,7 +501,7 @@ __device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, co
 
 // Many frames: persistent blocks walk the tiles of every frame in the batch.
 template<int S, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
+__global__ void __launch_bounds__((TROWS + 1) * 32, group_batch_min_blocks<TROWS>())
 das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
 		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
 {
