@@ -64,9 +64,8 @@ struct usgb_ctx {
 	float* d_apod = nullptr;
 	float* d_polyTaps = nullptr;
 	float2* d_tw = nullptr;
-	float2* d_cs = nullptr;
+	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
-	unsigned* d_perm = nullptr;
 	float* d_rf = nullptr;
 	void* d_sig = nullptr;
 	float* d_grid = nullptr;
@@ -95,7 +94,7 @@ struct usgb_ctx {
 
 	~usgb_ctx()
 	{
-		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_cs, d_stw, d_perm, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
+		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_hilb, d_stw, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
 		for (void* p : dev) if (p) cudaFree(p);
 		if (h_rf) cudaFreeHost(h_rf);
 		if (h_out) cudaFreeHost(h_out);
@@ -155,9 +154,8 @@ void build_tables(usgb_ctx* c)
 		if (!v.empty()) USGB_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice));
 	};
 	upload(&c->d_tw, t.tw);
-	upload(&c->d_cs, t.cs);
+	upload(&c->d_hilb, t.hilb);
 	upload(&c->d_stw, t.stageTw);
-	upload(&c->d_perm, t.perm);
 	c->stageTw = true;  // cleared by check_prep_fits when the tables do not fit
 }
 
@@ -273,8 +271,7 @@ usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
 	if (c->analytic) {
 		usgb::host::set_fft_params(pp, c->fft);
 		pp.tw = c->d_tw;
-		pp.cs = c->d_cs;
-		pp.perm = c->d_perm;
+		pp.hilb = c->d_hilb;
 		pp.stw = c->stageTw ? c->d_stw : nullptr;
 	}
 	return pp;

@@ -10,6 +10,8 @@ namespace usgb {
 constexpr int kPrepThreads = 512;
 constexpr int kMaxFFTStages = 24;
 constexpr unsigned kTwiddleSplit = 128;   // two-level twiddle tables: W^m = hi[m / 128] * lo[m % 128]
+constexpr unsigned kHilbertSkip = 0xFFFFFFFFu;
+constexpr unsigned kHilbertSwap = 0x80000000u;
 // FP32 delays (a sum of two rounded products of rounded distances) are off by
 // at most about 8 * 2^-24 * d samples; above 32768 samples that can exceed
 // 1/64 sample, and the staged kernel switches the tile to FP64 geometry.
@@ -36,9 +38,13 @@ struct PrepParams {
 	unsigned long long divMagic[kMaxFFTStages];  // floor(b / sub_s) = (b * divMagic[s]) >> 40
 	const float2* tw;            // twLo (128) then twHi (ceil(M/128)): exp(-2 pi i m / M)
 	unsigned twHiCount;
-	const float2* cs;            // csLo (128) then csHi: (cos, sin)(pi k / M), k <= M/2
-	unsigned csHiCount;
-	const unsigned* perm;        // M entries, digit-reversed position of bin k
+	// Hilbert pass over the pairs (k, M - k) in digit-reversed position
+	// order: entry p < hilbCount = ((cos, sin)(pi k_lo / M), code, 0) with
+	// code = the partner's position q > p (| kHilbertSwap when p holds M - k_lo
+	// rather than k_lo), p itself for k = 0 and k = M / 2, or kHilbertSkip
+	// when the pair was visited from the partner's lower position.
+	const float4* hilb;
+	unsigned hilbCount;
 	// Per-stage twiddle tables (stage s >= 1: W_Ms^j, j < Ms / radix, at
 	// stw + stwOffset[s]); null when they do not fit in shared memory, and
 	// every stage then reads the two-level table.

@@ -84,7 +84,7 @@ void* scratch_address()
 
 // Byte layout of one call inside the scratch array.
 struct Layout {
-	size_t err, taps, tw, cs, stw, perm, tx, rx, apod, sig, total;
+	size_t err, taps, tw, hilb, stw, tx, rx, apod, sig, total;
 };
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -153,9 +153,8 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	lay.err = off; off = align256(off + sizeof(unsigned));
 	lay.taps = off; off = align256(off + poly.poly.size() * sizeof(float));
 	lay.tw = off; off = align256(off + fft.tw.size() * sizeof(float2));
-	lay.cs = off; off = align256(off + fft.cs.size() * sizeof(float2));
+	lay.hilb = off; off = align256(off + fft.hilb.size() * sizeof(float4));
 	lay.stw = off; off = align256(off + fft.stageTw.size() * sizeof(float2));
-	lay.perm = off; off = align256(off + fft.perm.size() * sizeof(unsigned));
 	lay.tx = off; off = align256(off + 2 * p->num_tx * sizeof(float));
 	lay.rx = off; off = align256(off + 2 * p->num_rx * sizeof(float));
 	lay.apod = off; off = align256(off + apod.size() * sizeof(float));
@@ -173,12 +172,11 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
 	if (analytic) {
 		NA_CUDA(cudaMemcpyAsync(base + lay.tw, fft.tw.data(), fft.tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
-		NA_CUDA(cudaMemcpyAsync(base + lay.cs, fft.cs.data(), fft.cs.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
+		NA_CUDA(cudaMemcpyAsync(base + lay.hilb, fft.hilb.data(), fft.hilb.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
 		if (!fft.stageTw.empty()) {
 			NA_CUDA(cudaMemcpyAsync(base + lay.stw, fft.stageTw.data(), fft.stageTw.size() * sizeof(float2),
 					cudaMemcpyHostToDevice, stream));
 		}
-		NA_CUDA(cudaMemcpyAsync(base + lay.perm, fft.perm.data(), fft.perm.size() * sizeof(unsigned), cudaMemcpyHostToDevice, stream));
 	}
 	NA_CUDA(cudaMemcpyAsync(base + lay.tx, p->tx_xy, 2 * p->num_tx * sizeof(float), cudaMemcpyHostToDevice, stream));
 	NA_CUDA(cudaMemcpyAsync(base + lay.rx, p->rx_xy, 2 * p->num_rx * sizeof(float), cudaMemcpyHostToDevice, stream));
@@ -198,8 +196,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	const float scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
 	pp.outScale = scale;
 	pp.tw = reinterpret_cast<const float2*>(base + lay.tw);
-	pp.cs = reinterpret_cast<const float2*>(base + lay.cs);
-	pp.perm = reinterpret_cast<const unsigned*>(base + lay.perm);
+	pp.hilb = reinterpret_cast<const float4*>(base + lay.hilb);
 	pp.stw = (analytic && !fft.stageTw.empty()) ? reinterpret_cast<const float2*>(base + lay.stw) : nullptr;
 
 	int dev = 0, maxSmem = 0;

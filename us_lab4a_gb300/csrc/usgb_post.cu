@@ -83,9 +83,8 @@ struct usgb_post {
 	usgb::host::FFTTables fft;
 	float* d_taps = nullptr;
 	float2* d_tw = nullptr;
-	float2* d_cs = nullptr;
+	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
-	unsigned* d_perm = nullptr;
 	unsigned* d_max = nullptr;
 	bool stageTw = true;
 	unsigned numSMs = 0;
@@ -93,7 +92,7 @@ struct usgb_post {
 
 	~usgb_post()
 	{
-		void* dev[] = {d_taps, d_tw, d_cs, d_stw, d_perm, d_max};
+		void* dev[] = {d_taps, d_tw, d_hilb, d_stw, d_max};
 		for (void* p : dev) if (p) cudaFree(p);
 	}
 };
@@ -130,8 +129,7 @@ usgb::PrepParams envelope_params(const usgb_post* p, const float* in, float* out
 	pp.outScale = 1.0f;
 	usgb::host::set_fft_params(pp, p->fft);
 	pp.tw = p->d_tw;
-	pp.cs = p->d_cs;
-	pp.perm = p->d_perm;
+	pp.hilb = p->d_hilb;
 	pp.stw = p->stageTw ? p->d_stw : nullptr;
 	return pp;
 }
@@ -163,9 +161,8 @@ int usgb_post_create(uint32_t num_samples, usgb_post** out)
 			if (!v.empty()) POST_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(E), cudaMemcpyHostToDevice));
 		};
 		upload(&p->d_tw, p->fft.tw);
-		upload(&p->d_cs, p->fft.cs);
+		upload(&p->d_hilb, p->fft.hilb);
 		upload(&p->d_stw, p->fft.stageTw);
-		upload(&p->d_perm, p->fft.perm);
 		POST_CUDA(cudaMalloc(&p->d_max, sizeof(unsigned)));
 		int dev = 0, maxSmem = 0, sms = 0;
 		POST_CUDA(cudaGetDevice(&dev));

@@ -19,7 +19,7 @@
 //   convolution the reference computes with an FFT overlap-save filter.
 // * The N-point real FFT of the zero-padded signal is done as an N/2-point
 //   complex FFT of the even/odd-packed samples, in place in shared memory
-//   (mixed radix 2/3/4/5/6/8/9, decimation in frequency, output in digit-reversed
+//   (mixed radix 2/3/4/5/6/8/9/15/16, decimation in frequency, output in digit-reversed
 //   order; the packed buffer read as floats is the signal itself). The
 //   Hilbert multiplier -i*sgn(k) and the real-FFT split are folded into one
 //   pass over digit-reversed pairs (k, M-k), and the inverse is an in-place
@@ -164,6 +164,46 @@ template<> __device__ __forceinline__ float2 root<9>(int m)
 	default: return make_float2(0.76604444311897803520f, -0.64278760968653932632f);
 	}
 }
+// exp(2 pi i m / 15), m < 15: angles of 24 degrees (m > 7: conjugates of 15 - m).
+template<> __device__ __forceinline__ float2 root<15>(int m)
+{
+	const bool lower = m > 7;
+	float c, s;
+	switch (lower ? 15 - m : m) {
+	case 0: c = 1.0f; s = 0.0f; break;
+	case 1: c = 0.91354545764260089550f; s = 0.40673664307580020775f; break;
+	case 2: c = 0.66913060635885821383f; s = 0.74314482547739423501f; break;
+	case 3: c = 0.30901699437494742410f; s = 0.95105651629515357212f; break;
+	case 4: c = -0.10452846326765347140f; s = 0.99452189536827333692f; break;
+	case 5: c = -0.5f; s = 0.86602540378443864676f; break;
+	case 6: c = -0.80901699437494742410f; s = 0.58778525229247312917f; break;
+	default: c = -0.97814760073380563793f; s = 0.20791169081775933710f; break;
+	}
+	return make_float2(c, lower ? -s : s);
+}
+// exp(2 pi i m / 16), m < 16: angles of 22.5 degrees.
+template<> __device__ __forceinline__ float2 root<16>(int m)
+{
+	constexpr float a = 0.92387953251128675613f, b = 0.38268343236508977173f, h = 0.70710678118654752440f;
+	switch (m) {
+	case 0: return make_float2(1.0f, 0.0f);
+	case 1: return make_float2(a, b);
+	case 2: return make_float2(h, h);
+	case 3: return make_float2(b, a);
+	case 4: return make_float2(0.0f, 1.0f);
+	case 5: return make_float2(-b, a);
+	case 6: return make_float2(-h, h);
+	case 7: return make_float2(-a, b);
+	case 8: return make_float2(-1.0f, 0.0f);
+	case 9: return make_float2(-a, -b);
+	case 10: return make_float2(-h, -h);
+	case 11: return make_float2(-b, -a);
+	case 12: return make_float2(0.0f, -1.0f);
+	case 13: return make_float2(b, -a);
+	case 14: return make_float2(h, -h);
+	default: return make_float2(a, -b);
+	}
+}
 // DFT of size R = R1 R2 by the two-factor decomposition: input n = R2 n1 +
 // n2, output k = k1 + R1 k2; R2 DFTs of size R1, internal twiddles
 // W_R^(n2 k1), then R1 DFTs of size R2 (all in registers).
@@ -204,6 +244,12 @@ template<int SIGN> struct SmallDFT<6, SIGN> {
 template<int SIGN> struct SmallDFT<9, SIGN> {
 	static __device__ __forceinline__ void run(float2* v) { composite_dft<3, 3, SIGN>(v); }
 };
+template<int SIGN> struct SmallDFT<15, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<5, 3, SIGN>(v); }
+};
+template<int SIGN> struct SmallDFT<16, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<4, 4, SIGN>(v); }
+};
 
 // W^m from the two-level table in shared memory.
 __device__ __forceinline__ float2 twiddle(const float2* lo, const float2* hi, unsigned m)
@@ -242,19 +288,21 @@ __device__ __forceinline__ void fft_stage(float2* data, const float2* twLo, cons
 		float2 v[R];
 #pragma unroll
 		for (int q = 0; q < R; ++q) v[q] = data[base + q * sub];
+		// The powers of W are formed next to their use (the forward stage
+		// after its DFT), so that the R inputs and R powers are not all live
+		// at once.
 		float2 w[R];
-		if (twiddled) {
-			w[1] = st ? st[j] : twiddle(twLo, twHi, j * twStride);
-			twiddle_powers<R>(w);
-		}
+		if (twiddled) w[1] = st ? st[j] : twiddle(twLo, twHi, j * twStride);
 		if (!INVERSE) {
 			SmallDFT<R, -1>::run(v);
 			if (twiddled) {
+				twiddle_powers<R>(w);
 #pragma unroll
 				for (int q = 1; q < R; ++q) v[q] = cmul(v[q], w[q]);
 			}
 		} else {
 			if (twiddled) {
+				twiddle_powers<R>(w);
 #pragma unroll
 				for (int q = 1; q < R; ++q) v[q] = cmulc(v[q], w[q]);
 			}
@@ -281,7 +329,9 @@ __device__ __noinline__ void fft_run(float2* data, const PrepParams& p, const fl
 		case 5: fft_stage<5, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		case 6: fft_stage<6, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		case 8: fft_stage<8, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
-		default: fft_stage<9, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 9: fft_stage<9, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 15: fft_stage<15, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		default: fft_stage<16, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		}
 		__syncthreads();
 	}
@@ -307,7 +357,7 @@ __device__ float block_sum(float v, float* red)
 
 // Shared-memory layout of the prep kernels (float offsets).
 struct PrepLayout {
-	unsigned data, rfs, taps, twLo, twHi, csLo, csHi, stw, red, total;
+	unsigned data, rfs, taps, twLo, twHi, stw, red, total;
 	__host__ __device__ PrepLayout(const PrepParams& p, bool analytic)
 	{
 		const unsigned K = (p.tapsPerPhase - 1) / 2;
@@ -316,9 +366,7 @@ struct PrepLayout {
 		taps = rfs + ((p.ns + 2 * K + 1 + 3) & ~3u);
 		twLo = taps + p.U * p.tapsStride;
 		twHi = twLo + (analytic ? 2 * kTwiddleSplit : 0);
-		csLo = twHi + (analytic ? 2 * p.twHiCount : 0);
-		csHi = csLo + (analytic ? 2 * kTwiddleSplit : 0);
-		stw = csHi + (analytic ? 2 * p.csHiCount : 0);
+		stw = twHi + (analytic ? 2 * p.twHiCount : 0);
 		red = stw + ((analytic && p.stw) ? 2 * p.stwCount : 0);
 		total = red + 32;
 	}
@@ -342,9 +390,6 @@ __device__ void load_inputs(const PrepParams& p, const PrepLayout& lay, float* s
 		const unsigned ntw = 2 * (kTwiddleSplit + p.twHiCount);
 		const float* twg = reinterpret_cast<const float*>(p.tw);
 		for (unsigned i = threadIdx.x; i < ntw; i += blockDim.x) sm[lay.twLo + i] = __ldg(&twg[i]);
-		const unsigned ncs = 2 * (kTwiddleSplit + p.csHiCount);
-		const float* csg = reinterpret_cast<const float*>(p.cs);
-		for (unsigned i = threadIdx.x; i < ncs; i += blockDim.x) sm[lay.csLo + i] = __ldg(&csg[i]);
 		if (p.stw) {
 			const float* stg = reinterpret_cast<const float*>(p.stw);
 			for (unsigned i = threadIdx.x; i < 2 * p.stwCount; i += blockDim.x) sm[lay.stw + i] = __ldg(&stg[i]);
@@ -551,8 +596,6 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	const float* taps = sm + lay.taps;
 	const float2* twLo = reinterpret_cast<const float2*>(sm + lay.twLo);
 	const float2* twHi = reinterpret_cast<const float2*>(sm + lay.twHi);
-	const float2* csLo = reinterpret_cast<const float2*>(sm + lay.csLo);
-	const float2* csHi = reinterpret_cast<const float2*>(sm + lay.csHi);
 	const float2* stw = p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr;
 	const unsigned L = p.L;
 
@@ -581,23 +624,30 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	fft_run<false>(data, p, twLo, twHi, stw);
 
 	// 4. Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
-	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0.
-	const unsigned half = p.M / 2;
-	for (unsigned k = threadIdx.x; k <= half; k += blockDim.x) {
-		if (k == 0) {
-			data[__ldg(&p.perm[0])] = make_float2(0.f, 0.f);
-		} else if (2 * k == p.M) {
-			const unsigned q = __ldg(&p.perm[k]);
-			const float2 z = data[q];
-			data[q] = make_float2(-z.y, z.x);
-		} else {
-			const unsigned q1 = __ldg(&p.perm[k]);
-			const unsigned q2 = __ldg(&p.perm[p.M - k]);
-			const float2 A = data[q1], B = data[q2];
-			const float2 cs = cmul(csHi[k / kTwiddleSplit], csLo[k % kTwiddleSplit]);
-			data[q1] = make_float2(cs.x * B.x - cs.y * A.y, cs.y * A.x - cs.x * B.y);
-			data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
+	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0,
+	//    visited in digit-reversed position order (both members of
+	//    neighbouring lanes' pairs sit at neighbouring positions).
+	for (unsigned i = threadIdx.x; i < p.hilbCount; i += blockDim.x) {
+		const float4 h = __ldg(&p.hilb[i]);
+		const unsigned code = __float_as_uint(h.z);
+		if (code == kHilbertSkip) continue;
+		if (code == i) {
+			if (i == 0) {
+				data[0] = make_float2(0.f, 0.f);   // k = 0 sits at position 0
+			} else {
+				const float2 z = data[i];          // k = M / 2
+				data[i] = make_float2(-z.y, z.x);
+			}
+			continue;
 		}
+		const unsigned q = code & ~kHilbertSwap;
+		const bool swap = (code & kHilbertSwap) != 0u;
+		const unsigned q1 = swap ? q : i;      // position of k_lo
+		const unsigned q2 = swap ? i : q;      // position of M - k_lo
+		const float2 A = data[q1], B = data[q2];
+		const float2 cs = make_float2(h.x, h.y);
+		data[q1] = make_float2(cs.x * B.x - cs.y * A.y, cs.y * A.x - cs.x * B.y);
+		data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
 	}
 	__syncthreads();
 

@@ -335,9 +335,8 @@ struct usgb_single {
 	float* d_apod = nullptr;
 	float* d_polyTaps = nullptr;
 	float2* d_tw = nullptr;
-	float2* d_cs = nullptr;
+	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
-	unsigned* d_perm = nullptr;
 	float* d_rf = nullptr;
 	void* d_sig = nullptr;
 	float* d_grid = nullptr;
@@ -353,7 +352,7 @@ struct usgb_single {
 	~usgb_single()
 	{
 		if (stream) cudaStreamSynchronize(stream);
-		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_cs, d_stw, d_perm, d_rf, d_sig, d_grid, d_value,
+		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_hilb, d_stw, d_rf, d_sig, d_grid, d_value,
 		               d_factor};
 		for (void* p : dev) if (p) cudaFree(p);
 		if (ownStream && stream) cudaStreamDestroy(stream);
@@ -477,9 +476,8 @@ void build_tables(usgb_single* c)
 	upload(&c->d_polyTaps, poly.poly);
 	if (!usgb::host::make_fft_tables(c->L, c->fft)) SINGLE_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << c->fft.M << " not supported");
 	upload(&c->d_tw, c->fft.tw);
-	upload(&c->d_cs, c->fft.cs);
+	upload(&c->d_hilb, c->fft.hilb);
 	upload(&c->d_stw, c->fft.stageTw);
-	upload(&c->d_perm, c->fft.perm);
 	upload(&c->d_txXY, c->txXY);
 	upload(&c->d_rxXY, c->rxXY);
 	upload(&c->d_apod, c->apod);
@@ -502,8 +500,7 @@ usgb::PrepParams prep_params(const usgb_single* c, const float* d_rf, void* d_ou
 	pp.outScale = c->scale;
 	usgb::host::set_fft_params(pp, c->fft);
 	pp.tw = c->d_tw;
-	pp.cs = c->d_cs;
-	pp.perm = c->d_perm;
+	pp.hilb = c->d_hilb;
 	pp.stw = c->stageTw ? c->d_stw : nullptr;
 	return pp;
 }

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -135,14 +136,54 @@ struct FFTTables {
 	unsigned N = 0, M = 0;
 	std::vector<int> radices;                     // DIF order
 	std::vector<unsigned long long> divMagic;     // per stage: ceil(2^40 / sub)
-	std::vector<float2> tw, cs;                   // two-level tables (lo 128, then hi)
-	unsigned twHiCount = 0, csHiCount = 0;
-	std::vector<unsigned> perm;                   // digit-reversed position of bin k
+	std::vector<float2> tw;                       // two-level table (lo 128, then hi)
+	unsigned twHiCount = 0;
+	// Hilbert pass in digit-reversed position order (kHilbertSkip / the pair
+	// encoding of PrepParams::hilb): entry p < hilb.size() is
+	// (cos, sin)(pi k_lo / M), the partner's position and which of the two
+	// positions holds k_lo, for the pair (k, M - k) whose lower position is p.
+	std::vector<float4> hilb;
 	// Stage tables: for stage s >= 1 (span Ms, radix R), W_Ms^j for j < Ms / R,
 	// at stageTwOffset[s] (stage 0 reads the two-level table).
 	std::vector<float2> stageTw;
 	std::vector<unsigned> stageTwOffset;
 };
+
+// Shared-memory wavefronts of the in-place stages of `plan` over M points,
+// one direction: each warp request (32 consecutive butterflies b of a stage,
+// one of its R float2 loads or stores) costs the largest number of distinct
+// 4-byte words any of the 32 banks holds.
+inline double fft_plan_wavefronts(unsigned M, const std::vector<int>& plan)
+{
+	double total = 0.0;
+	unsigned Ms = M;
+	for (int R : plan) {
+		const unsigned r = static_cast<unsigned>(R);
+		const unsigned sub = Ms / r;
+		const unsigned nb = M / r;
+		for (unsigned w0 = 0; w0 < nb; w0 += 32) {
+			const unsigned n = std::min(32u, nb - w0);
+			for (unsigned q = 0; q < r; ++q) {
+				unsigned words[64];
+				for (unsigned l = 0; l < n; ++l) {
+					const unsigned b = w0 + l;
+					const unsigned blk = b / sub;
+					const unsigned pos = blk * Ms + (b - blk * sub) + q * sub;
+					words[2 * l] = 2 * pos;
+					words[2 * l + 1] = 2 * pos + 1;
+				}
+				std::sort(words, words + 2 * n);
+				const unsigned* end = std::unique(words, words + 2 * n);
+				unsigned banks[32] = {};
+				unsigned worst = 0;
+				for (const unsigned* w = words; w != end; ++w) worst = std::max(worst, ++banks[*w % 32]);
+				total += 2.0 * worst;   // the load and the store
+			}
+		}
+		Ms = sub;
+	}
+	return total;
+}
 
 inline bool make_fft_tables(unsigned L, FFTTables& t)
 {
@@ -155,33 +196,62 @@ inline bool make_fft_tables(unsigned L, FFTTables& t)
 	while (m % 3 == 0) { m /= 3; ++e3; }
 	while (m % 5 == 0) { m /= 5; ++e5; }
 	if (m != 1) return false;
-	// Few passes over the buffer: radix 8 for the power of two (one 4 for a
-	// remainder of 4; a remainder of 2 pairs with a 3 as radix 6), radix 9
-	// for the power of three (a remaining 3 alone), radix 5 for the rest. The
-	// power-of-two radices run first (long blocks), the odd ones last, where
-	// the blocks are short and odd strides keep the shared-memory banks apart.
-	t.radices.clear();
-	for (; e2 >= 3; e2 -= 3) t.radices.push_back(8);
-	if (e2 == 2) { t.radices.push_back(4); e2 = 0; }
+	// Few passes over the buffer (each pass reads and writes every point in
+	// shared memory), without bank conflicts where possible. The odd part:
+	// radix 15 for each 3 * 5 pair, radix 9 for the remaining 3^2, then a 3,
+	// and 5; a single 2 pairs with a leftover 3 as radix 6. The power of two:
+	// every non-increasing sequence of radices 16 / 8 / 4 / 2 with at most
+	// one pass more than the fewest, each plan scored by the shared-memory
+	// wavefronts of its passes (fft_plan_wavefronts); the power-of-two
+	// radices run first (long blocks), the odd ones last, where the blocks are
+	// short and odd strides keep the banks apart (cf2d, M = 17280:
+	// 16 * 8 * 9 * 15, four passes; the first form took eight).
+	std::vector<int> odd;
+	int n15 = std::min(e3, e5);
+	int r3 = e3 - n15, r5 = e5 - n15;
 	bool two = e2 == 1;
-	bool three = (e3 % 2) == 1;
-	if (two && three) { t.radices.push_back(6); two = three = false; }
-	if (two) t.radices.push_back(2);
-	for (int i = 0; i < e3 / 2; ++i) t.radices.push_back(9);
-	if (three) t.radices.push_back(3);
-	for (int i = 0; i < e5; ++i) t.radices.push_back(5);
+	if (two && r3 % 2 == 1) { odd.push_back(6); two = false; --r3; }
+	if (two) odd.push_back(2);
+	for (int i = 0; i < r3 / 2; ++i) odd.push_back(9);
+	if (r3 % 2 == 1) odd.push_back(3);
+	for (int i = 0; i < r5; ++i) odd.push_back(5);
+	for (int i = 0; i < n15; ++i) odd.push_back(15);
+	std::vector<std::vector<int>> pow2;
+	if (e2 > 1) {
+		const int fewest = (e2 + 3) / 4;
+		std::vector<int> cur;
+		// Non-increasing sequences of 2^b (b = 4 .. 1) summing to e2 bits.
+		auto rec = [&](auto&& self, int left, int maxBits) -> void {
+			if (left == 0) { pow2.push_back(cur); return; }
+			if (static_cast<int>(cur.size()) >= fewest + 1) return;
+			for (int bits = std::min(maxBits, left); bits >= 1; --bits) {
+				cur.push_back(1 << bits);
+				self(self, left - bits, bits);
+				cur.pop_back();
+			}
+		};
+		rec(rec, e2, 4);
+	} else {
+		pow2.push_back({});
+	}
+	double best = 0.0;
+	for (const auto& p2 : pow2) {
+		std::vector<int> plan = p2;
+		plan.insert(plan.end(), odd.begin(), odd.end());
+		const double cost = fft_plan_wavefronts(M, plan);
+		if (t.radices.empty() || cost < best || (cost == best && plan.size() < t.radices.size())) {
+			best = cost;
+			t.radices = plan;
+		}
+	}
 	if (t.radices.size() > static_cast<size_t>(kMaxFFTStages)) return false;
 
 	auto unit = [](double a) { return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a))); };
 	const unsigned S = kTwiddleSplit;
 	t.twHiCount = (M + S - 1) / S;
-	t.csHiCount = (M / 2 + 1 + S - 1) / S;
 	t.tw.resize(S + t.twHiCount);
-	t.cs.resize(S + t.csHiCount);
 	for (unsigned j = 0; j < S; ++j) t.tw[j] = unit(-2.0 * kPi * static_cast<double>(j) / M);
 	for (unsigned q = 0; q < t.twHiCount; ++q) t.tw[S + q] = unit(-2.0 * kPi * static_cast<double>(q) * S / M);
-	for (unsigned j = 0; j < S; ++j) t.cs[j] = unit(kPi * static_cast<double>(j) / M);
-	for (unsigned q = 0; q < t.csHiCount; ++q) t.cs[S + q] = unit(kPi * static_cast<double>(q) * S / M);
 
 	// Multiply-shift division by each stage's sub-block length:
 	// floor(b / sub) = (b * ceil(2^40 / sub)) >> 40, exact for b, sub < 2^20.
@@ -200,7 +270,7 @@ inline bool make_fft_tables(unsigned L, FFTTables& t)
 	}
 	// Digit-reversed position of bin k after the in-place DIF stages:
 	// k = k0 + r0 (k1 + r1 (k2 + ...)) sits at sum_s k_s * M / (r0 ... r_s).
-	t.perm.resize(M);
+	std::vector<unsigned> perm(M), binAt(M);
 	for (unsigned k = 0; k < M; ++k) {
 		unsigned kk = k, pos = 0, span = M;
 		for (int r : t.radices) {
@@ -208,7 +278,36 @@ inline bool make_fft_tables(unsigned L, FFTTables& t)
 			pos += (kk % r) * span;
 			kk /= r;
 		}
-		t.perm[k] = pos;
+		perm[k] = pos;
+		binAt[pos] = k;
+	}
+	// Pairs (k, M - k) visited in position order: consecutive lanes then read
+	// consecutive positions, and the partners' positions run consecutively
+	// too (in k order, consecutive bins sit M / r0 apart: every lane on one
+	// shared-memory bank). Each pair is handled from its lower position; the
+	// last such position bounds the table.
+	unsigned count = 0;
+	for (unsigned pos = 0; pos < M; ++pos) {
+		const unsigned q = perm[(M - binAt[pos]) % M];
+		if (q >= pos) count = pos + 1;
+	}
+	t.hilb.assign(count, make_float4(0.f, 0.f, 0.f, 0.f));
+	for (unsigned pos = 0; pos < count; ++pos) {
+		const unsigned k = binAt[pos];
+		const unsigned kp = (M - k) % M;
+		const unsigned q = perm[kp];
+		unsigned code = kHilbertSkip;
+		float2 cs = make_float2(0.f, 0.f);
+		if (q == pos) {
+			code = pos;                        // k = 0 or k = M / 2
+		} else if (q > pos) {
+			const unsigned klo = std::min(k, kp);
+			code = q | ((k == klo) ? 0u : kHilbertSwap);
+			cs = unit(kPi * static_cast<double>(klo) / M);
+		}
+		float codeBits;
+		std::memcpy(&codeBits, &code, sizeof(code));
+		t.hilb[pos] = make_float4(cs.x, cs.y, codeBits, 0.f);
 	}
 	return true;
 }
@@ -224,7 +323,7 @@ inline void set_fft_params(PrepParams& pp, const FFTTables& t)
 		pp.stwOffset[i] = t.stageTwOffset[i];
 	}
 	pp.twHiCount = t.twHiCount;
-	pp.csHiCount = t.csHiCount;
+	pp.hilbCount = static_cast<unsigned>(t.hilb.size());
 	pp.stwCount = static_cast<unsigned>(t.stageTw.size());
 }
 

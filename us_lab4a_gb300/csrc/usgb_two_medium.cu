@@ -421,9 +421,8 @@ struct usgb_two_medium {
 	float scale = 1, pcfFactor = 0, signalOffset = 0;
 	float* d_polyTaps = nullptr;
 	float2* d_tw = nullptr;
-	float2* d_cs = nullptr;
+	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
-	unsigned* d_perm = nullptr;
 	void* d_sig = nullptr;
 	DevBuf<float> rf, grid, iface, apod, medium1, delay, value;
 	DevBuf<unsigned> minRow;
@@ -436,7 +435,7 @@ struct usgb_two_medium {
 	~usgb_two_medium()
 	{
 		if (stream) cudaStreamSynchronize(stream);
-		void* dev[] = {d_polyTaps, d_tw, d_cs, d_stw, d_perm, d_sig};
+		void* dev[] = {d_polyTaps, d_tw, d_hilb, d_stw, d_sig};
 		for (void* q : dev) if (q) cudaFree(q);
 		if (ownStream && stream) cudaStreamDestroy(stream);
 	}
@@ -523,8 +522,7 @@ usgb::PrepParams prep_params(const usgb_two_medium* c, const float* d_rf)
 	pp.outScale = c->scale;
 	usgb::host::set_fft_params(pp, c->fft);
 	pp.tw = c->d_tw;
-	pp.cs = c->d_cs;
-	pp.perm = c->d_perm;
+	pp.hilb = c->d_hilb;
 	pp.stw = c->stageTw ? c->d_stw : nullptr;
 	return pp;
 }
@@ -545,9 +543,8 @@ void build_tables(usgb_two_medium* c)
 	upload(&c->d_polyTaps, poly.poly);
 	if (!usgb::host::make_fft_tables(c->L, c->fft)) TM_FAIL(USGB_ERR_INVALID_STATE, "FFT size " << c->fft.M << " not supported");
 	upload(&c->d_tw, c->fft.tw);
-	upload(&c->d_cs, c->fft.cs);
+	upload(&c->d_hilb, c->fft.hilb);
 	upload(&c->d_stw, c->fft.stageTw);
-	upload(&c->d_perm, c->fft.perm);
 	int dev = 0, maxSmem = 0;
 	TM_CUDA(cudaGetDevice(&dev));
 	TM_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
