@@ -581,6 +581,33 @@ __device__ void store_real_pass(const PrepParams& p, const float* rfs, const flo
 	}
 }
 
+// The Hilbert multiplier of the pair whose table entry h sits at position i
+// (PrepParams::hilb): W[k_lo] and W[M - k_lo] in place, or W[0] = 0, or
+// W[M/2] = i Z[M/2].
+constexpr int kHilbertBatch = 4;
+__device__ __forceinline__ void hilbert_pair(float2* data, unsigned i, const float4& h)
+{
+	const unsigned code = __float_as_uint(h.z);
+	if (code == kHilbertSkip) return;
+	if (code == i) {
+		if (i == 0) {
+			data[0] = make_float2(0.f, 0.f);   // k = 0 sits at position 0
+		} else {
+			const float2 z = data[i];          // k = M / 2
+			data[i] = make_float2(-z.y, z.x);
+		}
+		return;
+	}
+	const unsigned q = code & ~kHilbertSwap;
+	const bool swap = (code & kHilbertSwap) != 0u;
+	const unsigned q1 = swap ? q : i;      // position of k_lo
+	const unsigned q2 = swap ? i : q;      // position of M - k_lo
+	const float2 A = data[q1], B = data[q2];
+	const float2 cs = make_float2(h.x, h.y);
+	data[q1] = make_float2(cs.x * B.x - cs.y * A.y, cs.y * A.x - cs.x * B.y);
+	data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
+}
+
 // Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
 // the generic FIR loop. ENV: the envelope of the input itself instead
 // (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
@@ -605,7 +632,11 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
 	//    (block_sum's barriers also order the writes above).
 	//    The real parts of the output, (x[n] - mean) * scale, are stored here
-	//    (the FFT overwrites x); the imaginary parts follow in step 6.
+	//    (the FFT overwrites x) as whole complex samples with a zero
+	//    imaginary part, so that every 32-byte sector is written whole: a
+	//    sector holding only real halves was written back to HBM partially
+	//    and read back when the imaginary parts (step 6) arrived, 0.7 GB each
+	//    way per cf2d frame. The imaginary parts then merge into the lines in L2.
 	float mean = 0.f;
 	if constexpr (!ENV) {
 		mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
@@ -615,7 +646,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) {
 			const float d = xs[n] - mean;
 			xs[n] = d;
-			store_component<S>(out, n, 0, d * sc);
+			out[n] = Complex<S>::pack(d * sc, 0.0f);
 		}
 	}
 	__syncthreads();
@@ -626,28 +657,18 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	// 4. Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
 	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0,
 	//    visited in digit-reversed position order (both members of
-	//    neighbouring lanes' pairs sit at neighbouring positions).
-	for (unsigned i = threadIdx.x; i < p.hilbCount; i += blockDim.x) {
-		const float4 h = __ldg(&p.hilb[i]);
-		const unsigned code = __float_as_uint(h.z);
-		if (code == kHilbertSkip) continue;
-		if (code == i) {
-			if (i == 0) {
-				data[0] = make_float2(0.f, 0.f);   // k = 0 sits at position 0
-			} else {
-				const float2 z = data[i];          // k = M / 2
-				data[i] = make_float2(-z.y, z.x);
-			}
-			continue;
+	//    neighbouring lanes' pairs sit at neighbouring positions). A thread
+	//    loads the table entries of kHilbertBatch pairs before it works on
+	//    them, so their L2 latencies overlap (the pairs are disjoint).
+	for (unsigned i0 = threadIdx.x; i0 < p.hilbCount; i0 += kHilbertBatch * blockDim.x) {
+		float4 h[kHilbertBatch];
+#pragma unroll
+		for (int u = 0; u < kHilbertBatch; ++u) {
+			const unsigned i = i0 + u * blockDim.x;
+			h[u] = (i < p.hilbCount) ? __ldg(&p.hilb[i]) : make_float4(0.f, 0.f, __uint_as_float(kHilbertSkip), 0.f);
 		}
-		const unsigned q = code & ~kHilbertSwap;
-		const bool swap = (code & kHilbertSwap) != 0u;
-		const unsigned q1 = swap ? q : i;      // position of k_lo
-		const unsigned q2 = swap ? i : q;      // position of M - k_lo
-		const float2 A = data[q1], B = data[q2];
-		const float2 cs = make_float2(h.x, h.y);
-		data[q1] = make_float2(cs.x * B.x - cs.y * A.y, cs.y * A.x - cs.x * B.y);
-		data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
+#pragma unroll
+		for (int u = 0; u < kHilbertBatch; ++u) hilbert_pair(data, i0 + u * blockDim.x, h[u]);
 	}
 	__syncthreads();
 
