@@ -205,8 +205,9 @@ def run_gpu(args):
     eng = StaEngine(spec)
     if args.das == "plain":
         eng.set_das_variant(0)
-    elif args.das in ("staged", "group") and not args.autotune:
-        eng.set_das_variant(1 if args.das == "staged" else 2, args.tile_rows, args.stage_bytes, args.stages)
+    elif args.das in ("staged", "group", "group64") and not args.autotune:
+        eng.set_das_variant({"staged": 1, "group": 2, "group64": 3}[args.das], args.tile_rows, args.stage_bytes,
+                            args.stages)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream)
     with torch.cuda.stream(stream):
@@ -347,7 +348,8 @@ def run_gpu(args):
             "data": "synthetic (seeded point + speckle scatterers)",
             "config": {"workload": desc, "storage": spec.storage, "das_kernel": ("plain" if das_cfg["variant"] == 0 else
                            ("staged" if das_cfg["variant"] == 1 else "receiver-group")
-                           + f" (tile 32x{das_cfg['tile_rows']}, {das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
+                           + f" (tile {64 if das_cfg['variant'] == 3 else 32}x{das_cfg['tile_rows']}, "
+                           + f"{das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
                            + (", autotuned)" if args.autotune else ")")),
                        "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
                        "parallelism": f"replicas x{world}"},
@@ -724,7 +726,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cf2d", choices=["cf2d", "plain2d", "matrix3d"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
-    ap.add_argument("--das", default="auto", choices=["auto", "plain", "staged", "group"],
+    ap.add_argument("--das", default="auto", choices=["auto", "plain", "staged", "group", "group64"],
                     help="delay-and-sum kernel; auto = autotuned over every kernel and shape")
     ap.add_argument("--tile-rows", type=int, default=4)
     ap.add_argument("--stage-bytes", type=int, default=32768)

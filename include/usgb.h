@@ -174,9 +174,14 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * delays in a per-point table), 2 = receiver-group (the same ring, filled
  * receiver group by receiver group; a group's receive delays and sums stay in
  * registers, no per-point table, so arrays of hundreds of elements stage as
- * well). 0 for tile_rows / stage_bytes / stages keeps the current value. New
- * contexts start with the receiver-group kernel (4 rows, 2 x 32 KiB) where it
- * fits. */
+ * well), 3 = receiver-group on tiles of 64 columns x tile_rows (4 or 8) rows
+ * (windows only a little longer for twice the points: fewer bytes and half
+ * the copies staged per frame). 0 for tile_rows / stage_bytes / stages keeps
+ * the current value. New
+ * contexts start with the receiver-group kernel (32 x 4 tiles, 2 x 32 KiB)
+ * where it fits; setting a grid of at least two 64 x 4 tiles per SM then
+ * selects variant 3 (64 x 4, 2 x 48 KiB) where it fits, unless a variant was
+ * set here or by usgb_autotune_das. */
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);
@@ -265,7 +270,8 @@ int usgb_batch_create(uint32_t max_frames, uint32_t max_elements, uint32_t max_s
 void usgb_batch_destroy(usgb_batch* batch);
 const char* usgb_batch_last_error(const usgb_batch* batch);
 int usgb_batch_set_das_config(usgb_batch* batch, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
-/* Delay-and-sum kernel of the batch: 2 = receiver-group (default), 1 = staged. */
+/* Delay-and-sum kernel of the batch: 2 = receiver-group (default), 3 =
+ * receiver-group on 64-column tiles, 1 = staged. */
 int usgb_batch_set_das_variant(usgb_batch* batch, int variant);
 int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
 int usgb_batch_synchronize(usgb_batch* batch);

@@ -22,7 +22,7 @@ def _alone(frame, cuda, das_config):
         return v.cpu().numpy(), f.cpu().numpy()
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3])
 @pytest.mark.parametrize("use_graph", [False, True])
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 def test_batch_equals_frames_alone(cuda, use_graph, storage, variant):

@@ -266,26 +266,45 @@ def _staged_cases():
 @pytest.mark.parametrize("rows,stage_bytes", [(8, 16384), (4, 4096), (16, 1024)])
 @pytest.mark.parametrize("name,frame", _staged_cases(), ids=[n for n, _ in _staged_cases()])
 def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes):
-    """The shared-memory staged kernel and the receiver-group kernel read the
-    same samples with the same weights in the same order as the plain kernel:
-    the images are identical, also when windows overflow a stage (small stages
-    force the global-memory path), for partial tiles and for a receiver count
-    that leaves a partial receiver group (12 elements)."""
+    """The shared-memory staged kernel and the receiver-group kernel (32- and
+    64-column tiles) read the same samples with the same weights in the same
+    order as the plain kernel: the images are identical, also when windows
+    overflow a stage (small stages force the global-memory path), for partial
+    tiles and for a receiver count that leaves a partial receiver group (12
+    elements)."""
     import torch
     from us_lab4a_gb300 import StaEngine
     rf = torch.as_tensor(frame.make_rf_numpy(), device=cuda)
     g = torch.as_tensor(frame.grid_xyz, device=cuda)
     out = []
-    for variant in (0, 1, 2):
+    for variant in (0, 1, 2, 3):
         with StaEngine(frame.spec) as eng:
             eng.set_stream(torch.cuda.current_stream())
-            eng.set_das_variant(variant, rows, stage_bytes)
+            eng.set_das_variant(variant, min(rows, 8) if variant == 3 else rows, stage_bytes)
             eng.set_grid_device(g)
             v = torch.empty(frame.grid_xyz.shape[:2], device=cuda)
             f = torch.empty_like(v)
             eng.process_device(rf, v, f)
             eng.synchronize()
             out.append((v.cpu().numpy(), f.cpu().numpy()))
-    for variant in (1, 2):
+    for variant in (1, 2, 3):
         assert np.array_equal(out[0][0], out[variant][0]), variant
         assert np.array_equal(out[0][1], out[variant][1]), variant
+
+
+def test_grid_selects_tile_width(cuda):
+    """Without an explicit choice, a grid of at least two 64 x 4 tiles per SM
+    selects the receiver-group kernel on 64-column tiles, a small grid keeps
+    32-column tiles, and a variant set explicitly survives a new grid."""
+    import torch
+    from us_lab4a_gb300 import StaEngine, workloads
+    frame = workloads.cf2d(small=True)
+    with StaEngine(frame.spec) as eng:
+        eng.set_grid_device(torch.zeros((32, 32, 3), device=cuda))
+        assert eng.das_config()["variant"] == 2
+        eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
+        cfg = eng.das_config()
+        assert cfg["variant"] == 3 and cfg["tile_rows"] == 4
+        eng.set_das_variant(2, 8, 16384, 2)
+        eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
+        assert eng.das_config() == {"variant": 2, "tile_rows": 8, "stage_bytes": 16384, "stages": 2}

@@ -86,6 +86,7 @@ struct usgb_ctx {
 	bool hostDirectAvailable = false;  // kernels can read/write pageable host memory (host page tables)
 	bool hostDirect = false;
 	int dasVariant = 0;
+	bool dasExplicit = false;   // chosen by usgb_set_das_variant / usgb_autotune_das: kept when the grid changes
 	int delayMode = USGB_DELAY_AUTO;
 	unsigned tileRows = 8;
 	unsigned stageBytes = 16384;
@@ -307,11 +308,14 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.value = d_value;
 	dp.factor = d_factor;
 	dp.errWord = c->d_err;
+	dp.tileCols = usgb::das_tile_cols(c->dasVariant);
 	dp.tileRows = c->tileRows;
 	dp.stageBytes = c->stageBytes;
 	dp.stages = c->stages;
 	return dp;
 }
+
+void choose_grid_das(usgb_ctx* c);
 
 void ensure_grid(usgb_ctx* c, uint32_t ncols, uint32_t nrows)
 {
@@ -332,6 +336,7 @@ void ensure_grid(usgb_ctx* c, uint32_t ncols, uint32_t nrows)
 	c->ncols = ncols;
 	c->nrows = nrows;
 	c->npix = static_cast<unsigned>(npix);
+	if (!c->dasExplicit) choose_grid_das(c);
 }
 
 size_t max_smem()
@@ -347,7 +352,7 @@ size_t max_smem()
 // tiles), else the plain kernel.
 size_t das_smem_bytes(const usgb_ctx* c, int variant, unsigned rows, unsigned cap, unsigned nst)
 {
-	return variant == 2 ? usgb::das_group_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst)
+	return variant >= 2 ? usgb::das_group_smem_bytes(c->prm.num_tx, c->prm.num_rx, usgb::das_tile_cols(variant), rows, cap, nst)
 	                    : usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst);
 }
 
@@ -374,6 +379,30 @@ void choose_default_das(usgb_ctx* c)
 		}
 	}
 	c->dasVariant = 0;
+}
+
+// With the grid known: 64 x 4 tiles with 2 x 48 KiB stages (fewer, larger
+// window copies; measured 1.87 against 1.97 ms on cf2d) where the grid gives
+// at least two such tiles per SM and the shared memory fits, else the
+// creation-time default.
+void choose_grid_das(usgb_ctx* c)
+{
+	choose_default_das(c);
+	if (c->dasVariant != 2) return;
+	int dev = 0, sms = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) return;
+	if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return;
+	const size_t tiles = static_cast<size_t>((c->ncols + 63) / 64) * ((c->nrows + 3) / 4);
+	if (tiles < 2u * static_cast<size_t>(sms)) return;
+	for (unsigned cap : {49152u, 32768u}) {
+		if (das_smem_bytes(c, 3, 4u, cap, 2u) <= max_smem()) {
+			c->dasVariant = 3;
+			c->tileRows = 4;
+			c->stageBytes = cap;
+			c->stages = 2;
+			return;
+		}
+	}
 }
 
 void check_prep_fits(usgb_ctx* c)
@@ -655,12 +684,13 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return guarded(c, [&] {
-		if (variant < 0 || variant > 2) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
+		if (variant < 0 || variant > 3) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
 		const unsigned rows = tile_rows ? tile_rows : c->tileRows;
 		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
 		const unsigned nst = stages ? stages : c->stages;
 		if (variant != 0) {
 			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+			if (variant == 3 && rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
 				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 			}
@@ -675,6 +705,7 @@ int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t 
 		c->tileRows = rows;
 		c->stageBytes = cap;
 		c->stages = nst;
+		c->dasExplicit = true;
 	});
 }
 
@@ -708,11 +739,12 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		const unsigned iters = iterations ? iterations : 3;
 		struct Cand { int variant; unsigned rows, cap, stages; };
 		std::vector<Cand> cands;
-		for (int variant : {1, 2})
+		for (int variant : {1, 2, 3})
 			for (unsigned rows : {4u, 8u, 16u})
-				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u})
+				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u})
 					for (unsigned nst : {2u, 3u, 4u})
-						if ((variant == 2 || cap % 8192u == 0) && das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
+						if ((variant >= 2 || cap % 8192u == 0) && !(variant == 3 && rows == 16)
+								&& das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
 							cands.push_back({variant, rows, cap, nst});
 		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});
 		cudaEvent_t e0, e1;
@@ -760,6 +792,7 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		c->tileRows = bestC.rows;
 		c->stageBytes = bestC.cap;
 		c->stages = bestC.stages;
+		c->dasExplicit = true;
 		if (best_ms) *best_ms = best;
 	});
 }
@@ -815,7 +848,7 @@ int batch_guarded(usgb_batch* b, F&& f)
 
 size_t batch_das_smem(const usgb_batch* b, int variant, unsigned rows, unsigned cap, unsigned nst)
 {
-	return variant == 2 ? usgb::das_group_smem_bytes(b->maxElements, b->maxElements, rows, cap, nst)
+	return variant >= 2 ? usgb::das_group_smem_bytes(b->maxElements, b->maxElements, usgb::das_tile_cols(variant), rows, cap, nst)
 	                    : usgb::das_staged_smem_bytes(b->maxElements, b->maxElements, rows, cap, nst);
 }
 
@@ -875,7 +908,8 @@ const char* usgb_batch_last_error(const usgb_batch* b)
 int usgb_batch_set_das_variant(usgb_batch* b, int variant)
 {
 	return batch_guarded(b, [&] {
-		if (variant != 1 && variant != 2) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1 or 2.");
+		if (variant < 1 || variant > 3) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1, 2 or 3.");
+		if (variant == 3 && b->tileRows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 		if (batch_das_smem(b, variant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
 			USGB_FAIL(USGB_ERR_UNSUPPORTED, "the current tile shape does not fit in shared memory for this variant.");
 		}
@@ -891,6 +925,7 @@ int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_
 {
 	return batch_guarded(b, [&] {
 		if (tile_rows != 4 && tile_rows != 8 && tile_rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+		if (b->dasVariant == 3 && tile_rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 		if (stage_bytes < 1024 || stage_bytes % 128 != 0 || stage_bytes > (1u << 20)) {
 			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 		}
@@ -951,12 +986,13 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 			sigBegin += c->numSignals;
 			usgb::DasParams dp = das_params(c, c->d_sig, items[i].d_value, items[i].d_factor);
 			dp.errWord = b->d_err;
+			dp.tileCols = usgb::das_tile_cols(b->dasVariant);
 			dp.tileRows = b->tileRows;
 			dp.stageBytes = b->stageBytes;
 			dp.stages = b->stages;
 			dasF[i].das = dp;
 			dasF[i].tileBegin = tileBegin;
-			dasF[i].tilesX = (c->ncols + 31) / 32;
+			dasF[i].tilesX = (c->ncols + dp.tileCols - 1) / dp.tileCols;
 			dasF[i].cf = static_cast<int>(c->prm.coherence);
 			tileBegin += dasF[i].tilesX * ((c->nrows + b->tileRows - 1) / b->tileRows);
 		}
@@ -973,10 +1009,11 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 		const unsigned prepBlocks = b->numSMs * std::min(prepPerSM, 4u);
 		usgb::BatchDasConfig dc{};
 		dc.maxTx = dc.maxRx = b->maxElements;
+		dc.tileCols = usgb::das_tile_cols(b->dasVariant);
 		dc.tileRows = b->tileRows;
 		dc.stageBytes = b->stageBytes;
 		dc.stages = b->stages;
-		if (b->dasVariant == 2) {
+		if (b->dasVariant >= 2) {
 			dc.blocks = 0;  // the launcher fills the SMs (occupancy of the kernel at this shape)
 		} else {
 			const size_t dasSmem = usgb::das_staged_smem_bytes(dc.maxTx, dc.maxRx, dc.tileRows, dc.stageBytes, dc.stages);
@@ -990,7 +1027,7 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 		auto enqueue = [&](cudaStream_t st) {
 			USGB_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc, b->descBytes, cudaMemcpyHostToDevice, st));
 			USGB_CUDA(usgb::launch_prep_batch(dPrep, dHdr, prepSmem, prepBlocks, storage, analytic, st));
-			if (variant == 2) {
+			if (variant >= 2) {
 				USGB_CUDA(usgb::launch_das_group_batch(dDas, dHdr, dc, storage, analytic, st));
 			} else {
 				USGB_CUDA(usgb::launch_das_staged_batch(dDas, dHdr, dc, storage, analytic, st));

@@ -21,9 +21,10 @@ cudaError_t launch_das_group_batch(const BatchDasFrame* frames, const BatchHeade
 	}
 }
 
-size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages)
+size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileCols, unsigned tileRows, unsigned capBytes,
+		unsigned stages)
 {
-	return group_layout_bytes(numTx, numRx, tileRows, capBytes, stages);
+	return group_layout_bytes(numTx, numRx, tileCols, tileRows, capBytes, stages);
 }
 
 cudaError_t launch_das_group(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream)

@@ -1,7 +1,7 @@
-// Receiver-group delay-and-sum: one thread block per tile of 32 columns x
-// TROWS rows of grid points (lane = column, warp = row), like the staged
-// kernel (usgb_das_staged.cu), but the pairs are visited receiver group by
-// receiver group: for each group of kGroup receivers, every transmitter in
+// Receiver-group delay-and-sum: one thread block per tile of TCOLS (32 or
+// 64) columns x TROWS rows of grid points (lane = column, TCOLS / 32 warps a
+// row), like the staged kernel (usgb_das_staged.cu), but the pairs are
+// visited receiver group by receiver group: for each group of kGroup receivers, every transmitter in
 // turn, with the group's kGroup windows (one per receiver) staged together as
 // one unit. A consumer thread keeps the group's receive delays and its kGroup
 // receiver sums in registers and computes each transmitter's delay once per
@@ -9,6 +9,12 @@
 // only its stage ring and a few per-element tables, several blocks fit on an
 // SM, and arrays of hundreds of elements (2D matrix probes) stage like small
 // ones.
+//
+// Tile width: the delays change along a column by about 2 dz / (c / (fs U))
+// samples per row (45 on cf2d) and little across columns, so a wider tile
+// stages windows that are only a little longer for twice the points: 64 x 4
+// tiles stage 12.2 GB per cf2d frame against 16.4 GB for 32 x 4, with half as
+// many window copies, and one producer warp serves eight consumer warps.
 //
 // Arithmetic is the plain kernel's, term for term: delay = fl(fl(offset +
 // fl(dist_tx * invCT)) + fl(dist_rx * invCT)), the same index / fraction
@@ -55,7 +61,8 @@ static_assert(sizeof(GroupStage) % 16 == 0, "stage metadata must stay 16-byte al
 
 struct GroupLayout {
 	unsigned bars, tileMax, zero, meta, rxinfo, txinfo, minmax, partial, stage, total;
-	__host__ __device__ GroupLayout(unsigned maxTx, unsigned maxRx, unsigned trows, unsigned capBytes, unsigned stages)
+	// cwarps: consumer warps (one per 32 points of the tile).
+	__host__ __device__ GroupLayout(unsigned maxTx, unsigned maxRx, unsigned cwarps, unsigned capBytes, unsigned stages)
 	{
 		bars = 0;
 		tileMax = 2 * stages * 8;
@@ -65,7 +72,7 @@ struct GroupLayout {
 		txinfo = rxinfo + maxRx * 16;
 		minmax = (txinfo + maxTx * 8 + 15) & ~15u;
 		partial = minmax + 2 * (maxTx + maxRx) * 4;
-		stage = partial + 2 * trows * (maxTx + maxRx) * 4;
+		stage = partial + 2 * cwarps * (maxTx + maxRx) * 4;
 		stage = (stage + 127) & ~127u;
 		total = stage + stages * capBytes;
 	}
@@ -83,7 +90,7 @@ struct GroupSmem {
 	float* maxT;
 	float* minR;
 	float* maxR;
-	float* partMin;            // [TROWS][maxTx + maxRx]
+	float* partMin;            // [consumer warps][maxTx + maxRx]
 	float* partMax;
 	unsigned char* stageBuf;
 	unsigned nst;
@@ -92,7 +99,7 @@ struct GroupSmem {
 };
 
 __device__ __forceinline__ GroupSmem carve_group(unsigned char* smem, const GroupLayout& lay, unsigned maxTx,
-		unsigned maxRx, unsigned trows, unsigned nst, unsigned capBytes)
+		unsigned maxRx, unsigned cwarps, unsigned nst, unsigned capBytes)
 {
 	GroupSmem s;
 	s.full = reinterpret_cast<uint64_t*>(smem + lay.bars);
@@ -107,7 +114,7 @@ __device__ __forceinline__ GroupSmem carve_group(unsigned char* smem, const Grou
 	s.minR = s.maxT + maxTx;
 	s.maxR = s.minR + maxRx;
 	s.partMin = reinterpret_cast<float*>(smem + lay.partial);
-	s.partMax = s.partMin + trows * (maxTx + maxRx);
+	s.partMax = s.partMin + cwarps * (maxTx + maxRx);
 	s.stageBuf = smem + lay.stage;
 	s.nst = nst;
 	s.capBytes = capBytes;
@@ -115,13 +122,13 @@ __device__ __forceinline__ GroupSmem carve_group(unsigned char* smem, const Grou
 	return s;
 }
 
-__device__ __forceinline__ void init_group_barriers(const GroupSmem& sm, int trows)
+__device__ __forceinline__ void init_group_barriers(const GroupSmem& sm, int cwarps)
 {
 	if (threadIdx.x < 4) reinterpret_cast<unsigned*>(const_cast<unsigned char*>(sm.zero))[threadIdx.x] = 0u;
 	if (threadIdx.x == 0) {
 		for (unsigned s = 0; s < sm.nst; ++s) {
 			mbar_init(&sm.full[s], 1);
-			mbar_init(&sm.empty[s], trows);
+			mbar_init(&sm.empty[s], cwarps);
 		}
 		fence_barrier_init();
 	}
@@ -350,15 +357,17 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 }
 
 // One tile (bx, by) of one frame; `it` is the block's running stage counter.
-template<int S, int CF, bool ANALYTIC, int TROWS>
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
 __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx, unsigned by, int& it)
 {
 	using SP = Sample<ANALYTIC, S>;
+	constexpr int CW = TCOLS / 32;      // warps per tile row
+	constexpr int NCW = TROWS * CW;     // consumer warps
 	const int warp = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
-	const bool producer = warp == TROWS;
-	const unsigned col = bx * 32 + lane;
-	const unsigned row = by * TROWS + warp;
+	const bool producer = warp == NCW;
+	const unsigned col = bx * TCOLS + (warp % CW) * 32 + lane;
+	const unsigned row = by * TROWS + warp / CW;
 	const bool active = !producer && col < p.ncols && row < p.nrows;
 	const unsigned pix = col * p.nrows + row;
 	const unsigned nE = p.numTx + p.numRx;
@@ -407,7 +416,7 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	float topT = 0.f, topR = 0.f;
 	for (unsigned e = threadIdx.x; e < nE; e += blockDim.x) {
 		float mn = sm.partMin[e], mx = sm.partMax[e];
-		for (int w = 1; w < TROWS; ++w) {
+		for (int w = 1; w < NCW; ++w) {
 			mn = fminf(mn, sm.partMin[w * sm.maxE + e]);
 			mx = fmaxf(mx, sm.partMax[w * sm.maxE + e]);
 		}
@@ -426,46 +435,53 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	         : group_consume<SP, CF, false>(p, sm, it, px, py, pz, active, pix, fx);
 }
 
-// Resident blocks per SM the register allocation is held to. One frame: 5
-// for 4-row tiles (at most 81 registers a thread; measured fastest on the
-// 64-element frames even though 32 KiB stages let only 3 blocks in). Batches
-// (every coherence factor in one kernel, more live state): 3 for 4-row tiles
-// and 2 for 8-row tiles, which removes their spills (2-3 KiB a thread at 5
-// and 3).
-template<int TROWS> constexpr int group_min_blocks() { return TROWS == 4 ? 5 : (TROWS == 8 ? 3 : 1); }
-template<int TROWS> constexpr int group_batch_min_blocks() { return TROWS == 4 ? 3 : (TROWS == 8 ? 2 : 1); }
+// Resident blocks per SM the register allocation is held to, by consumer
+// warps. One frame: 5 for 4 consumer warps (at most 81 registers a thread;
+// measured fastest on the 64-element frames even though 32 KiB stages let
+// only 3 blocks in). Batches (every coherence factor in one kernel, more live
+// state): 3 for 4 and 2 for 8 consumer warps (fewer spills than at 5 and 3;
+// measured faster on the mixed batch).
+template<int NCW> constexpr int group_min_blocks() { return NCW == 4 ? 5 : (NCW == 8 ? 3 : 1); }
+template<int NCW> constexpr int group_batch_min_blocks() { return NCW == 4 ? 3 : (NCW == 8 ? 2 : 1); }
 
-template<int S, int CF, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32, group_min_blocks<TROWS>())
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
+__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_min_blocks<TROWS * TCOLS / 32>())
 das_group_kernel(DasParams p)
 {
+	constexpr int NCW = TROWS * TCOLS / 32;
 	extern __shared__ __align__(128) unsigned char smem[];
-	const GroupLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
-	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, TROWS, p.stages, p.stageBytes);
-	init_group_barriers(sm, TROWS);
+	const GroupLayout lay(p.numTx, p.numRx, NCW, p.stageBytes, p.stages);
+	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, NCW, p.stages, p.stageBytes);
+	init_group_barriers(sm, NCW);
 	int it = 0;
-	group_tile<S, CF, ANALYTIC, TROWS>(p, sm, blockIdx.x, blockIdx.y, it);
+	group_tile<S, CF, ANALYTIC, TCOLS, TROWS>(p, sm, blockIdx.x, blockIdx.y, it);
 }
 
-template<int S, int CF, bool ANALYTIC, int TROWS>
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
 cudaError_t launch_group_one(const DasParams& p, cudaStream_t stream)
 {
-	const GroupLayout lay(p.numTx, p.numRx, TROWS, p.stageBytes, p.stages);
-	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TROWS>,
+	constexpr int NCW = TROWS * TCOLS / 32;
+	const GroupLayout lay(p.numTx, p.numRx, NCW, p.stageBytes, p.stages);
+	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS>,
 			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
-	const dim3 grid((p.ncols + 31) / 32, (p.nrows + TROWS - 1) / TROWS);
-	das_group_kernel<S, CF, ANALYTIC, TROWS><<<grid, (TROWS + 1) * 32, lay.total, stream>>>(p);
+	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + TROWS - 1) / TROWS);
+	das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS><<<grid, (NCW + 1) * 32, lay.total, stream>>>(p);
 	return cudaGetLastError();
 }
 
+// Tile shapes (columns x rows): 32 x 4, 32 x 8, 32 x 16, 64 x 4, 64 x 8.
 template<int S, int CF, bool ANALYTIC>
 cudaError_t launch_group_rows(const DasParams& p, cudaStream_t stream)
 {
+	if (p.tileCols == 64) {
+		return p.tileRows == 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4>(p, stream)
+		                       : launch_group_one<S, CF, ANALYTIC, 64, 8>(p, stream);
+	}
 	switch (p.tileRows) {
-	case 4: return launch_group_one<S, CF, ANALYTIC, 4>(p, stream);
-	case 16: return launch_group_one<S, CF, ANALYTIC, 16>(p, stream);
-	default: return launch_group_one<S, CF, ANALYTIC, 8>(p, stream);
+	case 4: return launch_group_one<S, CF, ANALYTIC, 32, 4>(p, stream);
+	case 16: return launch_group_one<S, CF, ANALYTIC, 32, 16>(p, stream);
+	default: return launch_group_one<S, CF, ANALYTIC, 32, 8>(p, stream);
 	}
 }
 
@@ -483,35 +499,36 @@ cudaError_t launch_group_cf(const DasParams& p, int cf, bool analytic, cudaStrea
 	}
 }
 
-template<int S, bool ANALYTIC, int TROWS>
+template<int S, bool ANALYTIC, int TCOLS, int TROWS>
 __device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, const GroupSmem& sm, unsigned bx,
 		unsigned by, int& it)
 {
 	if (!ANALYTIC) {
-		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TROWS>(p, sm, bx, by, it)
-		                      : group_tile<S, CF_NONE, false, TROWS>(p, sm, bx, by, it);
+		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TCOLS, TROWS>(p, sm, bx, by, it)
+		                      : group_tile<S, CF_NONE, false, TCOLS, TROWS>(p, sm, bx, by, it);
 	}
 	switch (cf) {
-	case CF_PCF: return group_tile<S, CF_PCF, true, TROWS>(p, sm, bx, by, it);
-	case CF_SCF: return group_tile<S, CF_SCF, true, TROWS>(p, sm, bx, by, it);
-	case CF_MF: return group_tile<S, CF_MF, true, TROWS>(p, sm, bx, by, it);
-	default: return group_tile<S, CF_NONE, true, TROWS>(p, sm, bx, by, it);
+	case CF_PCF: return group_tile<S, CF_PCF, true, TCOLS, TROWS>(p, sm, bx, by, it);
+	case CF_SCF: return group_tile<S, CF_SCF, true, TCOLS, TROWS>(p, sm, bx, by, it);
+	case CF_MF: return group_tile<S, CF_MF, true, TCOLS, TROWS>(p, sm, bx, by, it);
+	default: return group_tile<S, CF_NONE, true, TCOLS, TROWS>(p, sm, bx, by, it);
 	}
 }
 
 // Many frames: persistent blocks walk the tiles of every frame in the batch.
-template<int S, bool ANALYTIC, int TROWS>
-__global__ void __launch_bounds__((TROWS + 1) * 32, group_batch_min_blocks<TROWS>())
+template<int S, bool ANALYTIC, int TCOLS, int TROWS>
+__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_batch_min_blocks<TROWS * TCOLS / 32>())
 das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
 		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
 {
+	constexpr int NCW = TROWS * TCOLS / 32;
 	extern __shared__ __align__(128) unsigned char smem[];
 	__shared__ DasParams sp;
 	__shared__ int sAbort;
-	const GroupLayout lay(maxTx, maxRx, TROWS, capBytes, stages);
-	const GroupSmem sm = carve_group(smem, lay, maxTx, maxRx, TROWS, stages, capBytes);
+	const GroupLayout lay(maxTx, maxRx, NCW, capBytes, stages);
+	const GroupSmem sm = carve_group(smem, lay, maxTx, maxRx, NCW, stages, capBytes);
 	if (threadIdx.x == 0) sAbort = 0;
-	init_group_barriers(sm, TROWS);
+	init_group_barriers(sm, NCW);
 	const unsigned count = hdr->count;
 	const unsigned totalTiles = hdr->totalTiles;
 	int it = 0;
@@ -524,28 +541,29 @@ das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHead
 		if (sAbort) break;
 		const unsigned local = w - frames[f].tileBegin;
 		const unsigned tilesX = frames[f].tilesX;
-		const bool ok = group_tile_any_cf<S, ANALYTIC, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
+		const bool ok = group_tile_any_cf<S, ANALYTIC, TCOLS, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
 		if (!ok) sAbort = 1;
 	}
 }
 
-template<int S, bool ANALYTIC, int TROWS>
+template<int S, bool ANALYTIC, int TCOLS, int TROWS>
 cudaError_t launch_group_batch_one(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
 		cudaStream_t stream)
 {
-	const GroupLayout lay(c.maxTx, c.maxRx, TROWS, c.stageBytes, c.stages);
-	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TROWS>;
+	constexpr int NCW = TROWS * TCOLS / 32;
+	const GroupLayout lay(c.maxTx, c.maxRx, NCW, c.stageBytes, c.stages);
+	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TCOLS, TROWS>;
 	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
 	unsigned blocks = c.blocks;
 	if (blocks == 0) {  // as many resident blocks as the SMs hold
 		int perSM = 0, dev = 0, sms = 0;
-		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, (TROWS + 1) * 32, lay.total)) != cudaSuccess) return e;
+		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, (NCW + 1) * 32, lay.total)) != cudaSuccess) return e;
 		if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
 		if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
 		blocks = static_cast<unsigned>(sms) * static_cast<unsigned>(perSM > 0 ? perSM : 1);
 	}
-	kernel<<<blocks, (TROWS + 1) * 32, lay.total, stream>>>(frames, hdr, c.maxTx, c.maxRx, c.stageBytes, c.stages);
+	kernel<<<blocks, (NCW + 1) * 32, lay.total, stream>>>(frames, hdr, c.maxTx, c.maxRx, c.stageBytes, c.stages);
 	return cudaGetLastError();
 }
 
@@ -553,10 +571,14 @@ template<int S, bool ANALYTIC>
 cudaError_t group_batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
 		cudaStream_t stream)
 {
+	if (c.tileCols == 64) {
+		return c.tileRows == 4 ? launch_group_batch_one<S, ANALYTIC, 64, 4>(frames, hdr, c, stream)
+		                       : launch_group_batch_one<S, ANALYTIC, 64, 8>(frames, hdr, c, stream);
+	}
 	switch (c.tileRows) {
-	case 4: return launch_group_batch_one<S, ANALYTIC, 4>(frames, hdr, c, stream);
-	case 16: return launch_group_batch_one<S, ANALYTIC, 16>(frames, hdr, c, stream);
-	default: return launch_group_batch_one<S, ANALYTIC, 8>(frames, hdr, c, stream);
+	case 4: return launch_group_batch_one<S, ANALYTIC, 32, 4>(frames, hdr, c, stream);
+	case 16: return launch_group_batch_one<S, ANALYTIC, 32, 16>(frames, hdr, c, stream);
+	default: return launch_group_batch_one<S, ANALYTIC, 32, 8>(frames, hdr, c, stream);
 	}
 }
 
@@ -576,9 +598,10 @@ cudaError_t launch_das_group_batch_storage(const BatchDasFrame* frames, const Ba
 	return analytic ? group_batch_rows<S, true>(frames, hdr, c, stream) : group_batch_rows<S, false>(frames, hdr, c, stream);
 }
 
-inline size_t group_layout_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages)
+inline size_t group_layout_bytes(unsigned numTx, unsigned numRx, unsigned tileCols, unsigned tileRows, unsigned capBytes,
+		unsigned stages)
 {
-	return GroupLayout(numTx, numRx, tileRows, capBytes, stages).total;
+	return GroupLayout(numTx, numRx, tileRows * (tileCols / 32), capBytes, stages).total;
 }
 
 }  // namespace usgb

@@ -89,19 +89,25 @@ struct DasParams {
 	float* value;
 	float* factor;
 	unsigned* errWord;
-	// Staged kernel: rows of the 32-column pixel tile, bytes per pipeline
-	// stage, number of stages (2..16).
+	// Staged kernels: columns (32; 64 for the receiver-group kernel's wide
+	// tiles) and rows of the pixel tile, bytes per pipeline stage, number of
+	// stages (2..16).
+	unsigned tileCols;
 	unsigned tileRows;
 	unsigned stageBytes;
 	unsigned stages;
 };
 
-// variant 0: plain kernel; 1: staged kernel; 2: receiver-group kernel.
+// variant 0: plain kernel; 1: staged kernel; 2: receiver-group kernel
+// (32-column tiles); 3: receiver-group kernel, 64-column tiles.
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
 cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
 // variant 2: receiver-group kernel (usgb_das_group.cu).
 cudaError_t launch_das_group(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
-size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileRows, unsigned capBytes, unsigned stages);
+size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileCols, unsigned tileRows, unsigned capBytes,
+		unsigned stages);
+// Tile columns of a delay-and-sum variant.
+inline unsigned das_tile_cols(int variant) { return variant == 3 ? 64u : 32u; }
 
 // ---------------------------------------------------------------------------
 // Batched (multi-frame) launches: persistent blocks walk the work items of
@@ -124,14 +130,14 @@ struct BatchPrepFrame {
 struct BatchDasFrame {
 	DasParams das;
 	unsigned tileBegin;      // first global tile index of the frame
-	unsigned tilesX;         // tiles per row of tiles (32-column tiles)
+	unsigned tilesX;         // tiles per row of tiles
 	int cf;
 	unsigned pad;
 };
 
 struct BatchDasConfig {
 	unsigned maxTx, maxRx;   // layout limits of the shared memory
-	unsigned tileRows, stageBytes, stages;
+	unsigned tileCols, tileRows, stageBytes, stages;
 	unsigned blocks;         // persistent grid size (0: as many blocks as the SMs hold)
 };
 

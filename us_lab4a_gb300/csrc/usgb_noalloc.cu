@@ -233,6 +233,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	dp.value = d_value;
 	dp.factor = d_factor;
 	dp.errWord = reinterpret_cast<unsigned*>(base + lay.err);
+	dp.tileCols = 32;
 	dp.tileRows = 8;
 	dp.stageBytes = 16384;
 	dp.stages = 4;
