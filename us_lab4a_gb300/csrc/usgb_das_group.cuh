@@ -45,6 +45,10 @@ using namespace tile;
 
 constexpr int kGroup = 8;                  // receivers per group
 constexpr int kMaxUnits = 32 / kGroup;     // units sized per producer pass (one lane per window)
+// Unit flag: every window of the unit is staged whole, without clamping to
+// the A-scan, so every delay of the tile for those pairs gives an index in
+// [0, L - 2] and the gathers need no range test.
+constexpr unsigned kUnitInterior = 0x100u;
 
 // One stage: up to kMaxUnits units (consecutive transmitters of one receiver
 // group). Window j of unit u: sample idx of receiver g * kGroup + j sits at
@@ -54,7 +58,7 @@ struct GroupStage {
 	int lastOfGroup;  // the stage ends its receiver group
 	int anyGlobal;    // some window is gathered from global memory
 	int pad;
-	int2 unit[kMaxUnits];           // (transmitter, bit j set: window j from global memory)
+	int2 unit[kMaxUnits];           // (transmitter, bit j set: window j from global memory; kUnitInterior)
 	int base[kMaxUnits][kGroup];
 };
 static_assert(sizeof(GroupStage) % 16 == 0, "stage metadata must stay 16-byte aligned");
@@ -173,9 +177,11 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 			const unsigned t = t0 + u;
 			int lo = 0, kind = kEmptyWindow;
 			unsigned wb = 0;
+			bool interior = false;   // the window needs no clamping to the A-scan
 			if (t < p.numTx && r < p.numRx) {
 				const float a = __fadd_rn(sm.minT[t], sm.minR[r]);
 				const float b = __fadd_rn(sm.maxT[t], sm.maxR[r]);
+				interior = floorf(a) - margin >= 0.0f && floorf(b) + 1.0f + margin <= static_cast<float>(L - 1);
 				const float lof = fmaxf(floorf(a) - margin, 0.0f);
 				const float hif = fminf(floorf(b) + 1.0f + margin, static_cast<float>(L - 1));
 				if (lof <= static_cast<float>(L - 2) && hif >= 1.0f && hif >= lof) {
@@ -201,12 +207,16 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 			const bool fits = t < p.numTx && unitEnd <= capBytes;
 			const int n = __popc(__ballot_sync(0xffffffffu, fits && j == 0));
 			const unsigned globalBits = __ballot_sync(0xffffffffu, kind == kGlobalWindow && u < n);
+			const unsigned interiorBits = __ballot_sync(0xffffffffu, interior && kind == 0);
 			const unsigned total = __shfl_sync(0xffffffffu, incl, n * kGroup - 1);
 			const unsigned excl = incl - wb;
 			GroupStage& m = sm.meta[s];
 			if (u < n) {
 				m.base[u][j] = (kind == 0) ? static_cast<int>(excl / sizeof(T)) - lo : 0;
-				if (j == 0) m.unit[u] = make_int2(static_cast<int>(t), static_cast<int>((globalBits >> (u * kGroup)) & 0xffu));
+				if (j == 0) {
+					const unsigned inside = ((interiorBits >> (u * kGroup)) & 0xffu) == 0xffu ? kUnitInterior : 0u;
+					m.unit[u] = make_int2(static_cast<int>(t), static_cast<int>(((globalBits >> (u * kGroup)) & 0xffu) | inside));
+				}
 			}
 			if (lane == 0) {
 				m.count = n;
@@ -251,7 +261,14 @@ __device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un,
 		const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
 {
 	using T = typename SP::T;
-	if (!anyGlobal) {
+	if (FULL && (un.y & kUnitInterior)) {
+#pragma unroll
+		for (int j = 0; j < kGroup; ++j) {
+			float k;
+			const int i = Delay<Q>::split(txv, rxd[j], k, fx);
+			SP::accumulate(buf + (i + base[j]), k, acc[j]);
+		}
+	} else if (!anyGlobal) {
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
 			if (FULL || static_cast<unsigned>(j) < nrg) gather_staged<SP, Q>(buf, base[j], txv, rxd[j], lastIdx, fx, zero, acc[j]);
@@ -272,18 +289,32 @@ __device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un,
 	}
 }
 
-// One unit u of stage m: its transmitter's delay once, then the group's gathers.
+// One unit u of stage m with its transmitter's delay txv: the group's gathers.
 template<typename SP, bool Q, bool FULL>
-__device__ __forceinline__ void group_unit(const DasParams& p, const GroupSmem& sm, const GroupStage& m, int u,
+__device__ __forceinline__ void group_unit(const DasParams& p, const GroupStage& m, int u, float txv,
 		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
-		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+		const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
 {
 	const int2 un = m.unit[u];
-	const float txv = Delay<Q>::tx(p, sm.txinfo[un.x], px, py, pz, fx);
 	const int4 b0 = *reinterpret_cast<const int4*>(&m.base[u][0]);
 	const int4 b1 = *reinterpret_cast<const int4*>(&m.base[u][4]);
 	const int base[kGroup] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 	group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, acc);
+}
+
+// The units of stage m (at least one), each unit's transmit delay computed
+// one unit ahead so that its square root overlaps the previous unit's gathers.
+template<typename SP, bool Q, bool FULL>
+__device__ __forceinline__ void group_stage_units(const DasParams& p, const GroupSmem& sm, const GroupStage& m,
+		int count, const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
+		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+{
+	float txNext = Delay<Q>::tx(p, sm.txinfo[m.unit[0].x], px, py, pz, fx);
+	for (int u = 0; u < count; ++u) {
+		const float txv = txNext;
+		if (u + 1 < count) txNext = Delay<Q>::tx(p, sm.txinfo[m.unit[u + 1].x], px, py, pz, fx);
+		group_unit<SP, Q, FULL>(p, m, u, txv, buf, zero, anyGlobal, g, nrg, rxd, lastIdx, fx, acc);
+	}
 }
 
 template<typename SP, int CF, bool Q>
@@ -319,15 +350,11 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
 			const int4 head = *reinterpret_cast<const int4*>(&m.count);
 			if (nrg == static_cast<unsigned>(kGroup)) {
-				for (int u = 0; u < head.x; ++u) {
-					group_unit<SP, Q, true>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
-							acc);
-				}
+				group_stage_units<SP, Q, true>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx,
+						fx, acc);
 			} else {
-				for (int u = 0; u < head.x; ++u) {
-					group_unit<SP, Q, false>(p, sm, m, u, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx, fx,
-							acc);
-				}
+				group_stage_units<SP, Q, false>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx,
+						fx, acc);
 			}
 			last = head.y != 0;
 			__syncwarp();
