@@ -229,13 +229,35 @@ def run_gpu(args):
         del sig_t
     das_cfg = eng.das_config()
 
+    # A stream of frames: `pipeline` contexts, each on its own stream, take
+    # the frames in turn, so one frame's preparation runs while the previous
+    # frame's delay-and-sum finishes its last wave of tiles (SMs that would
+    # idle). Every frame is prepared and imaged in full; the outputs of the
+    # contexts are separate buffers.
+    engines, streams, values, factors = [eng], [stream], [value], [factor]
+    for _ in range(args.pipeline - 1):
+        e = StaEngine(spec)
+        st = torch.cuda.Stream(device=dev)
+        e.set_stream(st)
+        e.set_grid_device(grid)
+        if das_cfg["variant"] == 0:
+            e.set_das_variant(0)
+        else:
+            e.set_das_variant(das_cfg["variant"], das_cfg["tile_rows"], das_cfg["stage_bytes"], das_cfg["stages"])
+        engines.append(e)
+        streams.append(st)
+        values.append(torch.empty_like(value))
+        factors.append(torch.empty_like(factor))
+
     def step(i):
-        eng.process_device(rfs[i % len(rfs)], value, factor)
+        k = i % len(engines)
+        engines[k].process_device(rfs[i % len(rfs)], values[k], factors[k])
 
     for i in range(args.warmup):
         step(i)
-    stream.synchronize()
-    eng.synchronize()
+    for st, e in zip(streams, engines):
+        st.synchronize()
+        e.synchronize()
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -246,17 +268,28 @@ def run_gpu(args):
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
+    for st in streams[1:]:
+        st.wait_event(t_start)
     for i in range(args.steps):
-        evs[i][0].record(stream)
+        st = streams[i % len(streams)]
+        evs[i][0].record(st)
         step(i)
-        evs[i][1].record(stream)
+        evs[i][1].record(st)
+    for st in streams[1:]:
+        done = torch.cuda.Event()
+        done.record(st)
+        stream.wait_event(done)
     t_end.record(stream)
     stream.synchronize()
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    eng.synchronize()
+    for e in engines:
+        e.synchronize()
+    for e in engines[1:]:
+        e.close()
+    del engines[1:], values[1:], factors[1:]
     total_ms = t_start.elapsed_time(t_end)
     per_step = [a.elapsed_time(b) for a, b in evs]
     if world > 1:
@@ -299,18 +332,47 @@ def run_gpu(args):
     # End to end through the host entry points (host RF in, host image out).
     e2e = None
     if not args.no_e2e:
+        # Host RF in, host image out, through usgb_process_rf: `pipeline`
+        # host threads, each with its own context, take the frames in turn
+        # (the native call releases the interpreter, so the frames overlap as
+        # in the resident measurement); latency is per call.
         rf_host = rf0.cpu().numpy()
-        for i in range(args.warmup):
-            eng.process_host(rf_host)
-        lat = []
+        hosts = [eng]
+        for _ in range(args.pipeline - 1):
+            e = StaEngine(spec)
+            e.set_grid_device(grid)
+            if das_cfg["variant"] == 0:
+                e.set_das_variant(0)
+            else:
+                e.set_das_variant(das_cfg["variant"], das_cfg["tile_rows"], das_cfg["stage_bytes"], das_cfg["stages"])
+            hosts.append(e)
+        for e in hosts:
+            for i in range(args.warmup):
+                e.process_host(rf_host)
+        lat = [[] for _ in hosts]
+        start = threading.Barrier(len(hosts) + 1)
+
+        def host_worker(k):
+            start.wait()
+            for i in range(k, args.steps, len(hosts)):
+                s0 = time.perf_counter()
+                hosts[k].process_host(rf_host)
+                lat[k].append(time.perf_counter() - s0)
+
+        workers = [threading.Thread(target=host_worker, args=(k,)) for k in range(len(hosts))]
+        for w in workers:
+            w.start()
+        start.wait()
         t0 = time.perf_counter()
-        for i in range(args.steps):
-            s0 = time.perf_counter()
-            eng.process_host(rf_host)
-            lat.append(time.perf_counter() - s0)
+        for w in workers:
+            w.join()
         e2e_s = time.perf_counter() - t0
+        for e in hosts[1:]:
+            e.close()
+        lat = [x for per in lat for x in per]
         e2e = {"value": world * args.steps / e2e_s if world == 1 else None, "unit": "frames/s",
                "h2d_bytes_per_step": int(rf_host.nbytes), "d2h_bytes_per_step": int(2 * frame.npix * 4),
+               "host_threads": len(hosts),
                "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99))}
         if world > 1:
             t = torch.tensor([e2e_s], device=dev)
@@ -352,6 +414,7 @@ def run_gpu(args):
                            + f"{das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
                            + (", autotuned)" if args.autotune else ")")),
                        "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
+                       "frames_in_flight": f"{args.pipeline} contexts on {args.pipeline} streams take the frames in turn",
                        "parallelism": f"replicas x{world}"},
             "voxels_per_s": fps * frame.npix,
             "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
@@ -733,6 +796,8 @@ def main():
     ap.add_argument("--stages", type=int, default=2)
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--pipeline", type=int, default=2,
+                    help="contexts (and streams) that take the resident frames in turn (1: one frame at a time)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the 48-frame mixed-size / serving section")
     ap.add_argument("--no-single", action="store_true", help="skip the single-term 3D processor section")
