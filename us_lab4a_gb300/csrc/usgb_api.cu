@@ -63,6 +63,7 @@ struct usgb_ctx {
 	float* d_rxXY = nullptr;
 	float* d_apod = nullptr;
 	float* d_polyTaps = nullptr;
+	std::vector<float> polyHost;   // the same taps, for the launch parameters
 	float2* d_tw = nullptr;
 	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
@@ -143,6 +144,7 @@ void build_tables(usgb_ctx* c)
 	}
 	c->tapsPerPhase = poly.tapsPerPhase;
 	c->tapsStride = poly.tapsStride;
+	c->polyHost = poly.poly;
 	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.poly.size() * sizeof(float)));
 	USGB_CUDA(cudaMemcpy(c->d_polyTaps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice));
 
@@ -267,6 +269,7 @@ usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
 	pp.tapsPerPhase = c->tapsPerPhase;
 	pp.tapsStride = c->tapsStride;
 	pp.polyTaps = c->d_polyTaps;
+	usgb::host::set_param_taps(pp, c->polyHost);
 	pp.deadZone = c->deadZone;
 	pp.outScale = c->scale;
 	if (c->analytic) {

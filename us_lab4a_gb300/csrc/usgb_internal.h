@@ -11,6 +11,10 @@ constexpr int kPrepThreads = 512;
 constexpr int kMaxFFTStages = 24;
 constexpr unsigned kTwiddleSplit = 128;   // two-level twiddle tables: W^m = hi[m / 128] * lo[m % 128]
 constexpr unsigned kHilbertSkip = 0xFFFFFFFFu;
+// FIR taps copied into the launch parameters for the specialised FIR shapes
+// (U x tapsStride: 8 phases x 28 at most), read there as constant-bank
+// operands instead of shared-memory loads.
+constexpr unsigned kParamTaps = 224;
 constexpr unsigned kHilbertSwap = 0x80000000u;
 // FP32 delays (a sum of two rounded products of rounded distances) are off by
 // at most about 8 * 2^-24 * d samples; above 32768 samples that can exceed
@@ -30,6 +34,7 @@ struct PrepParams {
 	unsigned tapsStride;         // tapsPerPhase rounded up to a multiple of 4
 	const float* polyTaps;       // U x tapsStride, polyTaps[r][t] = h[r + tU] (zero padded)
 	unsigned deadZone;           // first sample of the DC mean
+	float paramTaps[kParamTaps]; // polyTaps again when U * tapsStride <= kParamTaps (single-frame launches)
 	float outScale;              // applied before storage (1 for FP32)
 	// Hilbert FFT (analytic path): M = N/2 complex points.
 	unsigned M;

@@ -191,6 +191,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	pp.L = L;
 	pp.tapsPerPhase = poly.tapsPerPhase;
 	pp.tapsStride = poly.tapsStride;
+	usgb::host::set_param_taps(pp, poly.poly);
 	pp.polyTaps = reinterpret_cast<const float*>(base + lay.taps);
 	pp.deadZone = static_cast<unsigned>(dzd);
 	const float scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;

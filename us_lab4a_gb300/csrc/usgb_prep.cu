@@ -408,9 +408,25 @@ __device__ __forceinline__ float4 lds_taps(const float* p)
 	return v;
 }
 
+// Four taps from shared memory, or (PT) from the launch parameters, where the
+// compile-time offsets make them constant-bank operands of the FMAs.
+template<bool PT>
+__device__ __forceinline__ float4 tap4(const float* h)
+{
+	if constexpr (PT) {
+		return make_float4(h[0], h[1], h[2], h[3]);
+	} else {
+		return lds_taps(h);
+	}
+}
+
+// Whether a specialised FIR shape's taps fit in PrepParams::paramTaps.
+template<int NT, int U>
+__host__ __device__ constexpr bool param_taps_fit() { return NT > 0 && U * ((NT + 3) & ~3) <= static_cast<int>(kParamTaps); }
+
 // The U upsampled outputs of input position b: x[bU + r] = sum_t h[r][t] *
 // rf[b + K - t] (rfs holds rf shifted by K).
-template<int NT, int U>
+template<int NT, int U, bool PT = false>
 __device__ __forceinline__ void fir_outputs(const float* rfs, const float* taps, unsigned b, float* out)
 {
 	constexpr int NTP = (NT + 3) & ~3;
@@ -425,7 +441,7 @@ __device__ __forceinline__ void fir_outputs(const float* rfs, const float* taps,
 		float acc = 0.f;
 #pragma unroll
 		for (int q = 0; q < NTP / 4; ++q) {
-			const float4 c = lds_taps(h + 4 * q);
+			const float4 c = tap4<PT>(h + 4 * q);
 			acc = fmaf(c.x, win[4 * q], acc);
 			if (4 * q + 1 < NT) acc = fmaf(c.y, win[4 * q + 1], acc);
 			if (4 * q + 2 < NT) acc = fmaf(c.z, win[4 * q + 2], acc);
@@ -451,7 +467,7 @@ __device__ __forceinline__ float fir_one(const float* rfs, const float* taps, un
 // Pass 1: x[n] for n < L into xs (float view), partial sum of [deadZone, L).
 // fir_outputs for two input positions b0 and b1 at once: each broadcast tap
 // load serves both windows (half the tap traffic of two single calls).
-template<int NT, int U>
+template<int NT, int U, bool PT>
 __device__ __forceinline__ void fir_outputs2(const float* rfs, const float* taps, unsigned b0, unsigned b1,
 		float* out0, float* out1)
 {
@@ -470,7 +486,7 @@ __device__ __forceinline__ void fir_outputs2(const float* rfs, const float* taps
 		float a0 = 0.f, a1 = 0.f;
 #pragma unroll
 		for (int q = 0; q < NTP / 4; ++q) {
-			const float4 c = lds_taps(h + 4 * q);
+			const float4 c = tap4<PT>(h + 4 * q);
 			a0 = fmaf(c.x, w0[4 * q], a0);
 			a1 = fmaf(c.x, w1[4 * q], a1);
 			if (4 * q + 1 < NT) { a0 = fmaf(c.y, w0[4 * q + 1], a0); a1 = fmaf(c.y, w1[4 * q + 1], a1); }
@@ -504,7 +520,7 @@ __device__ __forceinline__ void fir_keep(const PrepParams& p, unsigned b, const 
 	}
 }
 
-template<int NT, int U>
+template<int NT, int U, bool PT>
 __device__ float fir_pass(const PrepParams& p, const float* rfs, const float* taps, float* xs)
 {
 	float part = 0.f;
@@ -514,14 +530,14 @@ __device__ float fir_pass(const PrepParams& p, const float* rfs, const float* ta
 			const unsigned b1 = b + blockDim.x;
 			const bool two = b1 < p.ns;
 			float o0[U], o1[U];
-			fir_outputs2<NT, U>(rfs, taps, b, two ? b1 : b, o0, o1);
+			fir_outputs2<NT, U, PT>(rfs, taps, b, two ? b1 : b, o0, o1);
 			fir_keep<U>(p, b, o0, xs, part);
 			if (two) fir_keep<U>(p, b1, o1, xs, part);
 		}
 	} else if constexpr (NT > 0) {
 		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
 			float o[U];
-			fir_outputs<NT, U>(rfs, taps, b, o);
+			fir_outputs<NT, U, PT>(rfs, taps, b, o);
 			fir_keep<U>(p, b, o, xs, part);
 		}
 	} else {
@@ -561,7 +577,7 @@ __device__ void store_imag_pass(const PrepParams& p, const float* ys, unsigned a
 }
 
 // Store pass of the real-RF path: x[n] - mean, with x recomputed from the A-scan.
-template<int S, int NT, int U>
+template<int S, int NT, int U, bool PT>
 __device__ void store_real_pass(const PrepParams& p, const float* rfs, const float* taps, float mean, unsigned a)
 {
 	const float sc = p.outScale;
@@ -570,7 +586,7 @@ __device__ void store_real_pass(const PrepParams& p, const float* rfs, const flo
 	if constexpr (NT > 0) {
 		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
 			float o[U];
-			fir_outputs<NT, U>(rfs, taps, b, o);
+			fir_outputs<NT, U, PT>(rfs, taps, b, o);
 #pragma unroll
 			for (int r = 0; r < U; ++r) out[b * U + r] = Real<S>::pack((o[r] - mean) * sc);
 		}
@@ -611,8 +627,9 @@ __device__ __forceinline__ void hilbert_pair(float2* data, unsigned i, const flo
 // Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
 // the generic FIR loop. ENV: the envelope of the input itself instead
 // (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
-// used with U = 1 on image columns).
-template<int S, int NT, int U, bool ENV = false>
+// used with U = 1 on image columns). PT: FIR taps from p.paramTaps (p a
+// launch parameter) instead of shared memory.
+template<int S, int NT, int U, bool ENV = false, bool PT = false>
 __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 {
 	const PrepLayout lay(p, true);
@@ -620,7 +637,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	float2* data = reinterpret_cast<float2*>(sm + lay.data);
 	float* xs = sm + lay.data;  // the packed complex buffer read as floats: x[n] at n
 	const float* rfs = sm + lay.rfs;
-	const float* taps = sm + lay.taps;
+	const float* taps = PT ? p.paramTaps : sm + lay.taps;
 	const float2* twLo = reinterpret_cast<const float2*>(sm + lay.twLo);
 	const float2* twHi = reinterpret_cast<const float2*>(sm + lay.twHi);
 	const float2* stw = p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr;
@@ -628,7 +645,7 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 
 	// 1. Upsampled signal into the packed buffer, zero past L.
 	for (unsigned n = L + threadIdx.x; n < 2 * p.M; n += blockDim.x) xs[n] = 0.f;
-	const float part = fir_pass<NT, U>(p, rfs, taps, xs);
+	const float part = fir_pass<NT, U, PT>(p, rfs, taps, xs);
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
 	//    (block_sum's barriers also order the writes above).
 	//    The real parts of the output, (x[n] - mean) * scale, are stored here
@@ -692,14 +709,15 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 }
 
 // Real-RF path: upsampling (fixed 4x FIR) and DC removal only.
-template<int S, int NT, int U>
+template<int S, int NT, int U, bool PT = false>
 __device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
 {
 	const PrepLayout lay(p, false);
 	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
-	const float part = fir_pass<NT, U>(p, sm + lay.rfs, sm + lay.taps, nullptr);
+	const float* taps = PT ? p.paramTaps : sm + lay.taps;
+	const float part = fir_pass<NT, U, PT>(p, sm + lay.rfs, taps, nullptr);
 	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
-	store_real_pass<S, NT, U>(p, sm + lay.rfs, sm + lay.taps, mean, a);
+	store_real_pass<S, NT, U, PT>(p, sm + lay.rfs, taps, mean, a);
 	__syncthreads();
 }
 
@@ -708,18 +726,20 @@ __device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
 // 512 threads with most of them idle in the FFT stages).
 template<int S, int NT, int U, int T>
 __global__ void __launch_bounds__(T, kPrepThreads / T)
-prep_analytic_kernel(PrepParams p)
+prep_analytic_kernel(const __grid_constant__ PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
-	prep_analytic_body<S, NT, U>(p, blockIdx.x, sm);
+	prep_analytic_body<S, NT, U, false, param_taps_fit<NT, U>()>(p, blockIdx.x, sm);
 }
 
 template<int S, int NT, int U, int T>
 __global__ void __launch_bounds__(T, kPrepThreads / T)
-prep_real_kernel(PrepParams p)
+prep_real_kernel(const __grid_constant__ PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
-	prep_real_body<S, NT, U>(p, blockIdx.x, sm);
+	// (U = 8 on the real path would hold its 224 loop-invariant taps in
+	// registers; that shape keeps them in shared memory.)
+	prep_real_body<S, NT, U, param_taps_fit<NT, U>() && U <= 4>(p, blockIdx.x, sm);
 }
 
 // FIR shapes with specialised code: the processors' Kaiser-sinc FIR (half
@@ -741,13 +761,20 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 {
 	extern __shared__ __align__(16) float sm[];
 	__shared__ PrepParams sp;
+	static_assert(sizeof(PrepParams) % 8 == 0 && alignof(PrepParams) == 8, "PrepParams is copied as 8-byte words");
 	const unsigned count = hdr->count;
 	const unsigned total = hdr->totalSignals;
-	unsigned f = 0;
+	unsigned f = 0, loaded = ~0u;
 	for (unsigned g = blockIdx.x; g < total; g += gridDim.x) {
 		while (f + 1 < count && frames[f + 1].signalBegin <= g) ++f;
-		__syncthreads();
-		if (threadIdx.x == 0) sp = frames[f].prep;
+		__syncthreads();  // the previous A-scan is done with sp
+		if (f != loaded) {
+			// The frame's parameters into shared memory, by the whole block.
+			const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&frames[f].prep);
+			unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sp);
+			for (unsigned i = threadIdx.x; i < sizeof(PrepParams) / 8; i += blockDim.x) dst[i] = src[i];
+			loaded = f;
+		}
 		__syncthreads();
 		const unsigned a = g - frames[f].signalBegin;
 		const int shape = fir_shape(sp.tapsPerPhase, sp.U);

@@ -334,6 +334,7 @@ struct usgb_single {
 	float* d_rxXY = nullptr;
 	float* d_apod = nullptr;
 	float* d_polyTaps = nullptr;
+	std::vector<float> polyHost;   // the same taps, for the launch parameters
 	float2* d_tw = nullptr;
 	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
@@ -468,6 +469,7 @@ void build_tables(usgb_single* c)
 	}
 	c->tapsPerPhase = poly.tapsPerPhase;
 	c->tapsStride = poly.tapsStride;
+	c->polyHost = poly.poly;
 	auto upload = [](auto** dst, const auto& v) {
 		using E = typename std::decay_t<decltype(v)>::value_type;
 		SINGLE_CUDA(cudaMalloc(dst, std::max<size_t>(v.size(), 1) * sizeof(E)));
@@ -496,6 +498,7 @@ usgb::PrepParams prep_params(const usgb_single* c, const float* d_rf, void* d_ou
 	pp.tapsPerPhase = c->tapsPerPhase;
 	pp.tapsStride = c->tapsStride;
 	pp.polyTaps = c->d_polyTaps;
+	usgb::host::set_param_taps(pp, c->polyHost);
 	pp.deadZone = c->deadZone;
 	pp.outScale = c->scale;
 	usgb::host::set_fft_params(pp, c->fft);

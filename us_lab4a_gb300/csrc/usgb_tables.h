@@ -129,6 +129,14 @@ inline bool make_poly_taps(bool analytic, unsigned U, PolyTaps& out)
 	return true;
 }
 
+// Copies the polyphase taps into the launch parameters (zero past them; the
+// specialised FIR kernels read them only when they fit).
+inline void set_param_taps(PrepParams& pp, const std::vector<float>& poly)
+{
+	std::fill(pp.paramTaps, pp.paramTaps + kParamTaps, 0.f);
+	std::copy(poly.begin(), poly.begin() + std::min<size_t>(poly.size(), kParamTaps), pp.paramTaps);
+}
+
 // Plan of the Hilbert FFT of an L-sample A-scan: N = max(nextFastEvenSize(L +
 // 1024), 2048) (src/util/HilbertEnvelope.h:152), computed as an M = N/2-point
 // complex FFT.

@@ -420,6 +420,7 @@ struct usgb_two_medium {
 	size_t elemBytes = 0, rfFloats = 0, sigBytes = 0;
 	float scale = 1, pcfFactor = 0, signalOffset = 0;
 	float* d_polyTaps = nullptr;
+	std::vector<float> polyHost;   // the same taps, for the launch parameters
 	float2* d_tw = nullptr;
 	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
@@ -518,6 +519,7 @@ usgb::PrepParams prep_params(const usgb_two_medium* c, const float* d_rf)
 	pp.tapsPerPhase = c->tapsPerPhase;
 	pp.tapsStride = c->tapsStride;
 	pp.polyTaps = c->d_polyTaps;
+	usgb::host::set_param_taps(pp, c->polyHost);
 	pp.deadZone = 0;  // Util::removeDC(signal, size): the mean of the whole A-scan
 	pp.outScale = c->scale;
 	usgb::host::set_fft_params(pp, c->fft);
@@ -535,6 +537,7 @@ void build_tables(usgb_two_medium* c)
 	}
 	c->tapsPerPhase = poly.tapsPerPhase;
 	c->tapsStride = poly.tapsStride;
+	c->polyHost = poly.poly;
 	auto upload = [](auto** dst, const auto& v) {
 		using E = typename std::decay_t<decltype(v)>::value_type;
 		TM_CUDA(cudaMalloc(dst, std::max<size_t>(v.size(), 1) * sizeof(E)));
