@@ -11,10 +11,12 @@
 // Four launches besides the preparation: the first imaged row of every
 // column, the medium-1 path table (element x interface point), the delay
 // table (one thread per column and element walks down the column, each row's
-// search starting at the previous row's interface point) and the image (one
-// thread per grid point and step, gathering over the step's transmit x
-// receive pairs from the table; the warps of a block take different steps of
-// the same 32 points). Every delay is rounded as the reference's float arithmetic
+// search starting at the previous row's interface point; columns fastest) and
+// the image (one thread per grid point and step, gathering over the step's
+// transmit x receive pairs from the table; a warp spans 32 neighbouring
+// columns of one row, whose delays differ by a few samples, so both the table
+// reads and the sample gathers of a warp fall on few sectors; the warps of a
+// block take different steps of the same 32 points). Every delay is rounded as the reference's float arithmetic
 // (no contraction, IEEE division and square root), so the searches pick the
 // same interface points and each gather reads the same samples with the same
 // weight; terms are summed in the reference's order.
@@ -58,7 +60,7 @@ struct TmParams {
 	float fsInvC2;               // fs * U / c2
 	unsigned* minRow;            // ncols: first imaged row
 	float* medium1;              // mux x nIf: element -> interface point, in medium-2 length
-	float* delay;                // (col, element, row), samples
+	float* delay;                // (row, element, col), samples
 	// Image.
 	const void* sig;             // (acquisition, tx, rx, sigStride) samples (storage type)
 	size_t acqStride, txStride, sigStride;
@@ -168,11 +170,12 @@ __global__ void __launch_bounds__(kTmThreads) tm_delay_kernel(const __grid_const
 {
 	const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= p.ncols * p.mux) return;
-	const unsigned col = t / p.mux, elem = t % p.mux;
+	const unsigned col = t % p.ncols, elem = t / p.ncols;  // neighbouring threads: neighbouring columns
 	const unsigned r0 = p.minRow[col];
 	if (r0 >= p.nrows) return;
 	const float2* g = p.grid + static_cast<size_t>(col) * p.nrows;
-	float* out = p.delay + (static_cast<size_t>(col) * p.mux + elem) * p.nrows;
+	const size_t rs = static_cast<size_t>(p.mux) * p.ncols;   // table row stride
+	float* out = p.delay + static_cast<size_t>(elem) * p.ncols + col;
 	const float x1 = element_x(p, elem);
 	unsigned last;
 	{
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(kTmThreads) tm_delay_kernel(const __grid_const
 				idxMin = i;
 			}
 		}
-		out[r0] = __fmul_rn(tMin, p.fsUp);
+		out[r0 * rs] = __fmul_rn(tMin, p.fsUp);
 		// No finite travel time (NaN coordinates): walk from point 0 rather
 		// than from the search's "none" marker.
 		last = idxMin < p.nIf ? idxMin : 0U;
@@ -231,10 +234,12 @@ __global__ void __launch_bounds__(kTmThreads) tm_delay_kernel(const __grid_const
 				idxMin = static_cast<unsigned>(i);
 			}
 		}
-		out[row] = __fmul_rn(tMin, p.fsInvC2);
+		out[row * rs] = __fmul_rn(tMin, p.fsInvC2);
 		last = idxMin;
 	}
 }
+
+constexpr unsigned kTmTxShared = 32;   // transmit offsets per step kept in shared memory (per warp)
 
 // v0 + k (v1 - v0) at `position` (0 outside [0, L - 2]), times invScale for
 // FP16/BF16 storage.
@@ -256,8 +261,10 @@ __device__ __forceinline__ float2 interp(const typename Complex<S>::T* row, floa
 // receive elements (each the sum over the step's transmit elements, or the
 // single transmit element's term), weighted by the coherence factor of the
 // receive terms. ONE_TX: ProcessColumnWithOneTxElem; else ProcessColumn.
+// drow: the point's delay of element 0; element e at drow[e * nr].
 template<int S, int CF, bool ONE_TX>
-__device__ __forceinline__ float2 step_contribution(const TmParams& p, const uint4 st, const float* drow, size_t nr)
+__device__ __forceinline__ float2 step_contribution(const TmParams& p, const uint4 st, const float* drow, size_t nr,
+		float* txs)
 {
 	using CT = typename Complex<S>::T;
 	const unsigned maxPos = p.L - 2U;
@@ -275,13 +282,20 @@ __device__ __forceinline__ float2 step_contribution(const TmParams& p, const uin
 			cf.add(term);
 		}
 	} else {
+		// The step's transmit offsets once, in this warp's shared table (lane
+		// fastest: no bank conflicts), when there are at most kTmTxShared.
+		const unsigned ntx = st.w - st.z + 1U;
+		const bool shared = ntx <= kTmTxShared;
+		if (shared) {
+			for (unsigned tx = 0; tx < ntx; ++tx) txs[tx * 32U] = __fadd_rn(p.signalOffset, d[(st.z + tx) * nr]);
+		}
 		for (unsigned rx = 0; rx < p.numElements; ++rx) {
 			const float rxDelay = d[rx * nr];
 			float2 acc = make_float2(0.f, 0.f);
 			const CT* sigRx = acq + rx * p.sigStride;
 #pragma unroll 4
 			for (unsigned tx = st.z; tx <= st.w; ++tx) {
-				const float txOffset = __fadd_rn(p.signalOffset, d[tx * nr]);
+				const float txOffset = shared ? txs[(tx - st.z) * 32U] : __fadd_rn(p.signalOffset, d[tx * nr]);
 				const float2 term = interp<S>(sigRx + (tx - st.z) * p.txStride, __fadd_rn(txOffset, rxDelay), maxPos,
 						p.invScale);
 				acc.x = __fadd_rn(acc.x, term.x);
@@ -300,30 +314,32 @@ __device__ __forceinline__ float2 step_contribution(const TmParams& p, const uin
 	return sum;
 }
 
-// A block covers kTmRows consecutive rows of one column (the lanes of a
-// warp, so the delay-table reads are coalesced) for kTmStepLanes steps at a
-// time (one warp per step); the steps' contributions meet in shared memory
-// and are added in step order, as the reference adds them.
-constexpr unsigned kTmRows = 32;
+// A block covers kTmCols neighbouring columns of one row (the lanes of a
+// warp: the delay-table reads are coalesced and the gathers of a warp fall on
+// few sectors) for kTmStepLanes steps at a time (one warp per step); the
+// steps' contributions meet in shared memory and are added in step order,
+// as the reference adds them.
+constexpr unsigned kTmCols = 32;
 constexpr unsigned kTmStepLanes = 8;
-constexpr int kTmImageThreads = kTmRows * kTmStepLanes;
+constexpr int kTmImageThreads = kTmCols * kTmStepLanes;
 
 template<int S, int CF, bool ONE_TX>
 __global__ void __launch_bounds__(kTmImageThreads, 4) tm_image_kernel(const __grid_constant__ TmParams p)
 {
-	__shared__ float2 contrib[kTmStepLanes][kTmRows];
-	const unsigned lane = threadIdx.x % kTmRows, sl = threadIdx.x / kTmRows;
-	const unsigned row = blockIdx.x * kTmRows + lane;
-	const unsigned col = blockIdx.y;
-	const bool inGrid = row < p.nrows;
+	__shared__ float2 contrib[kTmStepLanes][kTmCols];
+	__shared__ float txShared[kTmStepLanes][kTmTxShared * kTmCols];
+	const unsigned lane = threadIdx.x % kTmCols, sl = threadIdx.x / kTmCols;
+	const unsigned col = blockIdx.x * kTmCols + lane;
+	const unsigned row = blockIdx.y;
+	const bool inGrid = col < p.ncols;
 	const bool active = inGrid && row >= p.minRow[col];
-	const size_t nr = p.nrows;
-	const float* drow = p.delay + static_cast<size_t>(col) * p.mux * nr + row;
+	const size_t es = p.ncols;   // table element stride
+	const float* drow = p.delay + static_cast<size_t>(row) * p.mux * es + col;
 	float2 v = make_float2(0.f, 0.f);
 	for (unsigned s0 = 0; s0 < p.numSteps; s0 += kTmStepLanes) {
 		const unsigned s = s0 + sl;
 		float2 c = make_float2(0.f, 0.f);
-		if (active && s < p.numSteps) c = step_contribution<S, CF, ONE_TX>(p, p.steps[s], drow, nr);
+		if (active && s < p.numSteps) c = step_contribution<S, CF, ONE_TX>(p, p.steps[s], drow, es, &txShared[sl][lane]);
 		contrib[sl][lane] = c;
 		__syncthreads();
 		if (sl == 0 && active) {
@@ -335,13 +351,13 @@ __global__ void __launch_bounds__(kTmImageThreads, 4) tm_image_kernel(const __gr
 		}
 		__syncthreads();
 	}
-	if (sl == 0 && inGrid) p.out[static_cast<size_t>(col) * nr + row] = active ? v : make_float2(0.f, 0.f);
+	if (sl == 0 && inGrid) p.out[static_cast<size_t>(col) * p.nrows + row] = active ? v : make_float2(0.f, 0.f);
 }
 
 template<int S, int CF>
 cudaError_t launch_image_cf(const TmParams& p, bool oneTx, cudaStream_t st)
 {
-	const dim3 grid((p.nrows + kTmRows - 1) / kTmRows, p.ncols);
+	const dim3 grid((p.ncols + kTmCols - 1) / kTmCols, p.nrows);
 	if (oneTx) {
 		tm_image_kernel<S, CF, true><<<grid, kTmImageThreads, 0, st>>>(p);
 	} else {
