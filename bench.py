@@ -670,12 +670,21 @@ def _single_case(dev, name: str, storage: str, reps: int, threads: int):
     spec = oracle.SingleSpec(mode=mode, **kw)
     v64, _, _ = oracle.single(spec, rf_host, pts, dtype=np.float64)
     err_db = _db(float(np.abs(img[cols] - v64).max()), float(np.abs(v64).max()))
+    # Preparation alone (one grid point), best of two; then preparation plus
+    # 24 grid columns, enough points that the imaging part is most of the
+    # second timing (a difference of two preparation-dominated timings is
+    # noise).
+    t_prep = float("inf")
+    for _ in range(2):
+        t0 = time.perf_counter()
+        oracle.single(spec, rf_host, pts[:1, :1], dtype=np.float32)
+        t_prep = min(t_prep, time.perf_counter() - t0)
+    tcols = np.linspace(0, grid.shape[0] - 1, 24).astype(int)
+    tpts = grid[tcols]
     t0 = time.perf_counter()
-    oracle.single(spec, rf_host, pts[:, :1], dtype=np.float32)        # preparation (+ 3 points)
-    t_prep = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    oracle.single(spec, rf_host, pts, dtype=np.float32)
-    t_das = max(time.perf_counter() - t0 - t_prep, 1e-9) / (pts.shape[0] * (pts.shape[1] - 1))
+    oracle.single(spec, rf_host, tpts, dtype=np.float32)
+    t_all = time.perf_counter() - t0
+    t_das = max(t_all - t_prep, 0.5 * t_all) / (tpts.shape[0] * tpts.shape[1])
     npix = grid.shape[0] * grid.shape[1]
     # One frame of the CPU form prepares one acquisition and images the window.
     cpu_frame = t_prep / nacq + t_das * npix
@@ -683,7 +692,7 @@ def _single_case(dev, name: str, storage: str, reps: int, threads: int):
     return {"frames_per_s": 1e3 / ms, "ms_per_frame": ms, "terms_per_s": terms / (ms * 1e-3),
             "err_db_vs_fp64": err_db,
             "cpu_oracle": {"frames_per_s": 1.0 / cpu_frame, "cores": threads, "kind": "port",
-                           "sample": f"FP32 oracle: preparation of {n * nacq} A-scans and {pts.shape[0] * pts.shape[1]}"
+                           "sample": f"FP32 oracle: preparation of {n * nacq} A-scans and {tpts.shape[0] * tpts.shape[1]}"
                                      f" grid points, scaled to {npix} points"}}
 
 
