@@ -6,6 +6,7 @@
 // cos/sin(pi k / M).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
