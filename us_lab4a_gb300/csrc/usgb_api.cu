@@ -350,15 +350,17 @@ size_t max_smem()
 	return static_cast<size_t>(v);
 }
 
-// Default delay-and-sum kernel: the staged kernel with 32 x 8 tiles, 16 KiB
-// stages and the deepest pipeline that fits in shared memory (then 32 x 4
-// tiles), else the plain kernel.
+// Shared memory of a delay-and-sum configuration (variants 1-3).
 size_t das_smem_bytes(const usgb_ctx* c, int variant, unsigned rows, unsigned cap, unsigned nst)
 {
 	return variant >= 2 ? usgb::das_group_smem_bytes(c->prm.num_tx, c->prm.num_rx, usgb::das_tile_cols(variant), rows, cap, nst)
 	                    : usgb::das_staged_smem_bytes(c->prm.num_tx, c->prm.num_rx, rows, cap, nst);
 }
 
+// Default delay-and-sum kernel before a grid is known: the receiver-group
+// kernel on 32 x 4 tiles with 2 stages of 32, 16 or 8 KiB, whichever fits;
+// else the staged kernel with 32 x 8 (then 32 x 4) tiles, 16 KiB stages and
+// the deepest pipeline that fits; else the plain kernel.
 void choose_default_das(usgb_ctx* c)
 {
 	for (unsigned cap : {32768u, 16384u, 8192u}) {
