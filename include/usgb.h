@@ -179,9 +179,9 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * the copies staged per frame). 0 for tile_rows / stage_bytes / stages keeps
  * the current value. New
  * contexts start with the receiver-group kernel (32 x 4 tiles, 2 x 32 KiB)
- * where it fits; setting a grid of at least two 64 x 4 tiles per SM then
- * selects variant 3 (64 x 4, 2 x 48 KiB) where it fits, unless a variant was
- * set here or by usgb_autotune_das. */
+ * where it fits; setting a grid of at least two 64-column tiles per SM then
+ * selects variant 3 (64 x 8 with 2 x 96 KiB stages, else 64 x 4 with 2 x 48
+ * KiB) where it fits, unless a variant was set here or by usgb_autotune_das. */
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);

@@ -304,7 +304,31 @@ def test_grid_selects_tile_width(cuda):
         assert eng.das_config()["variant"] == 2
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
         cfg = eng.das_config()
-        assert cfg["variant"] == 3 and cfg["tile_rows"] == 4
+        assert cfg["variant"] == 3 and (cfg["tile_rows"], cfg["stage_bytes"]) in ((8, 98304), (4, 49152), (4, 32768))
         eng.set_das_variant(2, 8, 16384, 2)
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
         assert eng.das_config() == {"variant": 2, "tile_rows": 8, "stage_bytes": 16384, "stages": 2}
+
+
+@pytest.mark.parametrize("cfg", [(3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2)])
+def test_large_stages_equal_plain_kernel(cuda, cfg):
+    """Stages of 64-96 KiB (several units each, one block per SM) give the
+    plain kernel's images bit for bit (PCF, partial tiles, FP32 and FP16)."""
+    import torch
+    from us_lab4a_gb300 import StaEngine, workloads
+    for frame in (workloads.cf2d(small=True), workloads.with_storage(workloads.cf2d(small=True, coherence="mf"), "f16")):
+        rf = torch.as_tensor(frame.make_rf_numpy(), device=cuda)
+        g = torch.as_tensor(frame.grid_xyz, device=cuda)
+        out = []
+        for variant_cfg in ((0,), cfg):
+            with StaEngine(frame.spec) as eng:
+                eng.set_stream(torch.cuda.current_stream())
+                eng.set_das_variant(*variant_cfg)
+                eng.set_grid_device(g)
+                v = torch.empty(frame.grid_xyz.shape[:2], device=cuda)
+                f = torch.empty_like(v)
+                eng.process_device(rf, v, f)
+                eng.synchronize()
+                out.append((v.cpu().numpy(), f.cpu().numpy()))
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1], out[1][1])
