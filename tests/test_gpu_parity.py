@@ -304,13 +304,14 @@ def test_grid_selects_tile_width(cuda):
         assert eng.das_config()["variant"] == 2
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
         cfg = eng.das_config()
-        assert cfg["variant"] == 3 and (cfg["tile_rows"], cfg["stage_bytes"]) in ((8, 98304), (4, 49152), (4, 32768))
+        assert cfg["variant"] == 3 and (cfg["tile_rows"], cfg["stage_bytes"]) in ((8, 102400), (8, 98304), (4, 49152),
+                                                                                   (4, 32768))
         eng.set_das_variant(2, 8, 16384, 2)
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
         assert eng.das_config() == {"variant": 2, "tile_rows": 8, "stage_bytes": 16384, "stages": 2}
 
 
-@pytest.mark.parametrize("cfg", [(3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2)])
+@pytest.mark.parametrize("cfg", [(3, 8, 102400, 2), (3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2)])
 def test_large_stages_equal_plain_kernel(cuda, cfg):
     """Stages of 64-96 KiB (several units each, one block per SM) give the
     plain kernel's images bit for bit (PCF, partial tiles, FP32 and FP16)."""

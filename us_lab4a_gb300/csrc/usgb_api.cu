@@ -387,9 +387,10 @@ void choose_default_das(usgb_ctx* c)
 }
 
 // With the grid known: 64-column tiles where the grid gives at least two
-// tiles per SM and the shared memory fits — 64 x 8 with 2 x 96 KiB stages
-// (one block per SM; cf2d 1.80 ms), else 64 x 4 with 2 x 48 KiB (1.85 ms;
-// 32 x 4 with 2 x 32 KiB: 1.97 ms) — else the creation-time default.
+// tiles per SM and the shared memory fits — 64 x 8 with 2 x 100 or 96 KiB
+// stages (one block per SM; cf2d 1.77 / 1.80 ms), else 64 x 4 with 2 x 48
+// KiB (1.85 ms; 32 x 4 with 2 x 32 KiB: 1.97 ms) — else the creation-time
+// default.
 void choose_grid_das(usgb_ctx* c)
 {
 	choose_default_das(c);
@@ -399,7 +400,7 @@ void choose_grid_das(usgb_ctx* c)
 	if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return;
 	const size_t colTiles = (c->ncols + 63) / 64;
 	struct Shape { unsigned rows, cap; };
-	for (const Shape sh : {Shape{8u, 98304u}, Shape{4u, 49152u}, Shape{4u, 32768u}}) {
+	for (const Shape sh : {Shape{8u, 102400u}, Shape{8u, 98304u}, Shape{4u, 49152u}, Shape{4u, 32768u}}) {
 		const size_t tiles = colTiles * ((c->nrows + sh.rows - 1) / sh.rows);
 		if (tiles >= 2u * static_cast<size_t>(sms) && das_smem_bytes(c, 3, sh.rows, sh.cap, 2u) <= max_smem()) {
 			c->dasVariant = 3;
@@ -747,7 +748,7 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		std::vector<Cand> cands;
 		for (int variant : {1, 2, 3})
 			for (unsigned rows : {4u, 8u, 16u})
-				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u, 65536u, 98304u})
+				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u, 65536u, 98304u, 102400u})
 					for (unsigned nst : {2u, 3u, 4u})
 						if ((variant >= 2 || cap % 8192u == 0) && !(variant == 3 && rows == 16)
 								&& das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
