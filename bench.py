@@ -350,14 +350,18 @@ def run_gpu(args):
             for i in range(args.warmup):
                 e.process_host(rf_host)
         lat = [[] for _ in hosts]
+        failures = []
         start = threading.Barrier(len(hosts) + 1)
 
         def host_worker(k):
             start.wait()
-            for i in range(k, args.steps, len(hosts)):
-                s0 = time.perf_counter()
-                hosts[k].process_host(rf_host)
-                lat[k].append(time.perf_counter() - s0)
+            try:
+                for i in range(k, args.steps, len(hosts)):
+                    s0 = time.perf_counter()
+                    hosts[k].process_host(rf_host)
+                    lat[k].append(time.perf_counter() - s0)
+            except Exception as ex:  # reported after the join: a failed frame is no frame
+                failures.append(ex)
 
         workers = [threading.Thread(target=host_worker, args=(k,)) for k in range(len(hosts))]
         for w in workers:
@@ -367,6 +371,8 @@ def run_gpu(args):
         for w in workers:
             w.join()
         e2e_s = time.perf_counter() - t0
+        if failures:
+            raise failures[0]
         for e in hosts[1:]:
             e.close()
         lat = [x for per in lat for x in per]
