@@ -1,9 +1,9 @@
 // Receiver-group delay-and-sum: one thread block per tile of TCOLS (32 or
 // 64) columns x TROWS rows of grid points (lane = column, TCOLS / 32 warps a
 // row), like the staged kernel (usgb_das_staged.cu), but the pairs are
-// visited receiver group by receiver group: for each group of kGroup receivers, every transmitter in
-// turn, with the group's kGroup windows (one per receiver) staged together as
-// one unit. A consumer thread keeps the group's receive delays and its kGroup
+// visited receiver group by receiver group: for each group of kGroup
+// receivers, every transmitter in turn, with the group's kGroup windows (one
+// per receiver) staged together as one unit. A consumer thread keeps the group's receive delays and its kGroup
 // receiver sums in registers and computes each transmitter's delay once per
 // unit, so no per-pixel delay table lives in shared memory: a block holds
 // only its stage ring and a few per-element tables, several blocks fit on an
@@ -14,7 +14,11 @@
 // samples per row (45 on cf2d) and little across columns, so a wider tile
 // stages windows that are only a little longer for twice the points: 64 x 4
 // tiles stage 12.2 GB per cf2d frame against 16.4 GB for 32 x 4, with half as
-// many window copies, and one producer warp serves eight consumer warps.
+// many window copies, and one producer warp serves eight consumer warps;
+// 64 x 8 tiles with stages of ~100 KiB (one block of 16 consumer warps per
+// SM) stage 8.9 GB. Each stage is a barrier round trip gated by the slowest
+// consumer warp, so fewer, larger stages run faster than deeper rings of
+// small ones.
 //
 // Arithmetic is the plain kernel's, term for term: delay = fl(fl(offset +
 // fl(dist_tx * invCT)) + fl(dist_rx * invCT)), the same index / fraction
