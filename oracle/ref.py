@@ -15,7 +15,13 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(_HERE, "_ref", "libref.so")
-REF_SRC = "/root/reference/src"
+# The reference project's root: the environment variable US_LAB4A_REFERENCE,
+# else the read-only checkout this recipe was written against. Every user of
+# the reference sources (the refbuild Makefile, the fixture script, the tests
+# that read its test files or compile inside its headers) takes it from here.
+REF_ROOT = os.environ.get("US_LAB4A_REFERENCE") or "/root/reference"
+REF_SRC = os.path.join(REF_ROOT, "src")
+REF_TEST = os.path.join(REF_ROOT, "test")
 _lib = None
 
 
@@ -23,7 +29,7 @@ def build(force: bool = False) -> bool:
     """Compile libref.so when the reference sources are present."""
     if not os.path.isdir(REF_SRC):
         return False
-    cmd = ["make", "-s", "-C", os.path.join(_HERE, "refbuild")]
+    cmd = ["make", "-s", "-C", os.path.join(_HERE, "refbuild"), "REF=" + REF_ROOT]
     if force:
         cmd.append("-B")
     subprocess.run(cmd, check=True)
@@ -218,3 +224,16 @@ def two_medium(spec, rf: np.ndarray, grid_xz: np.ndarray, dtype=np.float32) -> n
     if rc != 0:
         raise RuntimeError(lib.ref_last_error().decode())
     return out.view(np.complex64 if dtype == np.float32 else np.complex128).reshape(g.shape[0], g.shape[1])
+
+
+def window(description: str, size: int) -> np.ndarray:
+    """The reference's WindowFunction::get<float>(description, size)
+    (src/util/WindowFunction.h:237-289), from the compiled reference."""
+    lib = _load()
+    f = lib.ref_window_f32
+    f.argtypes = [C.c_char_p, C.c_uint, C.POINTER(C.c_float)]
+    f.restype = C.c_int
+    out = np.zeros(max(size, 1), np.float32)
+    if f(description.encode(), size, out.ctypes.data_as(C.POINTER(C.c_float))) != 0:
+        raise ValueError(lib.ref_last_error().decode())
+    return out[:size]

@@ -25,6 +25,7 @@
 #include "Vectorial3DTnRnProcessor.h"
 #include "VectorialCombinedTwoMediumImagingProcessor.h"
 #include "VectorialSTAProcessor.h"
+#include "WindowFunction.h"
 #include "XYZValueFactor.h"
 
 using namespace Lab;
@@ -475,5 +476,22 @@ int ref_two_medium_f64(const RefTwoMediumDesc<double>* d, const double* rf, cons
 		double* out)
 {
 	return run_two_medium<double>(d, rf, grid, n1, n2, out);
+}
+// The reference's WindowFunction::get (src/util/WindowFunction.h:237-289) for
+// one description ("blackman", "trapezoidal 3 4 5", ...) and size, in float
+// (the apodization type of the float processors). Returns -1 with the
+// reference's exception message on an invalid description.
+int ref_window_f32(const char* description, unsigned size, float* out)
+{
+	try {
+		std::vector<float> w;
+		Lab::WindowFunction::get<float>(description, size, w);
+		if (w.size() != size) throw std::runtime_error("window size mismatch");
+		std::copy(w.begin(), w.end(), out);
+		return 0;
+	} catch (std::exception& e) {
+		g_err = e.what();
+		return -1;
+	}
 }
 }

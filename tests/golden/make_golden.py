@@ -17,12 +17,15 @@ sources are present; the fixtures are committed and travel with the tests).
    (Vectorial3DT1R1SAFTProcessor, Vectorial3DTnRnProcessor,
    SynthYVectorial3DTnRnProcessor) on a 6 x 5 matrix array, every input
    parameter stored beside the outputs.
-4. reference_two_medium.npz: the same for VectorialCombinedTwoMediumImagingProcessor
+4. reference_windows.npz: the reference's WindowFunction::get<float> for every
+   window name at sizes 2..256 and for trapezoidal descriptions (the
+   apodization vectors of the processors).
+5. reference_two_medium.npz: the same for VectorialCombinedTwoMediumImagingProcessor
    (one transmit element per step and STA steps, with and without PCF) on
    small two-medium scenes (noise-free RF, stored as FP16 values).
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
-           [--vectors-only | --single-only | --two-medium-only]
+Usage: python tests/golden/make_golden.py [--reference <reference root>]
+           [--vectors-only | --single-only | --two-medium-only | --windows-only]
 """
 from __future__ import annotations
 
@@ -264,13 +267,44 @@ def reference_two_medium_frames() -> dict:
     return out
 
 
+WINDOW_NAMES = ("rectangular", "triangular", "triangular2", "hanning", "hanning2", "hamming", "blackman",
+                "blackman2")
+WINDOW_SIZES = (2, 3, 4, 7, 8, 15, 16, 31, 32, 63, 64, 96, 127, 128, 256)
+TRAPEZOIDAL = (("trapezoidal", (1, 0, 1)), ("trapezoidal", (3, 4, 5)), ("trapezoidal", (8, 16, 8)),
+               ("trapezoidal", (0, 10, 6)), ("trapezoidal2", (3, 4, 5)), ("trapezoidal2", (16, 32, 16)),
+               ("trapezoidal2", (5, 0, 0)))
+
+
+def reference_windows() -> dict:
+    """reference_windows.npz: the reference's WindowFunction::get<float> for
+    every window name at the array sizes the processors use (and odd ones),
+    and the trapezoidal forms, from the compiled reference."""
+    from oracle import ref
+    out = {}
+    for name in WINDOW_NAMES:
+        for n in WINDOW_SIZES:
+            out[f"{name}/{n}"] = ref.window(name, n)
+    for name, (a, b, c) in TRAPEZOIDAL:
+        out[f"{name} {a} {b} {c}/{a + b + c}"] = ref.window(f"{name} {a} {b} {c}", a + b + c)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    from oracle.ref import REF_ROOT
+    ap.add_argument("--reference", default=REF_ROOT, help="reference project root (default: US_LAB4A_REFERENCE)")
     ap.add_argument("--vectors-only", action="store_true", help="rewrite reference_vectors.npz only")
     ap.add_argument("--single-only", action="store_true", help="rewrite reference_single.npz only")
     ap.add_argument("--two-medium-only", action="store_true", help="rewrite reference_two_medium.npz only")
+    ap.add_argument("--windows-only", action="store_true", help="rewrite reference_windows.npz only")
     args = ap.parse_args()
+    if args.windows_only:
+        from oracle import ref
+        if not ref.available():
+            ref.build()
+        np.savez_compressed(os.path.join(HERE, "reference_windows.npz"), **reference_windows())
+        print("reference_windows.npz", os.path.getsize(os.path.join(HERE, "reference_windows.npz")))
+        return
     if args.two_medium_only:
         from oracle import ref
         if not ref.available():
@@ -297,7 +331,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "reference_frames.npz"), **frames)
     np.savez_compressed(os.path.join(HERE, "reference_single.npz"), **reference_single_frames())
     np.savez_compressed(os.path.join(HERE, "reference_two_medium.npz"), **reference_two_medium_frames())
-    for f in ("reference_vectors.npz", "reference_frames.npz", "reference_single.npz", "reference_two_medium.npz"):
+    np.savez_compressed(os.path.join(HERE, "reference_windows.npz"), **reference_windows())
+    for f in ("reference_vectors.npz", "reference_frames.npz", "reference_single.npz", "reference_two_medium.npz",
+              "reference_windows.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-REF_TEST = "/root/reference/test"
+from oracle.ref import REF_TEST
 
 # golden vector -> reference test file (dataset "v")
 PAIRS = {

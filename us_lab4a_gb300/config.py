@@ -24,7 +24,7 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from .errors import InvalidParameterException, InvalidValueException
+from .errors import InvalidParameterException, InvalidValueException, MissingValueException
 
 PI = math.pi
 
@@ -360,6 +360,8 @@ def _fade(n: float, out: np.ndarray, at: int, second: bool, fade_out: bool) -> N
     i runs over 0 <= i < n (n may be non-integer); fadeIn writes i/n,
     fadeIn2 (i+1)/(n+1); the fade-outs write the same ramps mirrored over
     ceil(n) elements."""
+    if n <= 0:  # the reference's loop runs no iteration (its 1 / n is then inf, unused)
+        return
     c1 = 1.0 / (n + 1.0) if second else 1.0 / n
     m = int(math.ceil(n))
     i = 0
@@ -375,13 +377,14 @@ def window(description: str, size: int, dtype=np.float32) -> np.ndarray:
     "name nFadeIn nTop nFadeOut"; evaluated in double, stored as dtype."""
     parts = description.split()
     if not parts:
-        raise InvalidParameterException("Missing window function name.")
+        raise MissingValueException("Missing window function name.")
     name = parts[0]
     n = int(size)
     i = np.arange(n, dtype=np.float64)
     if name in ("trapezoidal", "trapezoidal2"):
-        if len(parts) < 4:
-            raise InvalidParameterException("Missing fade in/top/fade out sizes for the trapezoidal window function.")
+        for k, what in enumerate(("fade in", "top", "fade out")):
+            if len(parts) < 2 + k:
+                raise InvalidParameterException(f"Missing {what} size for the trapezoidal window function.")
         nin, ntop, nout = (int(x) for x in parts[1:4])
         if size != nin + ntop + nout:
             raise InvalidParameterException("Invalid total size for the trapezoidal window function.")

@@ -18,6 +18,10 @@ class InvalidStateException(Exception_):
     pass
 
 
+class MissingValueException(Exception_):
+    pass
+
+
 class CUDAException(Exception_):
     pass
 
