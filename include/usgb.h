@@ -239,11 +239,18 @@ int usgb_post_decibels_device(usgb_post* post, float* d_data, size_t n, float mi
  * uses, but calls whose GPU work overlaps race on it, so order them. The first
  * call on a device looks up the array's device address (cudaGetSymbolAddress)
  * with that device current; make that first call before any stream capture.
- * Asynchronous on cuda_stream (NULL = default stream). On failure the message
- * is copied into error_message (error_capacity bytes, may be NULL).
+ * Parameters are checked by the same rules, with the same messages, as
+ * usgb_create; grids above 2^31 points are rejected ("Grid too large.").
+ * d_status: optional device word for device-side failures. When given, the
+ * call clears it, the kernels set it (bit 0: a bounded delay-and-sum wait gave
+ * up, the image is incomplete) and the call returns without waiting for the
+ * GPU (asynchronous on cuda_stream, NULL = default stream); read the word with
+ * the images. When NULL, the call waits for its work on cuda_stream and
+ * returns USGB_ERR_DEVICE_TIMEOUT itself on such a failure. On failure the
+ * message is copied into error_message (error_capacity bytes, may be NULL).
  */
 int usgb_process_frame_noalloc(const usgb_sta_params* params, const float* d_rf, const float* d_grid_xyz,
-		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, void* cuda_stream,
+		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, uint32_t* d_status, void* cuda_stream,
 		char* error_message, size_t error_capacity);
 
 /*

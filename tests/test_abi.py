@@ -91,6 +91,51 @@ def test_create_rejects_invalid_frames(lib, field, value, status, msg):
     assert not h.value
 
 
+_NOALLOC_CASES = [
+    ("num_tx", 0, 1, "number of elements is zero"),
+    ("upsampling", 65, 2, "Invalid upsampling factor"),
+    ("dead_zone_m", 0.1, 2, "Invalid dead zone"),
+    ("coherence", 9, 1, "Invalid coherence factor"),
+    ("num_samples", 300000, 1, "greater than 1048576"),
+    ("pcf_gamma", float("nan"), 2, "Invalid phase_coherence_factor_gamma"),
+    ("pcf_gamma", 101.0, 2, "Invalid phase_coherence_factor_gamma"),
+    ("scf_p", -1.0, 2, "Invalid sign_coherence_factor_p"),
+]
+
+
+@pytest.mark.parametrize("field,value,status,msg", _NOALLOC_CASES)
+def test_noalloc_checks_like_create(lib, field, value, status, msg):
+    """usgb_process_frame_noalloc applies usgb_create's checks (one shared
+    function): same status, same message, before any device work."""
+    kw = {field: value}
+    if field == "pcf_gamma":
+        kw["coherence"] = 1
+    if field == "scf_p":
+        kw["coherence"] = 2
+    p, keep = _params(**kw)
+    h = C.c_void_p()
+    assert lib.usgb_create(C.byref(p), C.byref(h)) == status
+    create_msg = lib.usgb_last_error(None).decode()
+    assert msg in create_msg
+    err = C.create_string_buffer(256)
+    fake = C.c_void_p(0x1000)  # never dereferenced: the call fails before any device work
+    rc = lib.usgb_process_frame_noalloc(C.byref(p), fake, fake, 16, 16, fake, fake, None, None, err, 256)
+    assert rc == status
+    assert err.value.decode() == create_msg
+
+
+def test_noalloc_rejects_oversized_grid(lib):
+    p, keep = _params()
+    err = C.create_string_buffer(256)
+    fake = C.c_void_p(0x1000)
+    rc = lib.usgb_process_frame_noalloc(C.byref(p), fake, fake, 65536, 65537, fake, fake, None, None, err, 256)
+    assert rc == 2 and err.value == b"Grid too large."
+    rc = lib.usgb_process_frame_noalloc(C.byref(p), fake, fake, 0, 16, fake, fake, None, None, err, 256)
+    assert rc == 2 and err.value == b"Zero columns in the grid."
+    rc = lib.usgb_process_frame_noalloc(C.byref(p), None, fake, 16, 16, fake, fake, None, None, err, 256)
+    assert rc == 1 and err.value == b"null device pointer"
+
+
 def test_real_path_rejects_pcf(lib):
     p, keep = _params(signal_path=1, coherence=1)
     h = C.c_void_p()

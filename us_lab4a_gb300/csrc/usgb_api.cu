@@ -16,6 +16,7 @@
 #include "../../include/usgb.h"
 #include "usgb_common.cuh"
 #include "usgb_internal.h"
+#include "usgb_params.h"
 #include "usgb_tables.h"
 
 namespace {
@@ -162,68 +163,32 @@ void build_tables(usgb_ctx* c)
 	c->stageTw = true;  // cleared by check_prep_fits when the tables do not fit
 }
 
+// ParamError (the shared checks of usgb_params.h) as this file's Failure.
+template<typename F>
+auto rethrow_param_error(F&& f) -> decltype(f())
+{
+	try {
+		return f();
+	} catch (const usgb::host::ParamError& e) {
+		throw Failure{e.code, e.msg};
+	}
+}
+
 void check_and_derive(usgb_ctx* c, const usgb_sta_params* p)
 {
-	if (!p) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "null parameters");
-	if (p->num_tx == 0 || p->num_rx == 0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of elements is zero.");
-	if (p->num_tx > 1024 || p->num_rx > 1024) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "More than 1024 elements.");
-	if (p->num_samples == 0) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of samples is zero.");
-	if (!p->tx_xy || !p->rx_xy) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Missing element positions.");
-	if (p->signal_path != USGB_PATH_ANALYTIC && p->signal_path != USGB_PATH_REAL) {
-		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid signal path: " << p->signal_path << '.');
-	}
-	c->analytic = p->signal_path == USGB_PATH_ANALYTIC;
-	if (c->analytic) {
-		if (p->upsampling == 0 || p->upsampling > 64) {
-			USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid upsampling factor: " << p->upsampling << ". Must be >= 1 and <= 64.");
-		}
-	} else if (p->upsampling != 4) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "The real-RF path upsamples by 4 (got " << p->upsampling << ").");
-	}
-	if (!(p->sampling_frequency > 0) || !(p->propagation_speed > 0) || !(p->center_frequency > 0)) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Sampling frequency, propagation speed and center frequency must be > 0.");
-	}
-	if (!(p->dead_zone_m >= 0)) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
-	if (p->coherence > USGB_CF_MF) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid coherence factor method: " << p->coherence << '.');
-	if (!c->analytic && p->coherence != USGB_CF_NONE && p->coherence != USGB_CF_SCF) {
-		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The real-RF path supports only the sign coherence factor.");
-	}
-	if (p->coherence == USGB_CF_PCF && !(p->pcf_gamma >= 0 && p->pcf_gamma <= 100)) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid phase_coherence_factor_gamma: " << p->pcf_gamma << '.');
-	}
-	if (p->coherence == USGB_CF_SCF && !(p->scf_p >= 0 && p->scf_p <= 100)) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid sign_coherence_factor_p: " << p->scf_p << '.');
-	}
-	if (p->storage > USGB_STORE_BF16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid storage type: " << p->storage << '.');
-
+	const usgb::host::FrameConsts k = rethrow_param_error([&] { return usgb::host::check_frame_params(p); });
+	c->analytic = k.analytic;
 	c->prm = *p;
 	c->prm.tx_xy = c->prm.rx_xy = c->prm.rx_apod = nullptr;
-	c->U = p->upsampling;
-	c->numSignals = p->num_tx * p->num_rx;
-	const unsigned long long L = static_cast<unsigned long long>(p->num_samples) * c->U;
-	if (L < 2) USGB_FAIL(USGB_ERR_INVALID_VALUE, "The signal length (" << L << ") must be >= 2.");
-	if (c->analytic && L > (1ULL << 20)) {
-		USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of input samples (" << L << ") is greater than " << (1U << 20) << '.');
-	}
-	c->L = static_cast<unsigned>(L);
-	// deadZoneSamplesUp_ (src/user/processor/VectorialSTAProcessor.h:138).
-	const float upFs = c->U * p->sampling_frequency;
-	const double dz = upFs * 2.0 * p->dead_zone_m / p->propagation_speed;
-	if (!(dz < static_cast<double>(std::numeric_limits<unsigned>::max()))) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
-	}
-	c->deadZone = static_cast<unsigned>(dz);
-	if (c->deadZone >= c->L) {
-		USGB_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: deadZoneSamplesUp_ (" << c->deadZone
-				<< ") >= signalLength (" << c->L << ").");
-	}
-	// invCT and signalOffset_ (src/user/processor/VectorialSTAProcessor.h:147,241).
-	c->invCT = upFs / p->propagation_speed;
-	c->signalOffset = upFs * p->peak_offset / p->center_frequency;
-	c->valueCoef = 1.0f / static_cast<float>(c->numSignals);
-	const float sigma0 = static_cast<float>(kPi / std::sqrt(3.0));
-	c->pcfFactor = p->pcf_gamma / sigma0;
-	c->scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
+	c->U = k.U;
+	c->numSignals = k.numSignals;
+	c->L = k.L;
+	c->deadZone = k.deadZone;
+	c->invCT = k.invCT;
+	c->signalOffset = k.signalOffset;
+	c->valueCoef = k.valueCoef;
+	c->pcfFactor = k.pcfFactor;
+	c->scale = k.scale;
 
 	c->txXY.assign(p->tx_xy, p->tx_xy + 2 * p->num_tx);
 	c->rxXY.assign(p->rx_xy, p->rx_xy + 2 * p->num_rx);
@@ -232,8 +197,8 @@ void check_and_derive(usgb_ctx* c, const usgb_sta_params* p)
 	} else {
 		c->apod.assign(p->num_rx, 1.0f);  // the real-RF path has no apodization
 	}
-	c->elemBytes = (c->analytic ? 2 : 1) * (p->storage == USGB_STORE_F32 ? 4 : 2);
-	c->sigStride = (c->L + 7U) & ~7U;
+	c->elemBytes = k.elemBytes;
+	c->sigStride = k.sigStride;
 	c->sigBytes = static_cast<size_t>(c->numSignals) * c->sigStride * c->elemBytes + 256;
 }
 
@@ -322,10 +287,7 @@ void choose_grid_das(usgb_ctx* c);
 
 void ensure_grid(usgb_ctx* c, uint32_t ncols, uint32_t nrows)
 {
-	if (ncols == 0) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Zero columns in the grid.");
-	if (nrows == 0) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Zero rows in the grid.");
-	const size_t npix = static_cast<size_t>(ncols) * nrows;
-	if (npix > (1ULL << 31)) USGB_FAIL(USGB_ERR_INVALID_VALUE, "Grid too large.");
+	const size_t npix = rethrow_param_error([&] { return usgb::host::check_grid_size(ncols, nrows); });
 	if (npix > c->gridCap) {
 		if (c->d_grid) { cudaFree(c->d_grid); c->d_grid = nullptr; }
 		if (c->d_value) { cudaFree(c->d_value); c->d_value = nullptr; }

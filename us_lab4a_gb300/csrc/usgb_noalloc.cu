@@ -15,9 +15,16 @@
 // (64 MiB); every GPU that loads the library holds it until the process exits.
 // All calls share it and it keeps whatever the last call left there, so each
 // call rewrites every part it uses (tables, positions, tensor) and clears the
-// device error word before launching. Calls whose GPU work overlaps (on
+// device status word before launching. Calls whose GPU work overlaps (on
 // different streams, or from different threads) race on the array; the caller
 // must order them.
+//
+// Device-side failures (a bounded wait of the delay-and-sum that gave up, so
+// the image is incomplete) are reported through a status word: the caller's
+// own device word when it passes one (cleared by the call, set by the kernels,
+// read by the caller after the stream completes, so the call stays
+// asynchronous), else the call waits for its work on the stream and returns
+// USGB_ERR_DEVICE_TIMEOUT itself.
 //
 // In host code `g_noallocScratch` only stands in for the array: its device
 // address is obtained with cudaGetSymbolAddress once per device, with that
@@ -35,6 +42,7 @@
 #include "../../include/usgb.h"
 #include "usgb_common.cuh"
 #include "usgb_internal.h"
+#include "usgb_params.h"
 #include "usgb_tables.h"
 
 namespace {
@@ -42,8 +50,6 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;  // 64 MiB
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
-
-using usgb::host::kPi;
 
 std::mutex g_addrMutex;
 std::vector<void*> g_scratchAddr;  // per device ordinal; nullptr until looked up
@@ -90,47 +96,21 @@ struct Layout {
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32_t ncols, uint32_t nrows,
-		float* d_value, float* d_factor, cudaStream_t stream)
+		float* d_value, float* d_factor, uint32_t* d_status, cudaStream_t stream)
 {
-	// ---- parameter checks (same rules and messages as usgb_create) ----
-	if (!p) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "null parameters");
+	// ---- parameter checks: the same function, rules and messages as usgb_create ----
+	usgb::host::FrameConsts k{};
+	size_t npix = 0;
+	try {
+		k = usgb::host::check_frame_params(p);
+		npix = usgb::host::check_grid_size(ncols, nrows);
+	} catch (const usgb::host::ParamError& e) {
+		throw Fail{e.code, e.msg};
+	}
 	if (!d_rf || !d_grid || !d_value || !d_factor) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "null device pointer");
-	if (p->num_tx == 0 || p->num_rx == 0) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of elements is zero.");
-	if (p->num_tx > 1024 || p->num_rx > 1024) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "More than 1024 elements.");
-	if (p->num_samples == 0) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of samples is zero.");
-	if (!p->tx_xy || !p->rx_xy) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Missing element positions.");
-	if (p->signal_path != USGB_PATH_ANALYTIC && p->signal_path != USGB_PATH_REAL) {
-		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid signal path: " << p->signal_path << '.');
-	}
-	const bool analytic = p->signal_path == USGB_PATH_ANALYTIC;
-	if (analytic && (p->upsampling == 0 || p->upsampling > 64)) {
-		NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid upsampling factor: " << p->upsampling << ". Must be >= 1 and <= 64.");
-	}
-	if (!analytic && p->upsampling != 4) NA_FAIL(USGB_ERR_INVALID_VALUE, "The real-RF path upsamples by 4 (got " << p->upsampling << ").");
-	if (!(p->sampling_frequency > 0) || !(p->propagation_speed > 0) || !(p->center_frequency > 0)) {
-		NA_FAIL(USGB_ERR_INVALID_VALUE, "Sampling frequency, propagation speed and center frequency must be > 0.");
-	}
-	if (!(p->dead_zone_m >= 0)) NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: " << p->dead_zone_m << '.');
-	if (p->coherence > USGB_CF_MF) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid coherence factor method: " << p->coherence << '.');
-	if (!analytic && p->coherence != USGB_CF_NONE && p->coherence != USGB_CF_SCF) {
-		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The real-RF path supports only the sign coherence factor.");
-	}
-	if (p->storage > USGB_STORE_BF16) NA_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid storage type: " << p->storage << '.');
-	if (ncols == 0) NA_FAIL(USGB_ERR_INVALID_VALUE, "Zero columns in the grid.");
-	if (nrows == 0) NA_FAIL(USGB_ERR_INVALID_VALUE, "Zero rows in the grid.");
-	const unsigned U = p->upsampling;
-	const unsigned long long L64 = static_cast<unsigned long long>(p->num_samples) * U;
-	if (L64 < 2) NA_FAIL(USGB_ERR_INVALID_VALUE, "The signal length (" << L64 << ") must be >= 2.");
-	if (analytic && L64 > (1ULL << 20)) {
-		NA_FAIL(USGB_ERR_INVALID_PARAMETER, "The number of input samples (" << L64 << ") is greater than " << (1U << 20) << '.');
-	}
-	const unsigned L = static_cast<unsigned>(L64);
-	const float upFs = U * p->sampling_frequency;
-	const double dzd = upFs * 2.0 * p->dead_zone_m / p->propagation_speed;
-	if (!(dzd < static_cast<double>(L))) {
-		NA_FAIL(USGB_ERR_INVALID_VALUE, "Invalid dead zone: deadZoneSamplesUp_ (" << static_cast<unsigned long long>(dzd)
-				<< ") >= signalLength (" << L << ").");
-	}
+	const bool analytic = k.analytic;
+	const unsigned U = k.U;
+	const unsigned L = k.L;
 	const unsigned numSignals = p->num_tx * p->num_rx;
 
 	// ---- host tables (no device memory involved) ----
@@ -146,8 +126,8 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	if (analytic && p->rx_apod) apod.assign(p->rx_apod, p->rx_apod + p->num_rx);
 
 	// ---- scratch layout and size check ----
-	const size_t elemBytes = (analytic ? 2 : 1) * (p->storage == USGB_STORE_F32 ? 4 : 2);
-	const unsigned sigStride = (L + 7U) & ~7U;
+	const size_t elemBytes = k.elemBytes;
+	const unsigned sigStride = k.sigStride;
 	Layout lay{};
 	size_t off = 0;
 	lay.err = off; off = align256(off + sizeof(unsigned));
@@ -168,7 +148,8 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 
 	// ---- device work: everything below writes into the fixed array ----
 	unsigned char* base = static_cast<unsigned char*>(scratch_address());
-	NA_CUDA(cudaMemsetAsync(base + lay.err, 0, sizeof(unsigned), stream));
+	unsigned* status = d_status ? d_status : reinterpret_cast<unsigned*>(base + lay.err);
+	NA_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), stream));
 	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
 	if (analytic) {
 		NA_CUDA(cudaMemcpyAsync(base + lay.tw, fft.tw.data(), fft.tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
@@ -193,8 +174,8 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	pp.tapsStride = poly.tapsStride;
 	usgb::host::set_param_taps(pp, poly.poly);
 	pp.polyTaps = reinterpret_cast<const float*>(base + lay.taps);
-	pp.deadZone = static_cast<unsigned>(dzd);
-	const float scale = (p->storage == USGB_STORE_F32 || p->storage_scale == 0.0f) ? 1.0f : p->storage_scale;
+	pp.deadZone = k.deadZone;
+	const float scale = k.scale;
 	pp.outScale = scale;
 	pp.tw = reinterpret_cast<const float2*>(base + lay.tw);
 	pp.hilb = reinterpret_cast<const float4*>(base + lay.hilb);
@@ -219,21 +200,21 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	dp.rxXY = reinterpret_cast<const float*>(base + lay.rx);
 	dp.apod = reinterpret_cast<const float*>(base + lay.apod);
 	dp.grid = d_grid;
-	dp.npix = ncols * nrows;
+	dp.npix = static_cast<unsigned>(npix);  // <= 2^31 (check_grid_size)
 	dp.ncols = ncols;
 	dp.nrows = nrows;
-	dp.invCT = upFs / p->propagation_speed;
-	dp.signalOffset = upFs * p->peak_offset / p->center_frequency;
-	dp.valueCoef = 1.0f / static_cast<float>(numSignals);
+	dp.invCT = k.invCT;
+	dp.signalOffset = k.signalOffset;
+	dp.valueCoef = k.valueCoef;
 	dp.invScale = 1.0f / scale;
-	dp.pcfFactor = p->pcf_gamma / static_cast<float>(kPi / std::sqrt(3.0));
+	dp.pcfFactor = k.pcfFactor;
 	dp.scfP = p->scf_p;
 	dp.delayMode = USGB_DELAY_AUTO;
 	dp.invCTd = static_cast<double>(p->sampling_frequency) * U / p->propagation_speed;
 	dp.signalOffsetd = static_cast<double>(p->sampling_frequency) * U * p->peak_offset / p->center_frequency;
 	dp.value = d_value;
 	dp.factor = d_factor;
-	dp.errWord = reinterpret_cast<unsigned*>(base + lay.err);
+	dp.errWord = status;
 	dp.tileCols = 32;
 	dp.tileRows = 8;
 	dp.stageBytes = 16384;
@@ -246,19 +227,31 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	}
 	NA_CUDA(usgb::launch_das(dp, static_cast<int>(p->storage), static_cast<int>(p->coherence), analytic,
 			staged ? 1 : 0, stream));
+	if (!d_status) {
+		// No caller word: wait for this frame and read the array's word (a
+		// device-to-host copy into a local, then the stream's completion).
+		unsigned word = 0;
+		NA_CUDA(cudaMemcpyAsync(&word, status, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+		NA_CUDA(cudaStreamSynchronize(stream));
+		if (word & usgb::DEVERR_WAIT_TIMEOUT) {
+			NA_FAIL(USGB_ERR_DEVICE_TIMEOUT, "A delay-and-sum wait gave up on the device; the image is incomplete.");
+		}
+		if (word) NA_FAIL(USGB_ERR_INVALID_STATE, "Device-side error " << word << " in the delay-and-sum.");
+	}
 	return USGB_OK;
 }
 
 }  // namespace
 
 extern "C" int usgb_process_frame_noalloc(const usgb_sta_params* params, const float* d_rf, const float* d_grid_xyz,
-		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, void* cuda_stream,
+		uint32_t ncols, uint32_t nrows, float* d_value, float* d_factor, uint32_t* d_status, void* cuda_stream,
 		char* error_message, size_t error_capacity)
 {
 	std::string msg;
 	int rc = USGB_OK;
 	try {
-		rc = run(params, d_rf, d_grid_xyz, ncols, nrows, d_value, d_factor, static_cast<cudaStream_t>(cuda_stream));
+		rc = run(params, d_rf, d_grid_xyz, ncols, nrows, d_value, d_factor, d_status,
+				static_cast<cudaStream_t>(cuda_stream));
 	} catch (const Fail& f) {
 		msg = f.msg;
 		rc = f.code;

@@ -141,7 +141,7 @@ SIGNATURES = {
     "usgb_batch_run": (C.c_int, [C.c_void_p, C.POINTER(BatchItem), C.c_uint32, C.c_void_p, C.c_int]),
     "usgb_batch_synchronize": (C.c_int, [C.c_void_p]),
     "usgb_process_frame_noalloc": (C.c_int, [C.POINTER(StaParams), C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
-                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
+                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 
 _lib = None
