@@ -203,6 +203,17 @@ int usgb_autotune_das(usgb_ctx* ctx, const void* d_signals, float* d_value, floa
  * wait that gave up) as USGB_ERR_DEVICE_TIMEOUT. */
 int usgb_synchronize(usgb_ctx* ctx);
 
+/* Test hook of the timeout path (no counterpart in the reference). Every
+ * wait of the staged delay-and-sum kernels (variants 1-3) is bounded: after
+ * its limit the waiting warp records DEVERR_WAIT_TIMEOUT in the context's
+ * error word, the kernel winds down once its copies in flight have landed,
+ * and usgb_process / usgb_process_rf / usgb_synchronize return
+ * USGB_ERR_DEVICE_TIMEOUT; the context stays usable. wait_limit_us sets the
+ * limit (0: the default 2 s); skip_stage = k > 0 makes the window producer of
+ * every pixel tile leave its k-th stage unarmed, so the consumers' wait for it
+ * runs out. skip_stage = 0 and wait_limit_us = 0 restore normal operation. */
+int usgb_set_wait_test(usgb_ctx* ctx, uint32_t wait_limit_us, uint32_t skip_stage);
+
 /*
  * Image post-processing (the reference's dB image: envelope along each image
  * column, ParallelHilbertEnvelope<float>::calculateDim2Value,

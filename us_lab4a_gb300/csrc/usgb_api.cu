@@ -93,6 +93,8 @@ struct usgb_ctx {
 	unsigned tileRows = 8;
 	unsigned stageBytes = 16384;
 	unsigned stages = 4;
+	unsigned long long waitLimitNs = 0;   // usgb_set_wait_test: 0 = the kernels' 2 s
+	unsigned testSkipStage = 0;           // usgb_set_wait_test: 0 = none
 	std::string err;
 
 	~usgb_ctx()
@@ -280,6 +282,8 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.tileRows = c->tileRows;
 	dp.stageBytes = c->stageBytes;
 	dp.stages = c->stages;
+	dp.waitLimitNs = c->waitLimitNs;
+	dp.testSkipStage = c->testSkipStage;
 	return dp;
 }
 
@@ -584,6 +588,14 @@ int usgb_process_rf(usgb_ctx* c, const float* rf, float* value, float* factor)
 		unsigned errWord = 0;
 		USGB_CUDA(cudaMemcpy(&errWord, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
 		if (errWord) USGB_FAIL(USGB_ERR_DEVICE_TIMEOUT, "device-side wait gave up (code " << errWord << ")");
+	});
+}
+
+int usgb_set_wait_test(usgb_ctx* c, uint32_t wait_limit_us, uint32_t skip_stage)
+{
+	return guarded(c, [&] {
+		c->waitLimitNs = static_cast<unsigned long long>(wait_limit_us) * 1000ull;
+		c->testSkipStage = skip_stage;
 	});
 }
 

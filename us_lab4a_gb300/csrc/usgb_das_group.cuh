@@ -170,7 +170,7 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 		while (t0 < p.numTx) {
 			if (it >= nst) {
 				bool w = true;
-				if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], phase ^ 1u, kWaitLimitNs);
+				if (lane == 0) w = mbar_wait_bounded(&sm.empty[s], phase ^ 1u, wait_limit(p));
 				w = __shfl_sync(0xffffffffu, w, 0);
 				if (!w) {
 					if (lane == 0) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
@@ -229,9 +229,11 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 			}
 			__threadfence_block();
 			__syncwarp();
-			if (lane == 0) mbar_arrive_expect_tx(&sm.full[s], total);
+			// The test hook leaves this stage unarmed: its consumers' wait runs out.
+			const bool skip = p.testSkipStage != 0u && it - itStart + 1 == static_cast<int>(p.testSkipStage);
+			if (lane == 0 && !skip) mbar_arrive_expect_tx(&sm.full[s], total);
 			__syncwarp();
-			if (u < n && wb > 0) {
+			if (u < n && wb > 0 && !skip) {
 				const T* src = sig + t * txStride + static_cast<size_t>(r) * p.sigStride + lo;
 				bulk_copy_g2s(sm.stageBuf + static_cast<size_t>(s) * capBytes + excl, src, wb, &sm.full[s]);
 			}
@@ -243,17 +245,19 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 			}
 		}
 	}
+	// Let this tile's last copies land before the block moves on or exits:
+	// every stage still in the ring is waited for, also after one of them
+	// gave up (a stage that was never armed), so no copy is left in flight.
 	if (lane == 0) {
 		const int from = (it - nst > itStart) ? it - nst : itStart;
 		for (int q = from; q < it; ++q) {
-			if (!mbar_wait_bounded(&sm.full[q % nst], (q / nst) & 1, kWaitLimitNs)) {
+			if (!mbar_wait_bounded(&sm.full[q % nst], (q / nst) & 1, wait_limit(p))) {
 				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
 				ok = false;
-				break;
 			}
 		}
 	}
-	return ok;
+	return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
 }
 
 // ------------------------------------------------------------- consumers
@@ -346,7 +350,7 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 		}
 		bool last = false;
 		while (!last) {
-			if (!mbar_wait_bounded(&sm.full[s], phase, kWaitLimitNs)) {
+			if (!mbar_wait_bounded(&sm.full[s], phase, wait_limit(p))) {
 				atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
 				return false;
 			}

@@ -16,6 +16,12 @@ constexpr int kGlobalWindow = -1;   // window too large for a stage: gather from
 constexpr int kEmptyWindow = -2;    // no valid sample can be reached
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 
+// The launch's wait limit (DasParams::waitLimitNs, 0 = kWaitLimitNs).
+__device__ __forceinline__ uint64_t wait_limit(const DasParams& p)
+{
+	return p.waitLimitNs ? p.waitLimitNs : kWaitLimitNs;
+}
+
 template<bool ANALYTIC, int S> struct Sample;
 template<int S> struct Sample<true, S> {
 	using T = typename Complex<S>::T;

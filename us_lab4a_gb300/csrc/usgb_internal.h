@@ -94,6 +94,13 @@ struct DasParams {
 	float* value;
 	float* factor;
 	unsigned* errWord;
+	// Bounded waits of the staged kernels give up after waitLimitNs
+	// nanoseconds (0: the default of 2 s). testSkipStage = k > 0 makes the
+	// window producer of every pixel tile leave its k-th stage unarmed, so
+	// that the consumers' wait for it runs out (the timeout path's test
+	// hook; 0 in normal use).
+	unsigned long long waitLimitNs;
+	unsigned testSkipStage;
 	// Staged kernels: columns (32; 64 for the receiver-group kernel's wide
 	// tiles) and rows of the pixel tile, bytes per pipeline stage, number of
 	// stages (2..16).

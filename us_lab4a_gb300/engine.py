@@ -212,3 +212,9 @@ class StaEngine:
 
     def synchronize(self) -> None:
         self._check(self._lib.usgb_synchronize(self._h))
+
+    def set_wait_test(self, wait_limit_us: int = 0, skip_stage: int = 0) -> None:
+        """Test hook of the timeout path (usgb_set_wait_test): the staged
+        delay-and-sum's bounded waits give up after wait_limit_us (0: 2 s), and
+        skip_stage = k > 0 leaves every tile's k-th stage unarmed."""
+        self._check(self._lib.usgb_set_wait_test(self._h, int(wait_limit_us), int(skip_stage)))

@@ -133,6 +133,7 @@ SIGNATURES = {
     "usgb_autotune_das": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                     C.POINTER(C.c_float)]),
     "usgb_synchronize": (C.c_int, [C.c_void_p]),
+    "usgb_set_wait_test": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "usgb_version": (C.c_char_p, []),
     "usgb_batch_create": (C.c_int, [C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
     "usgb_batch_destroy": (None, [C.c_void_p]),
