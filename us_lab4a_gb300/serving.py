@@ -73,10 +73,13 @@ class _InFlight:
 class ServingLoop:
     def __init__(self, hbm_budget_bytes: int, max_batch: int = 48, max_elements: int = 128,
                  use_graph: bool = True, device="cuda:0", das_config: Optional[Tuple[int, int, int]] = None,
-                 plain: bool = False):
+                 plain: bool = False, per_frame: bool = False):
         """plain=True serves the plain form instead: every admitted frame is
         processed on its own (one preparation launch and one plain
-        delay-and-sum launch per frame), for comparison with the batched form."""
+        delay-and-sum launch per frame); per_frame=True also processes every
+        admitted frame on its own, but with the context's default (staged,
+        autoselected) delay-and-sum kernel. Both are for comparison with the
+        batched form."""
         import torch
         self.torch = torch
         self.device = torch.device(device)
@@ -84,6 +87,7 @@ class ServingLoop:
         self.max_batch = max_batch
         self.use_graph = use_graph
         self.plain = plain
+        self.per_frame = plain or per_frame
         self.batches = [Batch(max_batch, max_elements), Batch(max_batch, max_elements)]
         if das_config:
             for b in self.batches:
@@ -193,7 +197,7 @@ class ServingLoop:
                     with torch.cuda.stream(stream):
                         for req, slot in work:
                             slot.rf.copy_(req.rf, non_blocking=True)
-                        if self.plain:
+                        if self.per_frame:
                             for _, slot in work:
                                 slot.engine.set_stream(stream)
                                 slot.engine.process_device(slot.rf, slot.value, slot.factor)
