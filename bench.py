@@ -122,72 +122,100 @@ def _dist():
     return world, rank, local
 
 
-def cpu_baseline(frame, threads: int, a_sample: int = 128, p_sample: int = 8192, dtype=np.float32):
-    """Oracle (the C++ restatement of the reference processor) on a bounded
-    sample of the frame: preparation of `a_sample` A-scans and delay-and-sum
-    of `p_sample` grid points, scaled to one frame."""
+def _oracle_spec(spec, threads):
     import oracle
+    return oracle.OracleSpec(tx_xy=spec.tx_xy, rx_xy=spec.rx_xy, num_samples=spec.num_samples,
+                             upsampling=4 if spec.real_path else spec.upsampling,
+                             sampling_frequency=spec.sampling_frequency, propagation_speed=spec.propagation_speed,
+                             center_frequency=spec.center_frequency, peak_offset=spec.peak_offset,
+                             dead_zone_m=spec.dead_zone_m, rx_apod=spec.rx_apod,
+                             cf={"none": 0, "pcf": 1, "scf": 2, "mf": 3}[spec.coherence], pcf_gamma=spec.pcf_gamma,
+                             scf_p=spec.scf_p, real_path=spec.real_path, nthreads=threads)
+
+
+def cpu_rf(frame) -> np.ndarray:
+    """Host RF of the frame's shape for the CPU timings: the frame's point
+    scatterers and noise, without its speckle background (synthesising 20 000
+    speckle echoes on the host takes minutes; the oracle's cost does not
+    depend on the sample values)."""
     from us_lab4a_gb300 import synth
     spec = frame.spec
-    rng = np.random.default_rng(7)
-    # Preparation: a_sample A-scans of one transmit event, synthesized here.
-    tx = int(rng.integers(spec.num_tx))
-    rx_idx = np.sort(rng.choice(spec.num_rx, min(a_sample, spec.num_rx), replace=False))
-    reps = max(1, a_sample // len(rx_idx))
-    rf_rows = synth.synth_rf_numpy(spec.tx_xy[tx:tx + 1], spec.rx_xy[rx_idx], frame.scatterers,
-                                   spec.sampling_frequency, spec.propagation_speed, spec.center_frequency,
-                                   spec.num_samples, np.random.default_rng(frame.seed + 1))
-    cf = {"none": 0, "pcf": 1, "scf": 2, "mf": 3}[spec.coherence]
-    sub = oracle.OracleSpec(tx_xy=spec.tx_xy[tx:tx + 1], rx_xy=spec.rx_xy[rx_idx], num_samples=spec.num_samples,
-                            upsampling=spec.upsampling, sampling_frequency=spec.sampling_frequency,
-                            propagation_speed=spec.propagation_speed, center_frequency=spec.center_frequency,
-                            rx_apod=spec.rx_apod[rx_idx], cf=0, nthreads=threads)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        oracle.process(sub, rf_rows, None, dtype=dtype, want_signals=False)
-    t_prep = (time.perf_counter() - t0) / (reps * len(rx_idx))
-    # Delay-and-sum: p_sample grid points on a tensor of the frame's shape
-    # (its cost does not depend on the sample values).
-    L = spec.num_samples * spec.upsampling
-    full = oracle.OracleSpec(tx_xy=spec.tx_xy, rx_xy=spec.rx_xy, num_samples=spec.num_samples,
-                             upsampling=spec.upsampling, sampling_frequency=spec.sampling_frequency,
-                             propagation_speed=spec.propagation_speed, center_frequency=spec.center_frequency,
-                             rx_apod=spec.rx_apod, cf=cf, nthreads=threads)
-    tensor = np.zeros((spec.num_tx, spec.num_rx, L), np.complex64)
-    idx = rng.choice(frame.npix, min(p_sample, frame.npix), replace=False)
-    pts = frame.grid_xyz.reshape(-1, 3)[idx][:, None, :]
-    t0 = time.perf_counter()
-    oracle.das(full, tensor, pts, dtype=dtype)
-    t_das = (time.perf_counter() - t0) / len(idx)
-    n_sig = spec.num_tx * spec.num_rx
-    sec_per_frame = t_prep * n_sig + t_das * frame.npix
-    return {"value": 1.0 / sec_per_frame, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"prep of {reps * len(rx_idx)} A-scans + delay-and-sum of {len(idx)} grid points "
-                      f"(FP32 oracle, {threads} threads), scaled to {n_sig} A-scans and {frame.npix} points",
-            "sec_per_frame": sec_per_frame}
+    pts = frame.scatterers
+    n = min(len(pts), 64)
+    sub = synth.Scatterers(pts.x[:n], pts.y[:n], pts.z[:n], pts.amp[:n])
+    return synth.synth_rf_numpy(spec.tx_xy, spec.rx_xy, sub, spec.sampling_frequency, spec.propagation_speed,
+                                spec.center_frequency, spec.num_samples, np.random.default_rng(frame.seed + 1))
+
+
+def time_oracle_frames(frame, rf: np.ndarray, threads: int, warmup: int, steps: int):
+    """Whole frames through the FP32 oracle (the C++ restatement of the
+    reference processor: preparation of every A-scan, delay-and-sum of every
+    grid point, coherence factor), `warmup` untimed then `steps` timed runs,
+    as the reference's ExecutionTimeMeasurement does (src/util/ExecutionTimeMeasurement.h:25,75-86).
+    Returns the per-frame seconds of the timed runs."""
+    import oracle
+    spec = _oracle_spec(frame.spec, threads)
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        oracle.process(spec, rf, frame.grid_xyz, dtype=np.float32)
+        if i >= warmup:
+            times.append(time.perf_counter() - t0)
+    return times
+
+
+def _stats(times):
+    return {"mean_s": statistics.mean(times), "p50_s": float(np.percentile(times, 50)),
+            "p99_s": float(np.percentile(times, 99)), "runs": len(times)}
+
+
+def cpu_baseline(frame, threads: int, rf: np.ndarray, warmup: int = 1, steps: int = 2):
+    """CPU baseline leg: whole frames through the FP32 oracle on the host cores."""
+    times = time_oracle_frames(frame, rf, threads, warmup, steps)
+    st = _stats(times)
+    return {"value": 1.0 / st["mean_s"], "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} whole frames ({frame.spec.num_tx * frame.spec.num_rx} A-scans, {frame.npix} grid "
+                      f"points each) after {warmup} warm-up, FP32 oracle on {threads} threads",
+            **st}
 
 
 def run_reference(args):
+    """The reference arm: whole frames of the workload through the CPU oracle
+    (the reference's CPU processor restated; the reference itself is a C++
+    CMake/Qt project that does not install here), every host thread."""
     world, rank, _ = _dist()
     if rank != 0:
         return
     frame, desc = _workload(args.workload, "f32")
     threads = os.cpu_count() or 1
-    times = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(frame, threads, a_sample=64, p_sample=4096)
-        if i >= args.warmup:
-            times.append(r["sec_per_frame"])
-    value = 1.0 / statistics.mean(times)
+    rf = cpu_rf(frame)
+    times = time_oracle_frames(frame, rf, threads, args.warmup, args.steps)
+    st = _stats(times)
+    value = 1.0 / st["mean_s"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * st["mean_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded point + speckle scatterers)",
-            "config": {"workload": desc, "sample": "per step: bounded sample scaled to one frame"},
+            "config": _config(frame, desc, "f32"),
+            "latency_ms": {"p50": 1e3 * st["p50_s"], "p99": 1e3 * st["p99_s"]},
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
-                             "sample": r["sample"]},
+                             "sample": f"each step one whole frame ({frame.spec.num_tx * frame.spec.num_rx} A-scans, "
+                                       f"{frame.npix} grid points) through the FP32 oracle on {threads} threads; RF of "
+                                       "the frame's point scatterers and noise (speckle left out of the host input: "
+                                       "the cost does not depend on sample values)"},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _config(frame, desc: str, storage: str) -> dict:
+    """The workload identification both arms print (implementation details go elsewhere)."""
+    spec = frame.spec
+    n_sig = spec.num_tx * spec.num_rx
+    rf_mb = n_sig * spec.num_samples * 4 / 1e6
+    tensor_gb = n_sig * spec.num_samples * spec.upsampling * {"f32": 8, "f16": 4, "bf16": 4}[storage] / 1e9
+    return {"workload": desc, "storage": storage,
+            "l2": f"inputs larger than L2 (129 MB) / the host's last-level cache: {rf_mb:.0f} MB RF in and a "
+                  f"{tensor_gb:.2f} GB analytic tensor written and read per frame; GPU arm: 4 RF buffers rotate"}
 
 
 def run_gpu(args):
@@ -329,6 +357,25 @@ def run_gpu(args):
             traffic = tr
     gathers = frame.npix * n_sig
 
+    # On-chip roofline of the delay-and-sum (it is not HBM-bound): bytes
+    # through the shared-memory pipe (window copies written + two taps read
+    # per gather) against 152 SMs x 128 B/clk at the sampled SM clock, and
+    # its algorithmic FP32 work (12 FLOP per gather) against the FP32 peak
+    # (152 SMs x 128 lanes x 2 FLOP/clk).
+    onchip = None
+    if das_cfg["variant"] != 0:
+        staged = staged_bytes_model(frame, 64 if das_cfg["variant"] == 3 else 32, das_cfg["tile_rows"], esize)
+        tap_bytes = 2.0 * esize * gathers
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        smem_peak = 152 * 128 * mhz * 1e6 / 1e9
+        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+        smem_gbs = (staged + tap_bytes) / (das_ms * 1e-3) / 1e9
+        tflops = 12.0 * gathers / (das_ms * 1e-3) / 1e12
+        onchip = {"smem_bytes_per_launch": staged + tap_bytes, "staged_bytes_modelled": staged,
+                  "tap_bytes": tap_bytes, "smem_achieved_gbs": smem_gbs, "smem_peak_gbs": smem_peak,
+                  "smem_frac": smem_gbs / smem_peak, "fp32_tflops": tflops, "fp32_peak_tflops": fp32_peak,
+                  "fp32_frac": tflops / fp32_peak, "clock_mhz": mhz}
+
     # End to end through the host entry points (host RF in, host image out).
     e2e = None
     if not args.no_e2e:
@@ -386,9 +433,9 @@ def run_gpu(args):
             e2e["value"] = world * args.steps / float(t.item())
 
     cpu = None
+    rf_host_full = rf0.cpu().numpy()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(frame, os.cpu_count() or 1)
-        cpu.pop("sec_per_frame", None)
+        cpu = cpu_baseline(frame, os.cpu_count() or 1, rf_host_full)
 
     mixed = None
     if world == 1 and not args.no_mixed:
@@ -414,14 +461,15 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": spec.storage if spec.storage != "f32" else "f32",
             "data": "synthetic (seeded point + speckle scatterers)",
-            "config": {"workload": desc, "storage": spec.storage, "das_kernel": ("plain" if das_cfg["variant"] == 0 else
-                           ("staged" if das_cfg["variant"] == 1 else "receiver-group")
-                           + f" (tile {64 if das_cfg['variant'] == 3 else 32}x{das_cfg['tile_rows']}, "
-                           + f"{das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
-                           + (", autotuned)" if args.autotune else ")")),
-                       "l2": "inputs larger than L2: 4 rotating 67 MB RF buffers and a 1.07 GB analytic tensor per step",
-                       "frames_in_flight": f"{args.pipeline} contexts on {args.pipeline} streams take the frames in turn",
-                       "parallelism": f"replicas x{world}"},
+            "config": _config(frame, desc, spec.storage),
+            "implementation": {"das_kernel": ("plain" if das_cfg["variant"] == 0 else
+                               ("staged" if das_cfg["variant"] == 1 else "receiver-group")
+                               + f" (tile {64 if das_cfg['variant'] == 3 else 32}x{das_cfg['tile_rows']}, "
+                               + f"{das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
+                               + (", autotuned)" if args.autotune else ")")),
+                               "frames_in_flight": f"{args.pipeline} contexts on {args.pipeline} streams take the "
+                                                   "frames in turn",
+                               "parallelism": f"replicas x{world}"},
             "voxels_per_s": fps * frame.npix,
             "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
             "kernels_ms": {"prep": prep_ms, "das": das_ms},
@@ -429,39 +477,147 @@ def run_gpu(args):
                          "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                          "algorithmic_bytes": top[2]},
             "das_gathers_per_s": gathers / (das_ms * 1e-3),
+            "das_onchip": onchip,
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
             "mixed": mixed, "single": single, "two_medium": two_medium,
         }
+        line["north_star"] = _north_star(line)   # last key: the summary the record's tail keeps
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
+def staged_bytes_model(frame, tile_cols: int, tile_rows: int, esize: int) -> float:
+    """Bytes the staged delay-and-sum copies from L2 into shared memory per
+    frame: for every pixel tile and (tx, rx) pair, the sample window
+    [floor(min tx + min rx), floor(max tx + max rx) + 1] of the tile's
+    delays, clipped to the A-scan, its start aligned down to 16 bytes and its
+    length rounded up to 16 bytes (the producer's rule). Delays in FP32 as the
+    kernel computes them."""
+    spec = frame.spec
+    L = spec.num_samples * spec.upsampling
+    inv = np.float32(spec.sampling_frequency * spec.upsampling / spec.propagation_speed)
+    off = np.float32(spec.sampling_frequency * spec.upsampling * spec.peak_offset / spec.center_frequency)
+    g = frame.grid_xyz
+    ncols, nrows = g.shape[0], g.shape[1]
+    tx = np.asarray(spec.tx_xy, np.float32)
+    rx = np.asarray(spec.rx_xy, np.float32)
+    align = 16 // esize
+    total = 0.0
+    for c0 in range(0, ncols, tile_cols):
+        for r0 in range(0, nrows, tile_rows):
+            pts = g[c0:c0 + tile_cols, r0:r0 + tile_rows].reshape(-1, 3)
+
+            def delays(el):
+                d = np.sqrt((pts[None, :, 0] - el[:, None, 0]) ** 2 + (pts[None, :, 1] - el[:, None, 1]) ** 2
+                            + pts[None, :, 2] ** 2).astype(np.float32) * inv
+                return d.min(1), d.max(1)
+            tmin, tmax = delays(tx)
+            rmin, rmax = delays(rx)
+            tmin, tmax = tmin + off, tmax + off
+            lo = np.maximum(np.floor(tmin[:, None] + rmin[None, :]), 0)
+            hi = np.minimum(np.floor(tmax[:, None] + rmax[None, :]) + 1, L - 1)
+            ok = (lo <= L - 2) & (hi >= 1) & (hi >= lo)
+            lo = (lo.astype(np.int64) // align) * align
+            nbytes = ((hi.astype(np.int64) - lo + 1) * esize + 15) // 16 * 16
+            total += float(nbytes[ok].sum())
+    return total
+
+
+def _north_star(line: dict) -> dict:
+    """Compact summary of the headline and the mixed-precision / batching /
+    serving comparison (target: the FP16 batched serving form at >= 3x the
+    frames/s of the plain FP32 GPU form at <= -60 dB against the FP64 oracle)."""
+    out = {"cf2d_f32_frames_per_s": line["value"],
+           "cf2d_e2e_frames_per_s": (line.get("e2e") or {}).get("value"),
+           "kernels_ms": line["kernels_ms"],
+           "das_hbm_frac": line["roofline"]["frac"] if line["roofline"]["kernel"] == "das" else None,
+           "das_smem_pipe_frac": (line.get("das_onchip") or {}).get("smem_frac")}
+    m = line.get("mixed")
+    if m:
+        out["mixed_48"] = {
+            "plain_f32_direct_kernel_fps": m["plain_f32"]["frames_per_s"],
+            "default_f32_per_frame_fps": m["default_f32"]["frames_per_s"],
+            "batched_f32_fps": m["batched_f32"]["frames_per_s"],
+            "batched_f16_fps": m["batched_f16"]["frames_per_s"],
+            "batched_f16_vs_plain_f32": m["speedup_vs_plain_f32"]["batched_f16"],
+            "batched_f16_vs_default_f32": m["speedup_vs_default_f32"]["batched_f16"],
+            "worst_err_db_f16": m["batched_f16"]["err_db"]}
+        sv = m.get("serving")
+        if sv:
+            sat = {k: sv[k]["rates"][-1] for k in ("batched_f16", "plain_f32", "default_f32")}
+            out["serving_2000_per_s"] = {
+                k: {"fps": v["frames_per_s"], "p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"]} for k, v in sat.items()}
+            out["serving_f16_vs_plain_f32"] = sv["speedup_at_saturation"]
+            out["serving_f16_vs_default_f32"] = sv["speedup_at_saturation_vs_default_f32"]
+            out["serving_worst_err_db_f16"] = sat["batched_f16"].get("err_db")
+    return out
+
+
 def _db(err: float, peak: float) -> float:
     return float(20.0 * np.log10(max(err, 1e-30) / max(peak, 1e-30)))
 
 
-def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
+def _sample_idx(img: np.ndarray, n_top: int, n_rand: int, seed: int) -> np.ndarray:
+    """Flat indices of the n_top brightest points of an image and n_rand random ones."""
+    flat = np.abs(img).reshape(-1)
+    n_top = min(n_top, flat.size)
+    top = np.argpartition(flat, -n_top)[-n_top:]
+    rest = np.random.default_rng(seed).choice(flat.size, min(n_rand, flat.size), replace=False)
+    return np.unique(np.concatenate([top, rest]))
+
+
+def _fp64_refs(frames, rfs_host, images, threads, n_top=64, n_rand=192):
+    """FP64 oracle values at sampled points of every frame: the brightest
+    points of a GPU image of the frame and random ones (the oracle prepares
+    every A-scan of the frame). Returns {i: (flat indices, values)}."""
+    import oracle
+    refs = {}
+    for i, fr in enumerate(frames):
+        idx = _sample_idx(images[i], n_top, n_rand, seed=100 + i)
+        pts = fr.grid_xyz.reshape(-1, 3)[idx][:, None, :]
+        v, _, _ = oracle.process(_oracle_spec(fr.spec, threads), rfs_host[i].astype(np.float64), pts,
+                                 dtype=np.float64)
+        refs[i] = (idx, v[:, 0])
+    return refs
+
+
+def _worst_db(refs, images) -> float:
+    """Worst peak-relative error (dB) over every frame, at the sampled points."""
+    worst = -1e9
+    for i, (idx, ref) in refs.items():
+        v = np.asarray(images[i], np.float64).reshape(-1)[idx]
+        worst = max(worst, _db(float(np.abs(v - ref).max()), float(np.abs(ref).max())))
+    return worst
+
+
+def run_mixed(dev, num_frames: int = 48, reps: int = 2):
     """The mixed-size workload: `num_frames` frames (elements {32, 64, 96,
     128}, samples {1024, 2048, 4096} at 40 MHz, grids {128x128, 256x256,
     512x1024}, PCF on or off, 4x upsampling), every frame's RF resident.
 
-    plain_f32   frames/s of the plain FP32 form: one frame at a time, the
-                direct delay-and-sum kernel;
-    batched_*   frames/s of all frames in one persistent preparation launch +
-                one persistent staged delay-and-sum launch, replayed from a
-                CUDA graph, tile shape autotuned on the batch;
-    serving     run_serving(): the serving configuration (these frames plus
-                large ones as Poisson streams) through the continuous-batching
-                loop, FP16 batched against plain FP32;
-    err_db      peak-relative error of each form's image against the FP64
-                oracle on the `oracle_frames` smallest frames (worst case)."""
+    plain_f32    frames/s of the plain FP32 form: one frame at a time, the
+                 direct delay-and-sum kernel (one thread per grid point, both
+                 taps gathered from global memory);
+    default_f32  one frame at a time with the library's default FP32 kernels
+                 (staged receiver-group delay-and-sum, tile shape chosen per
+                 grid);
+    batched_*    frames/s of all frames in one persistent preparation launch +
+                 one persistent staged delay-and-sum launch, replayed from a
+                 CUDA graph, tile shape autotuned on the batch;
+    serving      run_serving(): the serving configuration (these frames plus
+                 large ones as Poisson streams) through the continuous-batching
+                 loop;
+    err_db       worst peak-relative error over every frame against the FP64
+                 oracle, at the 64 brightest and 192 random grid points of
+                 each frame."""
     import torch
     from dataclasses import replace
-    import oracle
     from us_lab4a_gb300 import StaEngine, workloads
-    from us_lab4a_gb300.batch import Batch, BatchItem
+    from us_lab4a_gb300.batch import Batch
+    from us_lab4a_gb300.batch import BatchItem
+    threads = os.cpu_count() or 1
     s = torch.cuda.Stream(device=dev)
     frames = workloads.mixed(num_frames, storage="f16")
     with torch.cuda.stream(s):
@@ -494,33 +650,29 @@ def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    small = sorted(range(num_frames), key=lambda i: frames[i].npix * frames[i].spec.num_tx ** 2)[:oracle_frames]
-    refs = {}
-    for i in small:
-        fr = frames[i]
-        sp = fr.spec
-        ospec = oracle.OracleSpec(tx_xy=sp.tx_xy, rx_xy=sp.rx_xy, num_samples=sp.num_samples,
-                                  upsampling=sp.upsampling, sampling_frequency=sp.sampling_frequency,
-                                  propagation_speed=sp.propagation_speed, center_frequency=sp.center_frequency,
-                                  rx_apod=sp.rx_apod, cf={"none": 0, "pcf": 1, "scf": 2, "mf": 3}[sp.coherence])
-        refs[i] = oracle.process(ospec, rfs[i].cpu().numpy().astype(np.float64), fr.grid_xyz, dtype=np.float64)[0]
-
-    def err_db(items):
-        worst = -1e9
-        for i in small:
-            v = items[i].value.cpu().numpy().astype(np.float64)
-            worst = max(worst, _db(float(np.abs(v - refs[i]).max()), float(np.abs(refs[i]).max())))
-        return worst
+    def images(items):
+        return [it.value.cpu().numpy() for it in items]
 
     out = {"workload": f"{num_frames} mixed-size frames (elements 32-128, 1024-4096 samples @40 MHz, 4x, "
                        f"grids 128x128 / 256x256 / 512x1024, PCF on/off), RF resident",
            "gathers": gathers}
+    per_frame = lambda items: [it.engine.process_device(it.rf, it.value, it.factor) for it in items]
     plain = items_for("f32", plain=True)
-    ms = timed(lambda: [it.engine.process_device(it.rf, it.value, it.factor) for it in plain])
-    out["plain_f32"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms, "err_db": err_db(plain)}
+    ms = timed(lambda: per_frame(plain))
+    plain_img = images(plain)
     for it in plain:
         it.engine.close()
     del plain
+    refs = _fp64_refs(frames, [rf.cpu().numpy() for rf in rfs], plain_img, threads)
+    out["plain_f32"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms,
+                        "err_db": _worst_db(refs, plain_img)}
+    default = items_for("f32", plain=False)
+    ms = timed(lambda: per_frame(default))
+    out["default_f32"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms,
+                          "err_db": _worst_db(refs, images(default))}
+    for it in default:
+        it.engine.close()
+    del default
     best_f16 = None
     for storage in ("f32", "f16"):
         items = items_for(storage, plain=False)
@@ -528,41 +680,66 @@ def run_mixed(dev, num_frames: int = 48, reps: int = 2, oracle_frames: int = 3):
             cfg, _ = b.autotune(items, s)
             ms = timed(lambda: b.run(items, s, use_graph=True))
             out[f"batched_{storage}"] = {"frames_per_s": num_frames * 1e3 / ms, "ms_per_pass": ms,
-                                         "das_config": list(cfg), "err_db": err_db(items)}
+                                         "das_config": list(cfg), "err_db": _worst_db(refs, images(items))}
         for it in items:
             it.engine.close()
         if storage == "f16":
             best_f16 = cfg
     torch.cuda.synchronize(dev)
-    out["serving"] = run_serving(dev, frames, rfs, refs, small, best_f16)
-    base = out["plain_f32"]["frames_per_s"]
+    out["err_db_frames"] = f"all {num_frames} frames, 64 brightest + 192 random grid points each, FP64 oracle"
+    out["serving"] = run_serving(dev, frames, rfs, refs, best_f16, threads)
+    base, dflt = out["plain_f32"]["frames_per_s"], out["default_f32"]["frames_per_s"]
     out["speedup_vs_plain_f32"] = {"batched_f16": out["batched_f16"]["frames_per_s"] / base,
-                                   "batched_f32": out["batched_f32"]["frames_per_s"] / base}
-    out["err_db_oracle_frames"] = len(small)
+                                   "batched_f32": out["batched_f32"]["frames_per_s"] / base,
+                                   "default_f32": dflt / base}
+    out["speedup_vs_default_f32"] = {"batched_f16": out["batched_f16"]["frames_per_s"] / dflt,
+                                     "batched_f32": out["batched_f32"]["frames_per_s"] / dflt}
     return out
 
 
-def run_serving(dev, frames, rfs, refs, small, das_config, rates=(50.0, 200.0, 2000.0), n_large=5):
+def run_serving(dev, frames, rfs, refs, das_config, threads, rates=(50.0, 200.0, 2000.0), n_large=5):
     """The serving configuration: the mixed-size frames plus ~10 % large frames
     (128 elements, 4096 samples, 8x, 1024 x 1024, Blackman, SCF) arriving as a
     Poisson stream at each rate in `rates`, RF in pinned host memory, images
     back in host memory, HBM budget 150 GB. The continuous-batching loop with
     FP16 storage and batched graph launches against the same loop serving the
-    plain FP32 form (one frame at a time, plain kernel). Latency = arrival to
-    image in host memory."""
+    plain FP32 form (one frame at a time, direct kernel) and the per-frame
+    FP32 form on the library's default kernels. Latency = arrival to image in
+    host memory. err_db: worst over every frame (mixed and large) against the
+    FP64 oracle at sampled points."""
+    import torch
     from dataclasses import replace
-    from us_lab4a_gb300 import workloads
+    from us_lab4a_gb300 import StaEngine, workloads
     from us_lab4a_gb300.serving import Request, ServingLoop, poisson_arrivals
     large = [workloads.large_serving_frame(seed=1004 + i, storage="f16") for i in range(n_large)]
     allf = list(frames) + large
-    host_rf = [rf.cpu().pin_memory() for rf in rfs] + [fr.make_rf_torch(dev).cpu().pin_memory() for fr in large]
+    large_rf = [fr.make_rf_torch(dev) for fr in large]
+    host_rf = [rf.cpu().pin_memory() for rf in rfs] + [rf.cpu().pin_memory() for rf in large_rf]
+    # FP64 oracle references of the large frames (sample points from an FP32 image of each).
+    large_img = []
+    for fr, rf in zip(large, large_rf):
+        with StaEngine(replace(fr.spec, storage="f32")) as e:
+            g = torch.as_tensor(fr.grid_xyz, device=dev)
+            e.set_grid_device(g)
+            v = torch.empty(fr.grid_xyz.shape[:2], device=dev)
+            f = torch.empty_like(v)
+            e.process_device(rf, v, f)
+            e.synchronize()
+            large_img.append(v.cpu().numpy())
+    del large_rf
+    lrefs = _fp64_refs(large, [h.numpy() for h in host_rf[len(frames):]], large_img, threads)
+    all_refs = dict(refs)
+    all_refs.update({len(frames) + i: r for i, r in lrefs.items()})
     order = np.random.default_rng(12).permutation(len(allf))  # large frames spread through the stream
     out = {"workload": f"{len(frames)} mixed-size frames + {n_large} frames of 128 elements, 4096 samples, 8x, "
                        f"1024x1024, SCF; Poisson arrivals; host RF in, host image out",
            "frames": len(allf), "hbm_budget_gb": 150}
-    for name, storage, plain in (("batched_f16", "f16", False), ("plain_f32", "f32", True)):
+    forms = (("batched_f16", "f16", False, False), ("plain_f32", "f32", True, False),
+             ("default_f32", "f32", False, True))
+    for name, storage, plain, per_frame in forms:
         loop = ServingLoop(hbm_budget_bytes=150 << 30, max_batch=len(allf), max_elements=128,
-                           das_config=None if plain else das_config, device=dev, plain=plain)
+                           das_config=None if (plain or per_frame) else das_config, device=dev, plain=plain,
+                           per_frame=per_frame)
 
         def requests(rate):
             arr = poisson_arrivals(len(allf), rate, seed=11)
@@ -576,15 +753,16 @@ def run_serving(dev, frames, rfs, refs, small, das_config, rates=(50.0, 200.0, 2
             row = {"arrival_rate": rate, "frames_per_s": st["frames_per_s"], "p50_ms": st["p50_ms"],
                    "p99_ms": st["p99_ms"], "batches": st["batches"], "mean_batch": st["mean_batch"]}
             if rate == max(rates):
-                by_id = {r.rid: r for r in reqs}
-                row["err_db"] = max(_db(float(np.abs(by_id[i].value.astype(np.float64) - refs[i]).max()),
-                                        float(np.abs(refs[i]).max())) for i in small)
+                by_id = {r.rid: r.value for r in reqs}
+                row["err_db"] = _worst_db(all_refs, by_id)
             per_rate.append(row)
         out[name] = {"rates": per_rate, "peak_resident_gb": loop.peak_bytes / 1e9}
         loop.close()
-    sat_f16 = out["batched_f16"]["rates"][-1]["frames_per_s"]
-    sat_f32 = out["plain_f32"]["rates"][-1]["frames_per_s"]
-    out["speedup_at_saturation"] = sat_f16 / sat_f32
+    sat = {k: out[k]["rates"][-1] for k, _, _, _ in forms}
+    out["speedup_at_saturation"] = sat["batched_f16"]["frames_per_s"] / sat["plain_f32"]["frames_per_s"]
+    out["speedup_at_saturation_vs_default_f32"] = (sat["batched_f16"]["frames_per_s"]
+                                                   / sat["default_f32"]["frames_per_s"])
+    out["err_db_frames"] = f"all {len(allf)} frames at 2000 arrivals/s, 64 brightest + 192 random points each"
     return out
 
 
