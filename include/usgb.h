@@ -176,7 +176,10 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * registers, no per-point table, so arrays of hundreds of elements stage as
  * well), 3 = receiver-group on tiles of 64 columns x tile_rows (4 or 8) rows
  * (windows only a little longer for twice the points: fewer bytes and half
- * the copies staged per frame). 0 for tile_rows / stage_bytes / stages keeps
+ * the copies staged per frame), 4 = as 3 with two grid points (neighbouring
+ * rows) per consumer thread, tiles of 64 columns x 2 * tile_rows rows (twice
+ * the independent loads per warp between two stage waits, fewer bytes staged
+ * per point). 0 for tile_rows / stage_bytes / stages keeps
  * the current value. New
  * contexts start with the receiver-group kernel (32 x 4 tiles, 2 x 32 KiB)
  * where it fits; setting a grid of at least two 64-column tiles per SM then

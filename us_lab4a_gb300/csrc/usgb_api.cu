@@ -279,6 +279,7 @@ usgb::DasParams das_params(const usgb_ctx* c, const void* d_sig, float* d_value,
 	dp.factor = d_factor;
 	dp.errWord = c->d_err;
 	dp.tileCols = usgb::das_tile_cols(c->dasVariant);
+	dp.pointsPerThread = usgb::das_points_per_thread(c->dasVariant);
 	dp.tileRows = c->tileRows;
 	dp.stageBytes = c->stageBytes;
 	dp.stages = c->stages;
@@ -665,13 +666,13 @@ int usgb_signal_info(const usgb_ctx* c, uint32_t* signal_length, uint32_t* fft_s
 int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return guarded(c, [&] {
-		if (variant < 0 || variant > 3) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
+		if (variant < 0 || variant > 4) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Invalid delay-and-sum variant: " << variant << '.');
 		const unsigned rows = tile_rows ? tile_rows : c->tileRows;
 		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
 		const unsigned nst = stages ? stages : c->stages;
 		if (variant != 0) {
 			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
-			if (variant == 3 && rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
+			if (variant >= 3 && rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
 				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 			}
@@ -720,11 +721,12 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		const unsigned iters = iterations ? iterations : 3;
 		struct Cand { int variant; unsigned rows, cap, stages; };
 		std::vector<Cand> cands;
-		for (int variant : {1, 2, 3})
+		for (int variant : {1, 2, 3, 4})
 			for (unsigned rows : {4u, 8u, 16u})
-				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u, 65536u, 98304u, 102400u})
+				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u, 65536u, 98304u, 102400u,
+						110592u})
 					for (unsigned nst : {2u, 3u, 4u})
-						if ((variant >= 2 || cap % 8192u == 0) && !(variant == 3 && rows == 16)
+						if ((variant >= 2 || cap % 8192u == 0) && !(variant >= 3 && rows == 16)
 								&& das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
 							cands.push_back({variant, rows, cap, nst});
 		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});

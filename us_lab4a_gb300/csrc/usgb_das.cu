@@ -146,7 +146,7 @@ cudaError_t dispatch_cf(const DasParams& p, int cf, bool analytic, cudaStream_t 
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream)
 {
 	if (variant == 1) return launch_das_staged(p, storage, cf, analytic, stream);
-	if (variant == 2 || variant == 3) return launch_das_group(p, storage, cf, analytic, stream);
+	if (variant >= 2 && variant <= 4) return launch_das_group(p, storage, cf, analytic, stream);
 	switch (storage) {
 	case STORE_F16: return dispatch_cf<STORE_F16>(p, cf, analytic, stream);
 	case STORE_BF16: return dispatch_cf<STORE_BF16>(p, cf, analytic, stream);

@@ -261,73 +261,103 @@ __device__ bool group_produce(const DasParams& p, const GroupSmem& sm, int& it, 
 }
 
 // ------------------------------------------------------------- consumers
-// The group's gathers of one unit into `acc` (the accumulators of the unit's
-// transmitter parity). FULL: every receiver of the group exists.
-template<typename SP, bool Q, bool FULL>
+// A consumer thread forms PY grid points of one column (PY = 1, or 2
+// neighbouring rows): each unit's gathers for every point are independent, so
+// a warp has PY times the loads in flight between two waits, and a tile of
+// PY x the rows stages windows that are only a little longer.
+//
+// The group's gathers of one unit into `acc` (point k's accumulators of the
+// group's receivers). FULL: every receiver of the group exists.
+template<typename SP, bool Q, bool FULL, int PY>
 __device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un, const int* base,
-		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg, float txv,
-		const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
+		const float (&txv)[PY], const float (&rxd)[PY][kGroup], unsigned lastIdx, const Fixed& fx,
+		float2 (&acc)[PY][kGroup])
 {
 	using T = typename SP::T;
 	if (FULL && (un.y & kUnitInterior)) {
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
-			float k;
-			const int i = Delay<Q>::split(txv, rxd[j], k, fx);
-			SP::accumulate(buf + (i + base[j]), k, acc[j]);
+#pragma unroll
+			for (int k = 0; k < PY; ++k) {
+				float w;
+				const int i = Delay<Q>::split(txv[k], rxd[k][j], w, fx);
+				SP::accumulate(buf + (i + base[j]), w, acc[k][j]);
+			}
 		}
 	} else if (!anyGlobal) {
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
-			if (FULL || static_cast<unsigned>(j) < nrg) gather_staged<SP, Q>(buf, base[j], txv, rxd[j], lastIdx, fx, zero, acc[j]);
+			if (FULL || static_cast<unsigned>(j) < nrg) {
+#pragma unroll
+				for (int k = 0; k < PY; ++k) {
+					gather_staged<SP, Q>(buf, base[j], txv[k], rxd[k][j], lastIdx, fx, zero, acc[k][j]);
+				}
+			}
 		}
 	} else {
 		const T* sig = reinterpret_cast<const T*>(p.sig) + static_cast<size_t>(un.x) * p.numRx * p.sigStride;
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
 			if (FULL || static_cast<unsigned>(j) < nrg) {
-				if ((un.y >> j) & 1) {
-					gather_global<SP, Q>(sig + static_cast<size_t>(g * kGroup + j) * p.sigStride, txv, rxd[j], lastIdx,
-							fx, acc[j]);
-				} else {
-					gather_staged<SP, Q>(buf, base[j], txv, rxd[j], lastIdx, fx, zero, acc[j]);
+#pragma unroll
+				for (int k = 0; k < PY; ++k) {
+					if ((un.y >> j) & 1) {
+						gather_global<SP, Q>(sig + static_cast<size_t>(g * kGroup + j) * p.sigStride, txv[k], rxd[k][j],
+								lastIdx, fx, acc[k][j]);
+					} else {
+						gather_staged<SP, Q>(buf, base[j], txv[k], rxd[k][j], lastIdx, fx, zero, acc[k][j]);
+					}
 				}
 			}
 		}
 	}
 }
 
-// One unit u of stage m with its transmitter's delay txv: the group's gathers.
-template<typename SP, bool Q, bool FULL>
-__device__ __forceinline__ void group_unit(const DasParams& p, const GroupStage& m, int u, float txv,
+// One unit u of stage m with its transmitter's delays txv: the group's gathers.
+template<typename SP, bool Q, bool FULL, int PY>
+__device__ __forceinline__ void group_unit(const DasParams& p, const GroupStage& m, int u, const float (&txv)[PY],
 		const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
-		const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+		const float (&rxd)[PY][kGroup], unsigned lastIdx, const Fixed& fx, float2 (&acc)[PY][kGroup])
 {
 	const int2 un = m.unit[u];
 	const int4 b0 = *reinterpret_cast<const int4*>(&m.base[u][0]);
 	const int4 b1 = *reinterpret_cast<const int4*>(&m.base[u][4]);
 	const int base[kGroup] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-	group_gathers<SP, Q, FULL>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, acc);
+	group_gathers<SP, Q, FULL, PY>(p, un, base, buf, zero, anyGlobal, g, nrg, txv, rxd, lastIdx, fx, acc);
 }
 
-// The units of stage m (at least one), each unit's transmit delay computed
-// one unit ahead so that its square root overlaps the previous unit's gathers.
-template<typename SP, bool Q, bool FULL>
+// The units of stage m (at least one), each unit's transmit delays computed
+// one unit ahead so that their square roots overlap the previous unit's gathers.
+template<typename SP, bool Q, bool FULL, int PY>
 __device__ __forceinline__ void group_stage_units(const DasParams& p, const GroupSmem& sm, const GroupStage& m,
 		int count, const typename SP::T* buf, const typename SP::T* zero, bool anyGlobal, unsigned g, unsigned nrg,
-		float px, float py, float pz, const float* rxd, unsigned lastIdx, const Fixed& fx, float2 (&acc)[kGroup])
+		const float (&px)[PY], const float (&py)[PY], const float (&pz)[PY], const float (&rxd)[PY][kGroup],
+		unsigned lastIdx, const Fixed& fx, float2 (&acc)[PY][kGroup])
 {
-	float txNext = Delay<Q>::tx(p, sm.txinfo[m.unit[0].x], px, py, pz, fx);
+	float txNext[PY];
+	{
+		const float2 e = sm.txinfo[m.unit[0].x];
+#pragma unroll
+		for (int k = 0; k < PY; ++k) txNext[k] = Delay<Q>::tx(p, e, px[k], py[k], pz[k], fx);
+	}
 	for (int u = 0; u < count; ++u) {
-		const float txv = txNext;
-		if (u + 1 < count) txNext = Delay<Q>::tx(p, sm.txinfo[m.unit[u + 1].x], px, py, pz, fx);
-		group_unit<SP, Q, FULL>(p, m, u, txv, buf, zero, anyGlobal, g, nrg, rxd, lastIdx, fx, acc);
+		float txv[PY];
+#pragma unroll
+		for (int k = 0; k < PY; ++k) txv[k] = txNext[k];
+		if (u + 1 < count) {
+			const float2 e = sm.txinfo[m.unit[u + 1].x];
+#pragma unroll
+			for (int k = 0; k < PY; ++k) txNext[k] = Delay<Q>::tx(p, e, px[k], py[k], pz[k], fx);
+		}
+		group_unit<SP, Q, FULL, PY>(p, m, u, txv, buf, zero, anyGlobal, g, nrg, rxd, lastIdx, fx, acc);
 	}
 }
 
-template<typename SP, int CF, bool Q>
-__device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, float px, float py, float pz,
-		bool active, unsigned pix, const Fixed& fx)
+template<typename SP, int CF, bool Q, int PY>
+__device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, const float (&px)[PY],
+		const float (&py)[PY], const float (&pz)[PY], const bool (&active)[PY], const unsigned (&pix)[PY],
+		const Fixed& fx)
 {
 	using T = typename SP::T;
 	const int nst = static_cast<int>(sm.nst);
@@ -335,18 +365,24 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 	const unsigned lastIdx = p.L - 2;
 	const T* zero = reinterpret_cast<const T*>(sm.zero);
 	const unsigned numGroups = (p.numRx + kGroup - 1) / kGroup;
-	float2 total = make_float2(0.f, 0.f);
-	CFState<CF> cf;
+	float2 total[PY];
+	CFState<CF> cf[PY];
+#pragma unroll
+	for (int k = 0; k < PY; ++k) total[k] = make_float2(0.f, 0.f);
 	int s = it % nst;
 	unsigned phase = static_cast<unsigned>(it / nst) & 1u;
 	for (unsigned g = 0; g < numGroups; ++g) {
 		const unsigned nrg = min(static_cast<unsigned>(kGroup), p.numRx - g * kGroup);
-		float rxd[kGroup];
-		float2 acc[kGroup];  // receiver g * kGroup + j's terms, in transmitter order
+		float rxd[PY][kGroup];
+		float2 acc[PY][kGroup];  // point k, receiver g * kGroup + j: its terms in transmitter order
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
-			rxd[j] = (static_cast<unsigned>(j) < nrg) ? Delay<Q>::rx(p, sm.rxinfo[g * kGroup + j], px, py, pz, fx) : 0.0f;
-			acc[j] = make_float2(0.f, 0.f);
+			const float4 e = (static_cast<unsigned>(j) < nrg) ? sm.rxinfo[g * kGroup + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+			for (int k = 0; k < PY; ++k) {
+				rxd[k][j] = (static_cast<unsigned>(j) < nrg) ? Delay<Q>::rx(p, e, px[k], py[k], pz[k], fx) : 0.0f;
+				acc[k][j] = make_float2(0.f, 0.f);
+			}
 		}
 		bool last = false;
 		while (!last) {
@@ -358,11 +394,11 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 			const T* buf = reinterpret_cast<const T*>(sm.stageBuf + static_cast<size_t>(s) * capBytes);
 			const int4 head = *reinterpret_cast<const int4*>(&m.count);
 			if (nrg == static_cast<unsigned>(kGroup)) {
-				group_stage_units<SP, Q, true>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx,
-						fx, acc);
+				group_stage_units<SP, Q, true, PY>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd,
+						lastIdx, fx, acc);
 			} else {
-				group_stage_units<SP, Q, false>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd, lastIdx,
-						fx, acc);
+				group_stage_units<SP, Q, false, PY>(p, sm, m, head.x, buf, zero, head.z != 0, g, nrg, px, py, pz, rxd,
+						lastIdx, fx, acc);
 			}
 			last = head.y != 0;
 			__syncwarp();
@@ -376,23 +412,33 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 #pragma unroll
 		for (int j = 0; j < kGroup; ++j) {
 			if (static_cast<unsigned>(j) < nrg) {
-				const float2 rs = receiver_sum(acc[j], sm.rxinfo[g * kGroup + j].z);
-				total.x += rs.x;
-				total.y += rs.y;
-				cf.add(rs);
+				const float w = sm.rxinfo[g * kGroup + j].z;
+#pragma unroll
+				for (int k = 0; k < PY; ++k) {
+					const float2 rs = receiver_sum(acc[k][j], w);
+					total[k].x += rs.x;
+					total[k].y += rs.y;
+					cf[k].add(rs);
+				}
 			}
 		}
 	}
-	if (active) {
-		const float v = SP::kAnalytic ? magnitude(total) : total.x;
-		p.value[pix] = v * p.valueCoef;
-		p.factor[pix] = cf.result(p.numRx, p, total);
+#pragma unroll
+	for (int k = 0; k < PY; ++k) {
+		if (active[k]) {
+			const float v = SP::kAnalytic ? magnitude(total[k]) : total[k].x;
+			p.value[pix[k]] = v * p.valueCoef;
+			p.factor[pix[k]] = cf[k].result(p.numRx, p, total[k]);
+		}
 	}
 	return true;
 }
 
-// One tile (bx, by) of one frame; `it` is the block's running stage counter.
-template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
+// One tile (bx, by) of one frame: TCOLS columns x TROWS * PY rows, thread
+// (warp w, lane l) on column bx * TCOLS + (w % CW) * 32 + l and rows
+// by * TROWS * PY + (w / CW) * PY + k, k < PY; `it` is the block's running
+// stage counter.
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
 __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx, unsigned by, int& it)
 {
 	using SP = Sample<ANALYTIC, S>;
@@ -402,18 +448,25 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	const int lane = threadIdx.x & 31;
 	const bool producer = warp == NCW;
 	const unsigned col = bx * TCOLS + (warp % CW) * 32 + lane;
-	const unsigned row = by * TROWS + warp / CW;
-	const bool active = !producer && col < p.ncols && row < p.nrows;
-	const unsigned pix = col * p.nrows + row;
+	const unsigned row0 = by * (TROWS * PY) + (warp / CW) * PY;
 	const unsigned nE = p.numTx + p.numRx;
 
 	// Threads beyond the grid's edge take the nearest grid point of the tile.
-	float px = 0.f, py = 0.f, pz = 0.f;
-	if (!producer) {
-		const unsigned q = min(col, p.ncols - 1) * p.nrows + min(row, p.nrows - 1);
-		px = p.grid[3 * q];
-		py = p.grid[3 * q + 1];
-		pz = p.grid[3 * q + 2];
+	float px[PY], py[PY], pz[PY];
+	bool active[PY];
+	unsigned pix[PY];
+#pragma unroll
+	for (int k = 0; k < PY; ++k) {
+		const unsigned row = row0 + k;
+		active[k] = !producer && col < p.ncols && row < p.nrows;
+		pix[k] = col * p.nrows + row;
+		px[k] = py[k] = pz[k] = 0.f;
+		if (!producer) {
+			const unsigned q = min(col, p.ncols - 1) * p.nrows + min(row, p.nrows - 1);
+			px[k] = p.grid[3 * q];
+			py[k] = p.grid[3 * q + 1];
+			pz[k] = p.grid[3 * q + 2];
+		}
 	}
 	if (threadIdx.x == 0) {
 		sm.tileMax[0] = 0;
@@ -428,15 +481,18 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	// Per-warp min/max of every element's FP32 delay over the tile.
 	if (!producer) {
 		for (unsigned e = 0; e < nE; ++e) {
-			float v;
-			if (e < p.numTx) {
-				v = __fadd_rn(p.signalOffset,
-						__fmul_rn(distance3d_z0(__ldg(&p.txXY[2 * e]), __ldg(&p.txXY[2 * e + 1]), px, py, pz), p.invCT));
-			} else {
-				const unsigned r = e - p.numTx;
-				v = __fmul_rn(distance3d_z0(__ldg(&p.rxXY[2 * r]), __ldg(&p.rxXY[2 * r + 1]), px, py, pz), p.invCT);
+			const bool isTx = e < p.numTx;
+			const unsigned r = e - p.numTx;
+			const float ex = isTx ? __ldg(&p.txXY[2 * e]) : __ldg(&p.rxXY[2 * r]);
+			const float ey = isTx ? __ldg(&p.txXY[2 * e + 1]) : __ldg(&p.rxXY[2 * r + 1]);
+			float mn = 0.f, mx = 0.f;
+#pragma unroll
+			for (int k = 0; k < PY; ++k) {
+				const float d = __fmul_rn(distance3d_z0(ex, ey, px[k], py[k], pz[k]), p.invCT);
+				const float v = isTx ? __fadd_rn(p.signalOffset, d) : d;
+				mn = (k == 0) ? v : fminf(mn, v);
+				mx = (k == 0) ? v : fmaxf(mx, v);
 			}
-			float mn = v, mx = v;
 			for (int o = 16; o > 0; o >>= 1) {
 				mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
 				mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -466,8 +522,8 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	const bool q = p.delayMode == 2 || (p.delayMode == 0 && topTx + topRx > kDeepDelaySamples);
 	const Fixed fx = fixed_format(fmaxf(fmaxf(topTx, topRx), fabsf(p.signalOffset)));
 	if (producer) return group_produce<SP>(p, sm, it, q ? 2.0f : 0.0f);
-	return q ? group_consume<SP, CF, true>(p, sm, it, px, py, pz, active, pix, fx)
-	         : group_consume<SP, CF, false>(p, sm, it, px, py, pz, active, pix, fx);
+	return q ? group_consume<SP, CF, true, PY>(p, sm, it, px, py, pz, active, pix, fx)
+	         : group_consume<SP, CF, false, PY>(p, sm, it, px, py, pz, active, pix, fx);
 }
 
 // Resident blocks per SM the register allocation is held to, by consumer
@@ -476,11 +532,14 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 // only 3 blocks in). Batches (every coherence factor in one kernel, more live
 // state): 3 for 4 and 2 for 8 consumer warps (fewer spills than at 5 and 3;
 // measured faster on the mixed batch).
-template<int NCW> constexpr int group_min_blocks() { return NCW == 4 ? 5 : (NCW == 8 ? 3 : 1); }
+template<int NCW, int PY = 1> constexpr int group_min_blocks()
+{
+	return PY == 2 ? 1 : (NCW == 4 ? 5 : (NCW == 8 ? 3 : 1));
+}
 template<int NCW> constexpr int group_batch_min_blocks() { return NCW == 4 ? 3 : (NCW == 8 ? 2 : 1); }
 
-template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
-__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_min_blocks<TROWS * TCOLS / 32>())
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY>
+__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_min_blocks<TROWS * TCOLS / 32, PY>())
 das_group_kernel(DasParams p)
 {
 	constexpr int NCW = TROWS * TCOLS / 32;
@@ -489,27 +548,33 @@ das_group_kernel(DasParams p)
 	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, NCW, p.stages, p.stageBytes);
 	init_group_barriers(sm, NCW);
 	int it = 0;
-	group_tile<S, CF, ANALYTIC, TCOLS, TROWS>(p, sm, blockIdx.x, blockIdx.y, it);
+	group_tile<S, CF, ANALYTIC, TCOLS, TROWS, PY>(p, sm, blockIdx.x, blockIdx.y, it);
 }
 
-template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS>
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
 cudaError_t launch_group_one(const DasParams& p, cudaStream_t stream)
 {
 	constexpr int NCW = TROWS * TCOLS / 32;
 	const GroupLayout lay(p.numTx, p.numRx, NCW, p.stageBytes, p.stages);
-	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS>,
+	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS, PY>,
 			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
-	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + TROWS - 1) / TROWS);
-	das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS><<<grid, (NCW + 1) * 32, lay.total, stream>>>(p);
+	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + TROWS * PY - 1) / (TROWS * PY));
+	das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS, PY><<<grid, (NCW + 1) * 32, lay.total, stream>>>(p);
 	return cudaGetLastError();
 }
 
-// Tile shapes (columns x rows): 32 x 4, 32 x 8, 32 x 16, 64 x 4, 64 x 8.
+// Tile shapes (columns x rows): 32 x 4, 32 x 8, 32 x 16, 64 x 4, 64 x 8; with
+// two points per thread (p.pointsPerThread == 2, 64-column tiles): 64 x 8
+// and 64 x 16.
 template<int S, int CF, bool ANALYTIC>
 cudaError_t launch_group_rows(const DasParams& p, cudaStream_t stream)
 {
 	if (p.tileCols == 64) {
+		if (p.pointsPerThread == 2) {
+			return p.tileRows == 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4, 2>(p, stream)
+			                       : launch_group_one<S, CF, ANALYTIC, 64, 8, 2>(p, stream);
+		}
 		return p.tileRows == 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4>(p, stream)
 		                       : launch_group_one<S, CF, ANALYTIC, 64, 8>(p, stream);
 	}

@@ -108,10 +108,14 @@ struct DasParams {
 	unsigned tileRows;
 	unsigned stageBytes;
 	unsigned stages;
+	// Receiver-group kernel: grid points per consumer thread (0 or 1: one;
+	// 2: two neighbouring rows, the tile then spans 2 x tileRows rows).
+	unsigned pointsPerThread;
 };
 
 // variant 0: plain kernel; 1: staged kernel; 2: receiver-group kernel
-// (32-column tiles); 3: receiver-group kernel, 64-column tiles.
+// (32-column tiles); 3: receiver-group kernel, 64-column tiles; 4: as 3 with
+// two grid points (neighbouring rows) per consumer thread.
 cudaError_t launch_das(const DasParams& p, int storage, int cf, bool analytic, int variant, cudaStream_t stream);
 cudaError_t launch_das_staged(const DasParams& p, int storage, int cf, bool analytic, cudaStream_t stream);
 // variant 2: receiver-group kernel (usgb_das_group.cu).
@@ -119,7 +123,9 @@ cudaError_t launch_das_group(const DasParams& p, int storage, int cf, bool analy
 size_t das_group_smem_bytes(unsigned numTx, unsigned numRx, unsigned tileCols, unsigned tileRows, unsigned capBytes,
 		unsigned stages);
 // Tile columns of a delay-and-sum variant.
-inline unsigned das_tile_cols(int variant) { return variant == 3 ? 64u : 32u; }
+inline unsigned das_tile_cols(int variant) { return variant >= 3 ? 64u : 32u; }
+// Grid-point rows of a tile per thread row (variant 4: two).
+inline unsigned das_points_per_thread(int variant) { return variant == 4 ? 2u : 1u; }
 
 // ---------------------------------------------------------------------------
 // Batched (multi-frame) launches: persistent blocks walk the work items of
