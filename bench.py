@@ -233,9 +233,9 @@ def run_gpu(args):
     eng = StaEngine(spec)
     if args.das == "plain":
         eng.set_das_variant(0)
-    elif args.das in ("staged", "group", "group64") and not args.autotune:
-        eng.set_das_variant({"staged": 1, "group": 2, "group64": 3}[args.das], args.tile_rows, args.stage_bytes,
-                            args.stages)
+    elif args.das in ("staged", "group", "group64", "group64x2") and not args.autotune:
+        eng.set_das_variant({"staged": 1, "group": 2, "group64": 3, "group64x2": 4}[args.das], args.tile_rows,
+                            args.stage_bytes, args.stages)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream)
     with torch.cuda.stream(stream):
@@ -364,7 +364,8 @@ def run_gpu(args):
     # (152 SMs x 128 lanes x 2 FLOP/clk).
     onchip = None
     if das_cfg["variant"] != 0:
-        staged = staged_bytes_model(frame, 64 if das_cfg["variant"] == 3 else 32, das_cfg["tile_rows"], esize)
+        staged = staged_bytes_model(frame, 64 if das_cfg["variant"] >= 3 else 32,
+                                    das_cfg["tile_rows"] * (2 if das_cfg["variant"] == 4 else 1), esize)
         tap_bytes = 2.0 * esize * gathers
         mhz = (clk or {}).get("sm_mhz") or 2070.0
         smem_peak = 152 * 128 * mhz * 1e6 / 1e9
@@ -464,7 +465,8 @@ def run_gpu(args):
             "config": _config(frame, desc, spec.storage),
             "implementation": {"das_kernel": ("plain" if das_cfg["variant"] == 0 else
                                ("staged" if das_cfg["variant"] == 1 else "receiver-group")
-                               + f" (tile {64 if das_cfg['variant'] == 3 else 32}x{das_cfg['tile_rows']}, "
+                               + f" (tile {64 if das_cfg['variant'] >= 3 else 32}x"
+                               + f"{das_cfg['tile_rows'] * (2 if das_cfg['variant'] == 4 else 1)}, "
                                + f"{das_cfg['stages']} x {das_cfg['stage_bytes']} B stages"
                                + (", autotuned)" if args.autotune else ")")),
                                "frames_in_flight": f"{args.pipeline} contexts on {args.pipeline} streams take the "
@@ -982,7 +984,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cf2d", choices=["cf2d", "plain2d", "matrix3d"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
-    ap.add_argument("--das", default="auto", choices=["auto", "plain", "staged", "group", "group64"],
+    ap.add_argument("--das", default="auto", choices=["auto", "plain", "staged", "group", "group64", "group64x2"],
                     help="delay-and-sum kernel; auto = autotuned over every kernel and shape")
     ap.add_argument("--tile-rows", type=int, default=4)
     ap.add_argument("--stage-bytes", type=int, default=32768)

@@ -277,17 +277,17 @@ def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes)
     rf = torch.as_tensor(frame.make_rf_numpy(), device=cuda)
     g = torch.as_tensor(frame.grid_xyz, device=cuda)
     out = []
-    for variant in (0, 1, 2, 3):
+    for variant in (0, 1, 2, 3, 4):
         with StaEngine(frame.spec) as eng:
             eng.set_stream(torch.cuda.current_stream())
-            eng.set_das_variant(variant, min(rows, 8) if variant == 3 else rows, stage_bytes)
+            eng.set_das_variant(variant, min(rows, 8) if variant >= 3 else rows, stage_bytes)
             eng.set_grid_device(g)
             v = torch.empty(frame.grid_xyz.shape[:2], device=cuda)
             f = torch.empty_like(v)
             eng.process_device(rf, v, f)
             eng.synchronize()
             out.append((v.cpu().numpy(), f.cpu().numpy()))
-    for variant in (1, 2, 3):
+    for variant in (1, 2, 3, 4):
         assert np.array_equal(out[0][0], out[variant][0]), variant
         assert np.array_equal(out[0][1], out[variant][1]), variant
 
@@ -311,7 +311,8 @@ def test_grid_selects_tile_width(cuda):
         assert eng.das_config() == {"variant": 2, "tile_rows": 8, "stage_bytes": 16384, "stages": 2}
 
 
-@pytest.mark.parametrize("cfg", [(3, 8, 102400, 2), (3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2)])
+@pytest.mark.parametrize("cfg", [(3, 8, 102400, 2), (3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2),
+                                 (4, 8, 102400, 2), (4, 8, 65536, 2), (4, 4, 102400, 2), (4, 8, 16384, 3)])
 def test_large_stages_equal_plain_kernel(cuda, cfg):
     """Stages of 64-96 KiB (several units each, one block per SM) give the
     plain kernel's images bit for bit (PCF, partial tiles, FP32 and FP16)."""

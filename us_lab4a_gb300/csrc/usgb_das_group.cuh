@@ -54,6 +54,28 @@ constexpr int kMaxUnits = 32 / kGroup;     // units sized per producer pass (one
 // [0, L - 2] and the gathers need no range test.
 constexpr unsigned kUnitInterior = 0x100u;
 
+// Block shape of a tile: NCW consumer warps and the producer. With two points
+// per thread on 16 consumer warps (64 x 16 tiles) the consumers need more
+// registers than an even share of the register file: the block then has
+// 20 warps (5 warpgroups), launched at kLaunchRegs registers a thread; the
+// producer warpgroup (the producer warp and 3 warps that exit) drops to
+// kProducerRegs and the 4 consumer warpgroups rise to kConsumerRegs
+// (setmaxnreg). The split balances exactly:
+// 640 x 96 = 128 x 32 + 512 x 112 = 61440 registers.
+template<int NCW, int PY> struct GroupShape {
+	static constexpr bool kSplit = PY == 2 && NCW == 16;
+	static constexpr int kWarps = kSplit ? NCW + 4 : NCW + 1;
+	static constexpr int kLaunchRegs = 96;
+	static constexpr int kProducerRegs = 32;
+	static constexpr int kConsumerRegs = 112;
+	static_assert(!kSplit || kWarps * 32 * kLaunchRegs == 128 * kProducerRegs + NCW * 32 * kConsumerRegs,
+			"register split must add up to the launch allocation");
+	static_assert(!kSplit || kWarps * 32 * kLaunchRegs <= 65536, "launch allocation exceeds the register file");
+};
+
+template<int N> __device__ __forceinline__ void regs_dec() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" :: "n"(N)); }
+template<int N> __device__ __forceinline__ void regs_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" :: "n"(N)); }
+
 // One stage: up to kMaxUnits units (consecutive transmitters of one receiver
 // group). Window j of unit u: sample idx of receiver g * kGroup + j sits at
 // stage element idx + base[u][j].
@@ -446,7 +468,7 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	constexpr int NCW = TROWS * CW;     // consumer warps
 	const int warp = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
-	const bool producer = warp == NCW;
+	const bool producer = warp >= NCW;   // the producer warp (NCW), and the exiting warps of a split block
 	const unsigned col = bx * TCOLS + (warp % CW) * 32 + lane;
 	const unsigned row0 = by * (TROWS * PY) + (warp / CW) * PY;
 	const unsigned nE = p.numTx + p.numRx;
@@ -521,6 +543,16 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	const float topTx = __int_as_float(sm.tileMax[0]), topRx = __int_as_float(sm.tileMax[1]);
 	const bool q = p.delayMode == 2 || (p.delayMode == 0 && topTx + topRx > kDeepDelaySamples);
 	const Fixed fx = fixed_format(fmaxf(fmaxf(topTx, topRx), fabsf(p.signalOffset)));
+	using Shape = GroupShape<NCW, PY>;
+	if constexpr (Shape::kSplit) {
+		// Warpgroup-uniform branches (warps 0-15: consumers; 16-19: producer group).
+		if (producer) {
+			regs_dec<Shape::kProducerRegs>();
+			if (warp != NCW) return true;
+		} else {
+			regs_inc<Shape::kConsumerRegs>();
+		}
+	}
 	if (producer) return group_produce<SP>(p, sm, it, q ? 2.0f : 0.0f);
 	return q ? group_consume<SP, CF, true, PY>(p, sm, it, px, py, pz, active, pix, fx)
 	         : group_consume<SP, CF, false, PY>(p, sm, it, px, py, pz, active, pix, fx);
@@ -539,7 +571,8 @@ template<int NCW, int PY = 1> constexpr int group_min_blocks()
 template<int NCW> constexpr int group_batch_min_blocks() { return NCW == 4 ? 3 : (NCW == 8 ? 2 : 1); }
 
 template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY>
-__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_min_blocks<TROWS * TCOLS / 32, PY>())
+__global__ void __launch_bounds__(GroupShape<TROWS * TCOLS / 32, PY>::kWarps * 32,
+		group_min_blocks<TROWS * TCOLS / 32, PY>())
 das_group_kernel(DasParams p)
 {
 	constexpr int NCW = TROWS * TCOLS / 32;
@@ -555,12 +588,20 @@ template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
 cudaError_t launch_group_one(const DasParams& p, cudaStream_t stream)
 {
 	constexpr int NCW = TROWS * TCOLS / 32;
+	using Shape = GroupShape<NCW, PY>;
+	const auto kernel = das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS, PY>;
 	const GroupLayout lay(p.numTx, p.numRx, NCW, p.stageBytes, p.stages);
-	cudaError_t e = cudaFuncSetAttribute(das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS, PY>,
-			cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
+	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
+	if constexpr (Shape::kSplit) {
+		// The register split assumes the launch allocation it was balanced
+		// against; a build that allocates otherwise is not launched.
+		cudaFuncAttributes fa{};
+		if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
+		if (fa.numRegs != Shape::kLaunchRegs) return cudaErrorInvalidConfiguration;
+	}
 	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + TROWS * PY - 1) / (TROWS * PY));
-	das_group_kernel<S, CF, ANALYTIC, TCOLS, TROWS, PY><<<grid, (NCW + 1) * 32, lay.total, stream>>>(p);
+	kernel<<<grid, Shape::kWarps * 32, lay.total, stream>>>(p);
 	return cudaGetLastError();
 }
 
