@@ -182,9 +182,11 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * per point). 0 for tile_rows / stage_bytes / stages keeps
  * the current value. New
  * contexts start with the receiver-group kernel (32 x 4 tiles, 2 x 32 KiB)
- * where it fits; setting a grid of at least two 64-column tiles per SM then
- * selects variant 3 (64 x 8 with 2 x 96 KiB stages, else 64 x 4 with 2 x 48
- * KiB) where it fits, unless a variant was set here or by usgb_autotune_das. */
+ * where it fits; setting a grid of at least 1.5 tiles of 64 x 16 points per
+ * SM then selects variant 4 (tile_rows 8, 2 x 100 KiB stages), else one of at
+ * least two 64-column tiles per SM variant 3 (64 x 8 with 2 x 100 or 96 KiB
+ * stages, else 64 x 4 with 2 x 48 KiB) where it fits, unless a variant was
+ * set here or by usgb_autotune_das. */
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);

@@ -293,9 +293,11 @@ def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes)
 
 
 def test_grid_selects_tile_width(cuda):
-    """Without an explicit choice, a grid of at least two 64 x 4 tiles per SM
-    selects the receiver-group kernel on 64-column tiles, a small grid keeps
-    32-column tiles, and a variant set explicitly survives a new grid."""
+    """Without an explicit choice, a grid of at least 1.5 tiles of 64 x 16 per
+    SM selects the two-points-per-thread kernel on 64 x 16 tiles, one of at
+    least two 64 x 8 tiles per SM the receiver-group kernel on 64-column
+    tiles, a small grid keeps 32-column tiles, and a variant set explicitly
+    survives a new grid."""
     import torch
     from us_lab4a_gb300 import StaEngine, workloads
     frame = workloads.cf2d(small=True)
@@ -303,6 +305,8 @@ def test_grid_selects_tile_width(cuda):
         eng.set_grid_device(torch.zeros((32, 32, 3), device=cuda))
         assert eng.das_config()["variant"] == 2
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
+        assert eng.das_config() == {"variant": 4, "tile_rows": 8, "stage_bytes": 102400, "stages": 2}
+        eng.set_grid_device(torch.zeros((256, 512, 3), device=cuda))
         cfg = eng.das_config()
         assert cfg["variant"] == 3 and (cfg["tile_rows"], cfg["stage_bytes"]) in ((8, 102400), (8, 98304), (4, 49152),
                                                                                    (4, 32768))

@@ -353,11 +353,13 @@ void choose_default_das(usgb_ctx* c)
 	c->dasVariant = 0;
 }
 
-// With the grid known: 64-column tiles where the grid gives at least two
-// tiles per SM and the shared memory fits — 64 x 8 with 2 x 100 or 96 KiB
-// stages (one block per SM; cf2d 1.77 / 1.80 ms), else 64 x 4 with 2 x 48
-// KiB (1.85 ms; 32 x 4 with 2 x 32 KiB: 1.97 ms) — else the creation-time
-// default.
+// With the grid known: 64 x 16 tiles of two points per thread (variant 4,
+// 2 x 100 KiB stages; cf2d FP32 1.645 ms, FP16 1.12 ms) where the grid gives
+// at least 1.5 such tiles per SM; else 64-column tiles of one point per
+// thread where the grid gives at least two tiles per SM — 64 x 8 with 2 x 100
+// or 96 KiB stages (one block per SM; cf2d 1.77 / 1.80 ms), else 64 x 4 with
+// 2 x 48 KiB (1.85 ms; 32 x 4 with 2 x 32 KiB: 1.97 ms) — wherever the
+// shared memory fits; else the creation-time default.
 void choose_grid_das(usgb_ctx* c)
 {
 	choose_default_das(c);
@@ -366,6 +368,14 @@ void choose_grid_das(usgb_ctx* c)
 	if (cudaGetDevice(&dev) != cudaSuccess) return;
 	if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return;
 	const size_t colTiles = (c->ncols + 63) / 64;
+	const size_t tiles16 = colTiles * ((c->nrows + 15) / 16);
+	if (2 * tiles16 >= 3u * static_cast<size_t>(sms) && das_smem_bytes(c, 4, 8u, 102400u, 2u) <= max_smem()) {
+		c->dasVariant = 4;
+		c->tileRows = 8;
+		c->stageBytes = 102400u;
+		c->stages = 2;
+		return;
+	}
 	struct Shape { unsigned rows, cap; };
 	for (const Shape sh : {Shape{8u, 102400u}, Shape{8u, 98304u}, Shape{4u, 49152u}, Shape{4u, 32768u}}) {
 		const size_t tiles = colTiles * ((c->nrows + sh.rows - 1) / sh.rows);

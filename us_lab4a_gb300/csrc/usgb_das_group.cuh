@@ -60,16 +60,32 @@ constexpr unsigned kUnitInterior = 0x100u;
 // 20 warps (5 warpgroups), launched at kLaunchRegs registers a thread; the
 // producer warpgroup (the producer warp and 3 warps that exit) drops to
 // kProducerRegs and the 4 consumer warpgroups rise to kConsumerRegs
-// (setmaxnreg). The split balances exactly:
-// 640 x 96 = 128 x 32 + 512 x 112 = 61440 registers.
+// (setmaxnreg). The split fits the launch allocation:
+// 128 x 64 + 512 x 104 = 61440 = 640 x 96 registers. Measured on the cf2d
+// frame (64 x 16 tiles, 2 x 100 KiB stages): FP32 1.645 ms with 64 / 104,
+// 1.659 ms without a split (17 warps at 96 registers, ~1 KB of spills), 1.82
+// and 1.87 ms with the producer held to 40 and 32 registers (its spills
+// slow the staging); FP16 1.12, 1.15, 1.08, 1.11 ms.
+#ifndef USGB_GROUP_SPLIT
+#define USGB_GROUP_SPLIT 1
+#endif
+#ifndef USGB_PRODUCER_REGS
+#define USGB_PRODUCER_REGS 64
+#endif
+#ifndef USGB_CONSUMER_REGS
+#define USGB_CONSUMER_REGS 104
+#endif
 template<int NCW, int PY> struct GroupShape {
-	static constexpr bool kSplit = PY == 2 && NCW == 16;
+	static constexpr bool kSplit = USGB_GROUP_SPLIT && PY == 2 && NCW == 16;
 	static constexpr int kWarps = kSplit ? NCW + 4 : NCW + 1;
 	static constexpr int kLaunchRegs = 96;
-	static constexpr int kProducerRegs = 32;
-	static constexpr int kConsumerRegs = 112;
-	static_assert(!kSplit || kWarps * 32 * kLaunchRegs == 128 * kProducerRegs + NCW * 32 * kConsumerRegs,
-			"register split must add up to the launch allocation");
+	static constexpr int kProducerRegs = USGB_PRODUCER_REGS;
+	static constexpr int kConsumerRegs = USGB_CONSUMER_REGS;
+	static_assert(kProducerRegs % 8 == 0 && kConsumerRegs % 8 == 0 && kProducerRegs >= 24 && kConsumerRegs <= 256,
+			"setmaxnreg counts are multiples of 8 in [24, 256]");
+	static_assert(kProducerRegs <= kLaunchRegs && kConsumerRegs >= kLaunchRegs, "producer gives, consumers take");
+	static_assert(!kSplit || 128 * kProducerRegs + NCW * 32 * kConsumerRegs <= kWarps * 32 * kLaunchRegs,
+			"register split must fit in the launch allocation");
 	static_assert(!kSplit || kWarps * 32 * kLaunchRegs <= 65536, "launch allocation exceeds the register file");
 };
 
