@@ -294,7 +294,8 @@ void usgb_batch_destroy(usgb_batch* batch);
 const char* usgb_batch_last_error(const usgb_batch* batch);
 int usgb_batch_set_das_config(usgb_batch* batch, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 /* Delay-and-sum kernel of the batch: 2 = receiver-group (default), 3 =
- * receiver-group on 64-column tiles, 1 = staged. */
+ * receiver-group on 64-column tiles, 4 = receiver-group on 64 x 2*tile_rows
+ * tiles with two points per thread, 1 = staged. */
 int usgb_batch_set_das_variant(usgb_batch* batch, int variant);
 int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
 int usgb_batch_synchronize(usgb_batch* batch);

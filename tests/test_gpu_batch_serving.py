@@ -22,15 +22,17 @@ def _alone(frame, cuda, das_config):
         return v.cpu().numpy(), f.cpu().numpy()
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant,rows", [(1, 4), (2, 4), (3, 4), (3, 8), (4, 4), (4, 8)])
 @pytest.mark.parametrize("use_graph", [False, True])
 @pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_batch_equals_frames_alone(cuda, use_graph, storage, variant):
+def test_batch_equals_frames_alone(cuda, use_graph, storage, variant, rows):
+    """Every batched kernel form, including two points per thread (variant 4:
+    64 x 8 tiles on 8 consumer warps, 64 x 16 tiles on 16)."""
     import torch
     from us_lab4a_gb300 import StaEngine, workloads
     from us_lab4a_gb300.batch import Batch, BatchItem
     frames = workloads.mixed(num_frames=7, small=True, storage=storage)
-    cfg = (4, 16384, 2)
+    cfg = (rows, 16384, 2)
     stream = torch.cuda.current_stream()
     batch = Batch(max_frames=16, max_elements=16)
     batch.set_das_config(*cfg, variant=variant)

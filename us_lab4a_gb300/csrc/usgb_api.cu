@@ -901,8 +901,8 @@ const char* usgb_batch_last_error(const usgb_batch* b)
 int usgb_batch_set_das_variant(usgb_batch* b, int variant)
 {
 	return batch_guarded(b, [&] {
-		if (variant < 1 || variant > 3) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1, 2 or 3.");
-		if (variant == 3 && b->tileRows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
+		if (variant < 1 || variant > 4) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1, 2, 3 or 4.");
+		if (variant >= 3 && b->tileRows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 		if (batch_das_smem(b, variant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
 			USGB_FAIL(USGB_ERR_UNSUPPORTED, "the current tile shape does not fit in shared memory for this variant.");
 		}
@@ -918,7 +918,7 @@ int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_
 {
 	return batch_guarded(b, [&] {
 		if (tile_rows != 4 && tile_rows != 8 && tile_rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
-		if (b->dasVariant == 3 && tile_rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
+		if (b->dasVariant >= 3 && tile_rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 		if (stage_bytes < 1024 || stage_bytes % 128 != 0 || stage_bytes > (1u << 20)) {
 			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 		}
@@ -983,11 +983,13 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 			dp.tileRows = b->tileRows;
 			dp.stageBytes = b->stageBytes;
 			dp.stages = b->stages;
+			dp.pointsPerThread = usgb::das_points_per_thread(b->dasVariant);
 			dasF[i].das = dp;
 			dasF[i].tileBegin = tileBegin;
 			dasF[i].tilesX = (c->ncols + dp.tileCols - 1) / dp.tileCols;
 			dasF[i].cf = static_cast<int>(c->prm.coherence);
-			tileBegin += dasF[i].tilesX * ((c->nrows + b->tileRows - 1) / b->tileRows);
+			const unsigned tileH = b->tileRows * dp.pointsPerThread;
+			tileBegin += dasF[i].tilesX * ((c->nrows + tileH - 1) / tileH);
 		}
 		hdr->count = count;
 		hdr->totalSignals = sigBegin;
@@ -1006,6 +1008,7 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 		dc.tileRows = b->tileRows;
 		dc.stageBytes = b->stageBytes;
 		dc.stages = b->stages;
+		dc.pointsPerThread = usgb::das_points_per_thread(b->dasVariant);
 		if (b->dasVariant >= 2) {
 			dc.blocks = 0;  // the launcher fills the SMs (occupancy of the kernel at this shape)
 		} else {

@@ -75,8 +75,12 @@ constexpr unsigned kUnitInterior = 0x100u;
 #ifndef USGB_CONSUMER_REGS
 #define USGB_CONSUMER_REGS 104
 #endif
+// Single-frame kernels only: the split happens once per block, right before
+// the producer and consumer paths part for good (batches loop over tiles, so
+// the two paths would meet again and ptxas would hold both to the producer's
+// count).
 template<int NCW, int PY> struct GroupShape {
-	static constexpr bool kSplit = USGB_GROUP_SPLIT && PY == 2 && NCW == 16;
+	static constexpr bool kSplit = USGB_GROUP_SPLIT && NCW == 16 && PY == 2;
 	static constexpr int kWarps = kSplit ? NCW + 4 : NCW + 1;
 	static constexpr int kLaunchRegs = 96;
 	static constexpr int kProducerRegs = USGB_PRODUCER_REGS;
@@ -91,6 +95,7 @@ template<int NCW, int PY> struct GroupShape {
 
 template<int N> __device__ __forceinline__ void regs_dec() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" :: "n"(N)); }
 template<int N> __device__ __forceinline__ void regs_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" :: "n"(N)); }
+
 
 // One stage: up to kMaxUnits units (consecutive transmitters of one receiver
 // group). Window j of unit u: sample idx of receiver g * kGroup + j sits at
@@ -656,25 +661,31 @@ cudaError_t launch_group_cf(const DasParams& p, int cf, bool analytic, cudaStrea
 	}
 }
 
-template<int S, bool ANALYTIC, int TCOLS, int TROWS>
+template<int S, bool ANALYTIC, int TCOLS, int TROWS, int PY>
 __device__ __forceinline__ bool group_tile_any_cf(const DasParams& p, int cf, const GroupSmem& sm, unsigned bx,
 		unsigned by, int& it)
 {
 	if (!ANALYTIC) {
-		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TCOLS, TROWS>(p, sm, bx, by, it)
-		                      : group_tile<S, CF_NONE, false, TCOLS, TROWS>(p, sm, bx, by, it);
+		return (cf == CF_SCF) ? group_tile<S, CF_SCF, false, TCOLS, TROWS, PY>(p, sm, bx, by, it)
+		                      : group_tile<S, CF_NONE, false, TCOLS, TROWS, PY>(p, sm, bx, by, it);
 	}
 	switch (cf) {
-	case CF_PCF: return group_tile<S, CF_PCF, true, TCOLS, TROWS>(p, sm, bx, by, it);
-	case CF_SCF: return group_tile<S, CF_SCF, true, TCOLS, TROWS>(p, sm, bx, by, it);
-	case CF_MF: return group_tile<S, CF_MF, true, TCOLS, TROWS>(p, sm, bx, by, it);
-	default: return group_tile<S, CF_NONE, true, TCOLS, TROWS>(p, sm, bx, by, it);
+	case CF_PCF: return group_tile<S, CF_PCF, true, TCOLS, TROWS, PY>(p, sm, bx, by, it);
+	case CF_SCF: return group_tile<S, CF_SCF, true, TCOLS, TROWS, PY>(p, sm, bx, by, it);
+	case CF_MF: return group_tile<S, CF_MF, true, TCOLS, TROWS, PY>(p, sm, bx, by, it);
+	default: return group_tile<S, CF_NONE, true, TCOLS, TROWS, PY>(p, sm, bx, by, it);
 	}
 }
 
+// Two points per thread: one block per SM (168 registers on 8 consumer warps).
+template<int NCW, int PY> constexpr int group_batch_blocks()
+{
+	return PY == 2 ? 1 : group_batch_min_blocks<NCW>();
+}
+
 // Many frames: persistent blocks walk the tiles of every frame in the batch.
-template<int S, bool ANALYTIC, int TCOLS, int TROWS>
-__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_batch_min_blocks<TROWS * TCOLS / 32>())
+template<int S, bool ANALYTIC, int TCOLS, int TROWS, int PY>
+__global__ void __launch_bounds__((TROWS * TCOLS / 32 + 1) * 32, group_batch_blocks<TROWS * TCOLS / 32, PY>())
 das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHeader* __restrict__ hdr,
 		unsigned maxTx, unsigned maxRx, unsigned capBytes, unsigned stages)
 {
@@ -698,18 +709,19 @@ das_group_batch_kernel(const BatchDasFrame* __restrict__ frames, const BatchHead
 		if (sAbort) break;
 		const unsigned local = w - frames[f].tileBegin;
 		const unsigned tilesX = frames[f].tilesX;
-		const bool ok = group_tile_any_cf<S, ANALYTIC, TCOLS, TROWS>(sp, frames[f].cf, sm, local % tilesX, local / tilesX, it);
+		const bool ok = group_tile_any_cf<S, ANALYTIC, TCOLS, TROWS, PY>(sp, frames[f].cf, sm, local % tilesX,
+				local / tilesX, it);
 		if (!ok) sAbort = 1;
 	}
 }
 
-template<int S, bool ANALYTIC, int TCOLS, int TROWS>
+template<int S, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
 cudaError_t launch_group_batch_one(const BatchDasFrame* frames, const BatchHeader* hdr, const BatchDasConfig& c,
 		cudaStream_t stream)
 {
 	constexpr int NCW = TROWS * TCOLS / 32;
 	const GroupLayout lay(c.maxTx, c.maxRx, NCW, c.stageBytes, c.stages);
-	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TCOLS, TROWS>;
+	const auto kernel = das_group_batch_kernel<S, ANALYTIC, TCOLS, TROWS, PY>;
 	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(lay.total));
 	if (e != cudaSuccess) return e;
 	unsigned blocks = c.blocks;
@@ -729,6 +741,10 @@ cudaError_t group_batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr
 		cudaStream_t stream)
 {
 	if (c.tileCols == 64) {
+		if (c.pointsPerThread == 2) {
+			return c.tileRows == 4 ? launch_group_batch_one<S, ANALYTIC, 64, 4, 2>(frames, hdr, c, stream)
+			                       : launch_group_batch_one<S, ANALYTIC, 64, 8, 2>(frames, hdr, c, stream);
+		}
 		return c.tileRows == 4 ? launch_group_batch_one<S, ANALYTIC, 64, 4>(frames, hdr, c, stream)
 		                       : launch_group_batch_one<S, ANALYTIC, 64, 8>(frames, hdr, c, stream);
 	}

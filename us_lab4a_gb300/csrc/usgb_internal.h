@@ -157,6 +157,7 @@ struct BatchDasConfig {
 	unsigned maxTx, maxRx;   // layout limits of the shared memory
 	unsigned tileCols, tileRows, stageBytes, stages;
 	unsigned blocks;         // persistent grid size (0: as many blocks as the SMs hold)
+	unsigned pointsPerThread;  // receiver-group kernel: 1, or 2 (64 x 2*tileRows tiles)
 };
 
 cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* hdr, size_t smem, unsigned blocks,
