@@ -43,7 +43,8 @@ class Batch:
 
     # (variant, tile rows, stage bytes, stages) tried by autotune(), most likely first;
     # variant 3 is the receiver-group kernel on 64-column tiles.
-    CANDIDATES = ((4, 8, 102400, 2), (4, 8, 65536, 2), (3, 8, 98304, 2), (3, 8, 65536, 2), (2, 16, 98304, 2),
+    CANDIDATES = ((4, 4, 102400, 2), (4, 4, 65536, 2), (4, 4, 49152, 2), (4, 8, 102400, 2), (4, 8, 65536, 2),
+                  (3, 8, 98304, 2), (3, 8, 65536, 2), (2, 16, 98304, 2),
                   (3, 4, 32768, 2), (3, 4, 49152, 2), (3, 8, 49152, 2), (3, 4, 24576, 3), (2, 8, 24576, 2),
                   (2, 8, 32768, 2), (2, 4, 32768, 2), (2, 4, 24576, 2), (2, 8, 20480, 2),
                   (2, 4, 16384, 2), (1, 8, 24576, 3), (1, 4, 32768, 2), (1, 4, 16384, 2))
