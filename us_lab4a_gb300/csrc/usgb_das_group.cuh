@@ -480,8 +480,12 @@ __device__ bool group_consume(const DasParams& p, const GroupSmem& sm, int& it, 
 // One tile (bx, by) of one frame: TCOLS columns x TROWS * PY rows, thread
 // (warp w, lane l) on column bx * TCOLS + (w % CW) * 32 + l and rows
 // by * TROWS * PY + (w / CW) * PY + k, k < PY; `it` is the block's running
-// stage counter.
-template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
+// stage counter. SPLIT: the block is the single-frame kernel's
+// GroupShape<NCW, PY>::kWarps warps and this is its only tile, so the
+// register split may happen here (a batch block walks many tiles with NCW + 1
+// warps and never splits: setmaxnreg needs whole warpgroups, and a repeated
+// .inc would wait for registers no warp gives back).
+template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1, bool SPLIT = false>
 __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx, unsigned by, int& it)
 {
 	using SP = Sample<ANALYTIC, S>;
@@ -565,7 +569,8 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	const bool q = p.delayMode == 2 || (p.delayMode == 0 && topTx + topRx > kDeepDelaySamples);
 	const Fixed fx = fixed_format(fmaxf(fmaxf(topTx, topRx), fabsf(p.signalOffset)));
 	using Shape = GroupShape<NCW, PY>;
-	if constexpr (Shape::kSplit) {
+	static_assert(!SPLIT || Shape::kSplit, "only the split block shape splits its registers");
+	if constexpr (SPLIT) {
 		// Warpgroup-uniform branches (warps 0-15: consumers; 16-19: producer group).
 		if (producer) {
 			regs_dec<Shape::kProducerRegs>();
@@ -602,7 +607,7 @@ das_group_kernel(DasParams p)
 	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, NCW, p.stages, p.stageBytes);
 	init_group_barriers(sm, NCW);
 	int it = 0;
-	group_tile<S, CF, ANALYTIC, TCOLS, TROWS, PY>(p, sm, blockIdx.x, blockIdx.y, it);
+	group_tile<S, CF, ANALYTIC, TCOLS, TROWS, PY, GroupShape<NCW, PY>::kSplit>(p, sm, blockIdx.x, blockIdx.y, it);
 }
 
 template<int S, int CF, bool ANALYTIC, int TCOLS, int TROWS, int PY = 1>
