@@ -4,6 +4,7 @@ processors' outputs (golden fixtures) and the FP32 CPU oracle.
 Tolerances: value within 1e-5 of the image maximum (before log compression);
 coherence factor within 1e-4 absolute (PCF within 1e-3: its phases come from
 atan2 of sums accumulated in a different order)."""
+import math
 import os
 
 import numpy as np
@@ -294,7 +295,8 @@ def test_staged_kernel_equals_plain_kernel(cuda, name, frame, rows, stage_bytes)
 
 def test_grid_selects_tile_width(cuda):
     """Without an explicit choice, a grid of at least 1.5 tiles of 64 x 16 per
-    SM selects the two-points-per-thread kernel on 64 x 16 tiles, one of at
+    SM selects the two-points-per-thread kernel on 64 x 2R tiles (512 rows on
+    152 SMs: R = 7, 296 tiles in two waves), one of at
     least two 64 x 8 tiles per SM the receiver-group kernel on 64-column
     tiles, a small grid keeps 32-column tiles, and a variant set explicitly
     survives a new grid."""
@@ -305,7 +307,10 @@ def test_grid_selects_tile_width(cuda):
         eng.set_grid_device(torch.zeros((32, 32, 3), device=cuda))
         assert eng.das_config()["variant"] == 2
         eng.set_grid_device(torch.zeros((512, 512, 3), device=cuda))
-        assert eng.das_config() == {"variant": 4, "tile_rows": 8, "stage_bytes": 102400, "stages": 2}
+        sms = torch.cuda.get_device_properties(cuda).multi_processor_count
+        cost = {r: math.ceil(8 * math.ceil(512 / (2 * r)) / sms) * (r + 0.6) for r in (8, 7, 6, 5)}
+        best = min(cost, key=lambda r: (cost[r], -r))
+        assert eng.das_config() == {"variant": 4, "tile_rows": best, "stage_bytes": 102400, "stages": 2}
         eng.set_grid_device(torch.zeros((256, 512, 3), device=cuda))
         cfg = eng.das_config()
         assert cfg["variant"] == 3 and (cfg["tile_rows"], cfg["stage_bytes"]) in ((8, 102400), (8, 98304), (4, 49152),
@@ -316,10 +321,14 @@ def test_grid_selects_tile_width(cuda):
 
 
 @pytest.mark.parametrize("cfg", [(3, 8, 102400, 2), (3, 8, 98304, 2), (3, 4, 65536, 2), (2, 16, 98304, 2),
-                                 (4, 8, 102400, 2), (4, 8, 65536, 2), (4, 4, 102400, 2), (4, 8, 16384, 3)])
+                                 (4, 8, 102400, 2), (4, 8, 65536, 2), (4, 4, 102400, 2), (4, 8, 16384, 3),
+                                 (4, 7, 102400, 2), (4, 5, 102400, 2), (4, 3, 65536, 2), (3, 6, 98304, 2),
+                                 (3, 1, 32768, 2)])
 def test_large_stages_equal_plain_kernel(cuda, cfg):
     """Stages of 64-96 KiB (several units each, one block per SM) give the
-    plain kernel's images bit for bit (PCF, partial tiles, FP32 and FP16)."""
+    plain kernel's images bit for bit (PCF, partial tiles, FP32 and FP16),
+    also with tiles of fewer thread rows than the block holds (the other
+    consumer warps idle)."""
     import torch
     from us_lab4a_gb300 import StaEngine, workloads
     for frame in (workloads.cf2d(small=True), workloads.with_storage(workloads.cf2d(small=True, coherence="mf"), "f16")):

@@ -65,6 +65,8 @@ struct usgb_ctx {
 	float* d_apod = nullptr;
 	float* d_polyTaps = nullptr;
 	std::vector<float> polyHost;   // the same taps, for the launch parameters
+	float* d_dcCoef = nullptr;     // DC weights of the input samples (usgb::host::dc_coefficients)
+	bool prepStream = false;       // the persistent preparation kernel fits in shared memory
 	float2* d_tw = nullptr;
 	float4* d_hilb = nullptr;
 	float2* d_stw = nullptr;
@@ -99,7 +101,7 @@ struct usgb_ctx {
 
 	~usgb_ctx()
 	{
-		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_tw, d_hilb, d_stw, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
+		void* dev[] = {d_txXY, d_rxXY, d_apod, d_polyTaps, d_dcCoef, d_tw, d_hilb, d_stw, d_rf, d_sig, d_grid, d_value, d_factor, d_err};
 		for (void* p : dev) if (p) cudaFree(p);
 		if (h_rf) cudaFreeHost(h_rf);
 		if (h_out) cudaFreeHost(h_out);
@@ -150,6 +152,9 @@ void build_tables(usgb_ctx* c)
 	c->polyHost = poly.poly;
 	USGB_CUDA(cudaMalloc(&c->d_polyTaps, poly.poly.size() * sizeof(float)));
 	USGB_CUDA(cudaMemcpy(c->d_polyTaps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice));
+	const std::vector<float> dc = usgb::host::dc_coefficients(poly, c->U, c->prm.num_samples, c->deadZone);
+	USGB_CUDA(cudaMalloc(&c->d_dcCoef, dc.size() * sizeof(float)));
+	USGB_CUDA(cudaMemcpy(c->d_dcCoef, dc.data(), dc.size() * sizeof(float), cudaMemcpyHostToDevice));
 
 	if (!c->analytic) return;
 	usgb::host::FFTTables& t = c->fft;
@@ -239,6 +244,18 @@ usgb::PrepParams prep_params(const usgb_ctx* c, const float* d_rf, void* d_sig)
 	usgb::host::set_param_taps(pp, c->polyHost);
 	pp.deadZone = c->deadZone;
 	pp.outScale = c->scale;
+	pp.errWord = c->d_err;
+	if (c->prepStream) {
+		pp.dcCoef = c->d_dcCoef;
+		// Bulk copies of the RF rows need device memory and 16-byte rows (a
+		// host pointer read through the host's page tables takes plain loads).
+		cudaPointerAttributes at{};
+		if (d_rf && pp.ns % 4 == 0 && reinterpret_cast<uintptr_t>(d_rf) % 16 == 0 &&
+				cudaPointerGetAttributes(&at, d_rf) == cudaSuccess && at.type == cudaMemoryTypeDevice) {
+			pp.rfBulk = 1;
+		}
+		cudaGetLastError();   // a failed attribute query leaves no error behind
+	}
 	if (c->analytic) {
 		usgb::host::set_fft_params(pp, c->fft);
 		pp.tw = c->d_tw;
@@ -370,8 +387,23 @@ void choose_grid_das(usgb_ctx* c)
 	const size_t colTiles = (c->ncols + 63) / 64;
 	const size_t tiles16 = colTiles * ((c->nrows + 15) / 16);
 	if (2 * tiles16 >= 3u * static_cast<size_t>(sms) && das_smem_bytes(c, 4, 8u, 102400u, 2u) <= max_smem()) {
+		// 64 x 2R tiles, R in [5, 8] thread rows: the fewest waves of tiles
+		// (one block per SM) times the rows of a tile, plus about 0.6 row of
+		// set-up per tile (cf2d, 512 rows: R = 7, 296 tiles in 2 waves against
+		// 256 tiles of R = 8 in 1.7 waves, which take 2 full waves).
+		unsigned bestR = 8;
+		double bestCost = 1e30;
+		for (unsigned R = 8; R >= 5; --R) {
+			const size_t tiles = colTiles * ((c->nrows + 2 * R - 1) / (2 * R));
+			const double waves = std::ceil(static_cast<double>(tiles) / sms);
+			const double cost = waves * (R + 0.6);
+			if (cost < bestCost - 1e-9) {
+				bestCost = cost;
+				bestR = R;
+			}
+		}
 		c->dasVariant = 4;
-		c->tileRows = 8;
+		c->tileRows = bestR;
 		c->stageBytes = 102400u;
 		c->stages = 2;
 		return;
@@ -403,6 +435,10 @@ void check_prep_fits(usgb_ctx* c)
 		USGB_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation: needs " << need
 				<< " bytes of shared memory, the device offers " << maxSmem << " (signal length " << c->L << ").");
 	}
+	// The persistent kernel holds a second RF row and the DC weights as well.
+	c->prepStream = true;
+	const usgb::PrepParams sp = prep_params(c, nullptr, nullptr);
+	c->prepStream = usgb::prep_uses_stream(sp) && usgb::prep_stream_smem_bytes(sp, c->analytic) <= static_cast<size_t>(maxSmem);
 	const size_t dasSmem = static_cast<size_t>(c->prm.num_tx) * 128 * sizeof(float);
 	if (dasSmem > static_cast<size_t>(maxSmem)) {
 		USGB_FAIL(USGB_ERR_UNSUPPORTED, "Too many transmit elements for the delay table: " << c->prm.num_tx << '.');
@@ -681,8 +717,11 @@ int usgb_set_das_variant(usgb_ctx* c, int variant, uint32_t tile_rows, uint32_t 
 		const unsigned cap = stage_bytes ? stage_bytes : c->stageBytes;
 		const unsigned nst = stages ? stages : c->stages;
 		if (variant != 0) {
-			if (rows != 4 && rows != 8 && rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
-			if (variant >= 3 && rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
+			if (variant >= 3) {
+				if (rows < 1 || rows > 8) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 1 to 8 rows.");
+			} else if (rows != 4 && rows != 8 && rows != 16) {
+				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+			}
 			if (cap < 1024 || cap % 128 != 0 || cap > (1u << 20)) {
 				USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");
 			}
@@ -732,11 +771,12 @@ int usgb_autotune_das(usgb_ctx* c, const void* d_signals, float* d_value, float*
 		struct Cand { int variant; unsigned rows, cap, stages; };
 		std::vector<Cand> cands;
 		for (int variant : {1, 2, 3, 4})
-			for (unsigned rows : {4u, 8u, 16u})
+			for (unsigned rows : {4u, 5u, 6u, 7u, 8u, 16u})
 				for (unsigned cap : {8192u, 12288u, 16384u, 20480u, 24576u, 32768u, 49152u, 65536u, 98304u, 102400u,
 						110592u})
 					for (unsigned nst : {2u, 3u, 4u})
 						if ((variant >= 2 || cap % 8192u == 0) && !(variant >= 3 && rows == 16)
+								&& (variant >= 3 || rows == 4 || rows == 8 || rows == 16)
 								&& das_smem_bytes(c, variant, rows, cap, nst) <= max_smem())
 							cands.push_back({variant, rows, cap, nst});
 		cands.push_back({0, c->tileRows, c->stageBytes, c->stages});

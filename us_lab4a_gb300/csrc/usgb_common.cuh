@@ -134,6 +134,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 	}
 }
 
+// Orders this thread's earlier generic-proxy accesses of shared memory before
+// the async-proxy (bulk copy) accesses it issues next.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Bulk global -> shared copy completing on `bar` (both addresses 16-byte
 // aligned, bytes a multiple of 16).
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)

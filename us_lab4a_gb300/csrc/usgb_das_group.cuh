@@ -490,12 +490,19 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 {
 	using SP = Sample<ANALYTIC, S>;
 	constexpr int CW = TCOLS / 32;      // warps per tile row
-	constexpr int NCW = TROWS * CW;     // consumer warps
+	constexpr int NCW = TROWS * CW;     // consumer warps of the block
+	// Thread rows with grid points: p.tileRows (at most TROWS; a single-frame
+	// launch may use shorter tiles so that the tiles fill whole waves). The
+	// consumer warps beyond them take part in the set-up barriers and the
+	// register split, then leave.
+	const int rowsA = min(static_cast<int>(p.tileRows), TROWS);
+	const int ncwa = rowsA * CW;
 	const int warp = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
 	const bool producer = warp >= NCW;   // the producer warp (NCW), and the exiting warps of a split block
+	const bool idle = !producer && warp >= ncwa;
 	const unsigned col = bx * TCOLS + (warp % CW) * 32 + lane;
-	const unsigned row0 = by * (TROWS * PY) + (warp / CW) * PY;
+	const unsigned row0 = by * (rowsA * PY) + (warp / CW) * PY;
 	const unsigned nE = p.numTx + p.numRx;
 
 	// Threads beyond the grid's edge take the nearest grid point of the tile.
@@ -505,10 +512,10 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 #pragma unroll
 	for (int k = 0; k < PY; ++k) {
 		const unsigned row = row0 + k;
-		active[k] = !producer && col < p.ncols && row < p.nrows;
+		active[k] = !producer && !idle && col < p.ncols && row < p.nrows;
 		pix[k] = col * p.nrows + row;
 		px[k] = py[k] = pz[k] = 0.f;
-		if (!producer) {
+		if (!producer && !idle) {
 			const unsigned q = min(col, p.ncols - 1) * p.nrows + min(row, p.nrows - 1);
 			px[k] = p.grid[3 * q];
 			py[k] = p.grid[3 * q + 1];
@@ -526,7 +533,7 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 		sm.txinfo[t] = make_float2(__ldg(&p.txXY[2 * t]), __ldg(&p.txXY[2 * t + 1]));
 	}
 	// Per-warp min/max of every element's FP32 delay over the tile.
-	if (!producer) {
+	if (!producer && !idle) {
 		for (unsigned e = 0; e < nE; ++e) {
 			const bool isTx = e < p.numTx;
 			const unsigned r = e - p.numTx;
@@ -554,7 +561,7 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 	float topT = 0.f, topR = 0.f;
 	for (unsigned e = threadIdx.x; e < nE; e += blockDim.x) {
 		float mn = sm.partMin[e], mx = sm.partMax[e];
-		for (int w = 1; w < NCW; ++w) {
+		for (int w = 1; w < ncwa; ++w) {
 			mn = fminf(mn, sm.partMin[w * sm.maxE + e]);
 			mx = fmaxf(mx, sm.partMax[w * sm.maxE + e]);
 		}
@@ -580,6 +587,7 @@ __device__ bool group_tile(const DasParams& p, const GroupSmem& sm, unsigned bx,
 		}
 	}
 	if (producer) return group_produce<SP>(p, sm, it, q ? 2.0f : 0.0f);
+	if (idle) return true;
 	return q ? group_consume<SP, CF, true, PY>(p, sm, it, px, py, pz, active, pix, fx)
 	         : group_consume<SP, CF, false, PY>(p, sm, it, px, py, pz, active, pix, fx);
 }
@@ -605,7 +613,7 @@ das_group_kernel(DasParams p)
 	extern __shared__ __align__(128) unsigned char smem[];
 	const GroupLayout lay(p.numTx, p.numRx, NCW, p.stageBytes, p.stages);
 	const GroupSmem sm = carve_group(smem, lay, p.numTx, p.numRx, NCW, p.stages, p.stageBytes);
-	init_group_barriers(sm, NCW);
+	init_group_barriers(sm, min(static_cast<int>(p.tileRows), TROWS) * (TCOLS / 32));   // consumer warps with grid points
 	int it = 0;
 	group_tile<S, CF, ANALYTIC, TCOLS, TROWS, PY, GroupShape<NCW, PY>::kSplit>(p, sm, blockIdx.x, blockIdx.y, it);
 }
@@ -626,23 +634,24 @@ cudaError_t launch_group_one(const DasParams& p, cudaStream_t stream)
 		if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
 		if (fa.numRegs != Shape::kLaunchRegs) return cudaErrorInvalidConfiguration;
 	}
-	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + TROWS * PY - 1) / (TROWS * PY));
+	const unsigned tileH = min(p.tileRows, static_cast<unsigned>(TROWS)) * PY;
+	const dim3 grid((p.ncols + TCOLS - 1) / TCOLS, (p.nrows + tileH - 1) / tileH);
 	kernel<<<grid, Shape::kWarps * 32, lay.total, stream>>>(p);
 	return cudaGetLastError();
 }
 
-// Tile shapes (columns x rows): 32 x 4, 32 x 8, 32 x 16, 64 x 4, 64 x 8; with
-// two points per thread (p.pointsPerThread == 2, 64-column tiles): 64 x 8
-// and 64 x 16.
+// Tile shapes (columns x thread rows): 32 x 4, 32 x 8, 32 x 16, and 64 x 1-8
+// (blocks of 4 or 8 thread rows); a thread row is one grid row, or two with
+// two points per thread (p.pointsPerThread == 2: 64 x 2-16 grid rows).
 template<int S, int CF, bool ANALYTIC>
 cudaError_t launch_group_rows(const DasParams& p, cudaStream_t stream)
 {
-	if (p.tileCols == 64) {
+	if (p.tileCols == 64) {   // 1-8 thread rows: blocks of 4 or 8, the rest of the rows idle
 		if (p.pointsPerThread == 2) {
-			return p.tileRows == 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4, 2>(p, stream)
+			return p.tileRows <= 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4, 2>(p, stream)
 			                       : launch_group_one<S, CF, ANALYTIC, 64, 8, 2>(p, stream);
 		}
-		return p.tileRows == 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4>(p, stream)
+		return p.tileRows <= 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4>(p, stream)
 		                       : launch_group_one<S, CF, ANALYTIC, 64, 8>(p, stream);
 	}
 	switch (p.tileRows) {
@@ -776,10 +785,13 @@ cudaError_t launch_das_group_batch_storage(const BatchDasFrame* frames, const Ba
 	return analytic ? group_batch_rows<S, true>(frames, hdr, c, stream) : group_batch_rows<S, false>(frames, hdr, c, stream);
 }
 
+// Shared memory of a block; 64-column tiles of 1-8 thread rows run in blocks
+// of 4 or 8 (the kernel's compile-time rows).
 inline size_t group_layout_bytes(unsigned numTx, unsigned numRx, unsigned tileCols, unsigned tileRows, unsigned capBytes,
 		unsigned stages)
 {
-	return GroupLayout(numTx, numRx, tileRows * (tileCols / 32), capBytes, stages).total;
+	const unsigned blockRows = tileCols == 64 ? (tileRows <= 4 ? 4u : 8u) : tileRows;
+	return GroupLayout(numTx, numRx, blockRows * (tileCols / 32), capBytes, stages).total;
 }
 
 }  // namespace usgb

@@ -56,6 +56,16 @@ struct PrepParams {
 	const float2* stw;
 	unsigned stwCount;
 	unsigned stwOffset[kMaxFFTStages];
+	// DC removal inside the FIR pass (single-frame launches of the
+	// specialised FIR shapes): dcCoef[b] is the sum of the FIR taps through
+	// which input sample b reaches an output in [deadZone, L), so the mean of
+	// [deadZone, L) is sum_b rf[b] dcCoef[b] / (L - deadZone), known before
+	// the FIR runs. Null: the mean is taken from the FIR outputs.
+	const float* dcCoef;
+	// The rows of `rf` are device memory, 16-byte aligned, ns a multiple of 4:
+	// they may be fetched with bulk copies.
+	unsigned rfBulk;
+	unsigned* errWord;           // device status word of the bounded waits, or null
 };
 
 size_t prep_smem_bytes(const PrepParams& p, bool analytic);
@@ -66,6 +76,10 @@ int prep_threads(size_t smem);
 // p.ns = p.L samples (U = 1, one FIR tap of 1), float output, p.outStride apart.
 cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream);
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream);
+// Whether launch_prep runs the persistent single-frame kernel (DC weights
+// given, specialised FIR shape), and the shared memory a block of it needs.
+bool prep_uses_stream(const PrepParams& p);
+size_t prep_stream_smem_bytes(const PrepParams& p, bool analytic);
 
 // One launch of the delay-and-sum kernel over the grid points of one frame.
 struct DasParams {

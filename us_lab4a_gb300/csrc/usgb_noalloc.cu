@@ -31,6 +31,7 @@
 // device current, on the first call on that device.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <sstream>
@@ -90,7 +91,7 @@ void* scratch_address()
 
 // Byte layout of one call inside the scratch array.
 struct Layout {
-	size_t err, taps, tw, hilb, stw, tx, rx, apod, sig, total;
+	size_t err, taps, dc, tw, hilb, stw, tx, rx, apod, sig, total;
 };
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -122,6 +123,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 		if (!usgb::host::make_fft_tables(L, fft)) NA_FAIL(USGB_ERR_INVALID_STATE, "FFT size not supported");
 		usgb::host::set_fft_params(pp, fft);
 	}
+	const std::vector<float> dc = usgb::host::dc_coefficients(poly, U, p->num_samples, k.deadZone);
 	std::vector<float> apod(p->num_rx, 1.0f);
 	if (analytic && p->rx_apod) apod.assign(p->rx_apod, p->rx_apod + p->num_rx);
 
@@ -132,6 +134,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	size_t off = 0;
 	lay.err = off; off = align256(off + sizeof(unsigned));
 	lay.taps = off; off = align256(off + poly.poly.size() * sizeof(float));
+	lay.dc = off; off = align256(off + dc.size() * sizeof(float));
 	lay.tw = off; off = align256(off + fft.tw.size() * sizeof(float2));
 	lay.hilb = off; off = align256(off + fft.hilb.size() * sizeof(float4));
 	lay.stw = off; off = align256(off + fft.stageTw.size() * sizeof(float2));
@@ -151,6 +154,7 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	unsigned* status = d_status ? d_status : reinterpret_cast<unsigned*>(base + lay.err);
 	NA_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), stream));
 	NA_CUDA(cudaMemcpyAsync(base + lay.taps, poly.poly.data(), poly.poly.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+	NA_CUDA(cudaMemcpyAsync(base + lay.dc, dc.data(), dc.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
 	if (analytic) {
 		NA_CUDA(cudaMemcpyAsync(base + lay.tw, fft.tw.data(), fft.tw.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
 		NA_CUDA(cudaMemcpyAsync(base + lay.hilb, fft.hilb.data(), fft.hilb.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
@@ -187,6 +191,21 @@ int run(const usgb_sta_params* p, const float* d_rf, const float* d_grid, uint32
 	if (pp.stw && usgb::prep_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) pp.stw = nullptr;
 	if (usgb::prep_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) {
 		NA_FAIL(USGB_ERR_UNSUPPORTED, "A-scan too long for on-chip preparation (signal length " << L << ").");
+	}
+	// The preparation usgb_create's context chooses: the persistent kernel
+	// with the DC removed in the FIR pass where it fits, so both entry points
+	// form the same signals.
+	pp.dcCoef = reinterpret_cast<const float*>(base + lay.dc);
+	pp.errWord = status;
+	if (!usgb::prep_uses_stream(pp) || usgb::prep_stream_smem_bytes(pp, analytic) > static_cast<size_t>(maxSmem)) {
+		pp.dcCoef = nullptr;
+	} else {
+		cudaPointerAttributes at{};
+		if (pp.ns % 4 == 0 && reinterpret_cast<uintptr_t>(d_rf) % 16 == 0 &&
+				cudaPointerGetAttributes(&at, d_rf) == cudaSuccess && at.type == cudaMemoryTypeDevice) {
+			pp.rfBulk = 1;
+		}
+		cudaGetLastError();
 	}
 	NA_CUDA(usgb::launch_prep(pp, static_cast<int>(p->storage), analytic, stream));
 

@@ -33,6 +33,8 @@
 //   lo[m % 128]), later stages from per-stage tables indexed by j, so that
 //   consecutive lanes read consecutive words. Stage indices use
 //   multiply-shift division by host-computed constants.
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include "usgb_common.cuh"
@@ -624,6 +626,153 @@ __device__ __forceinline__ void hilbert_pair(float2* data, unsigned i, const flo
 	data[q2] = make_float2(-cs.y * B.y - cs.x * A.x, cs.y * B.x + cs.x * A.y);
 }
 
+// y[n] - mean for the U outputs of input position b: into xs (analytic path,
+// the FFT buffer; store_real_parts writes them to the output afterwards with
+// coalesced stores) or into the real output.
+template<int S, int U, bool ANALYTIC>
+__device__ __forceinline__ void fir_store_dc_free(const PrepParams& p, unsigned b, const float* o, float mean,
+		float* xs, void* outRow)
+{
+	const float sc = p.outScale;
+	float d[U];
+#pragma unroll
+	for (int r = 0; r < U; ++r) d[r] = o[r] - mean;
+	if constexpr (ANALYTIC) {
+		if constexpr (U % 4 == 0) {
+#pragma unroll
+			for (int r = 0; r < U; r += 4) *reinterpret_cast<float4*>(xs + b * U + r) = make_float4(d[r], d[r + 1], d[r + 2], d[r + 3]);
+		} else {
+#pragma unroll
+			for (int r = 0; r < U; ++r) xs[b * U + r] = d[r];
+		}
+	} else {
+		using RT = typename Real<S>::T;
+		RT* out = reinterpret_cast<RT*>(outRow) + static_cast<size_t>(b) * U;
+		if constexpr (S == STORE_F32 && U % 4 == 0) {
+#pragma unroll
+			for (int r = 0; r < U; r += 4) {
+				*reinterpret_cast<float4*>(out + r) = make_float4(d[r] * sc, d[r + 1] * sc, d[r + 2] * sc, d[r + 3] * sc);
+			}
+		} else {
+#pragma unroll
+			for (int r = 0; r < U; ++r) out[r] = Real<S>::pack(d[r] * sc);
+		}
+	}
+}
+
+// The real parts of the analytic output, (x[n] * scale, 0) for n < L, from the
+// DC-free signal in xs: four samples a thread and step (one 16-byte shared
+// load, 16-byte global stores), consecutive threads on consecutive samples.
+// Every 32-byte sector is written whole (the imaginary halves merge into the
+// lines in L2 later).
+template<int S>
+__device__ void store_real_parts(const PrepParams& p, const float* xs, void* outRow)
+{
+	using CT = typename Complex<S>::T;
+	CT* out = reinterpret_cast<CT*>(outRow);
+	const float sc = p.outScale;
+	const unsigned L4 = p.L & ~3u;
+	for (unsigned n = 4 * threadIdx.x; n < L4; n += 4 * blockDim.x) {
+		const float4 v = *reinterpret_cast<const float4*>(xs + n);
+		if constexpr (S == STORE_F32) {
+			float4* o = reinterpret_cast<float4*>(out + n);
+			o[0] = make_float4(v.x * sc, 0.0f, v.y * sc, 0.0f);
+			o[1] = make_float4(v.z * sc, 0.0f, v.w * sc, 0.0f);
+		} else {
+			const CT c0 = Complex<S>::pack(v.x * sc, 0.0f), c1 = Complex<S>::pack(v.y * sc, 0.0f);
+			const CT c2 = Complex<S>::pack(v.z * sc, 0.0f), c3 = Complex<S>::pack(v.w * sc, 0.0f);
+			uint4 w;
+			w.x = *reinterpret_cast<const unsigned*>(&c0);
+			w.y = *reinterpret_cast<const unsigned*>(&c1);
+			w.z = *reinterpret_cast<const unsigned*>(&c2);
+			w.w = *reinterpret_cast<const unsigned*>(&c3);
+			*reinterpret_cast<uint4*>(out + n) = w;
+		}
+	}
+	for (unsigned n = L4 + threadIdx.x; n < p.L; n += blockDim.x) out[n] = Complex<S>::pack(xs[n] * sc, 0.0f);
+}
+
+// The mean of [deadZone, L) from the inputs: sum_i x[i] dc[i] / count, in
+// an order that does not depend on the block size (128 partial sums over
+// i = j mod 128, folded in a fixed tree), so that every kernel preparing an
+// A-scan takes the same mean. Contains the block's barriers.
+__device__ float dc_mean(const float* x, const float* dc, unsigned n, float* red, float count)
+{
+	float v = 0.f;
+	if (threadIdx.x < 128) {
+		for (unsigned i = threadIdx.x; i < n; i += 128) v = fmaf(x[i], dc[i], v);
+	}
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	const unsigned warp = threadIdx.x >> 5;
+	if ((threadIdx.x & 31) == 0 && warp < 4) red[warp] = v;
+	__syncthreads();
+	const float r = ((red[0] + red[1]) + (red[2] + red[3])) / count;
+	__syncthreads();
+	return r;
+}
+
+// FIR pass with the DC removed (the mean known beforehand): the DC-free
+// signal into xs and, analytic path, (real, 0) into the output row; real
+// path, the output row itself.
+template<int S, int NT, int U, bool PT, bool ANALYTIC>
+__device__ __forceinline__ void fir_dc_free_pass(const PrepParams& p, const float* rfs, const float* taps, float mean,
+		float* xs, void* outRow)
+{
+	if constexpr (NT > 1) {
+		for (unsigned b = threadIdx.x; b < p.ns; b += 2 * blockDim.x) {
+			const unsigned b1 = b + blockDim.x;
+			const bool two = b1 < p.ns;
+			float o0[U], o1[U];
+			fir_outputs2<NT, U, PT>(rfs, taps, b, two ? b1 : b, o0, o1);
+			fir_store_dc_free<S, U, ANALYTIC>(p, b, o0, mean, xs, outRow);
+			if (two) fir_store_dc_free<S, U, ANALYTIC>(p, b1, o1, mean, xs, outRow);
+		}
+	} else {
+		for (unsigned b = threadIdx.x; b < p.ns; b += blockDim.x) {
+			float o[U];
+			fir_outputs<NT, U, PT>(rfs, taps, b, o);
+			fir_store_dc_free<S, U, ANALYTIC>(p, b, o, mean, xs, outRow);
+		}
+	}
+}
+
+// Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
+// W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0, visited in
+// digit-reversed position order (both members of neighbouring lanes' pairs
+// sit at neighbouring positions). A thread loads the table entries of
+// kHilbertBatch pairs before it works on them, so their L2 latencies overlap
+// (the pairs are disjoint).
+__device__ __forceinline__ void hilbert_pass(const PrepParams& p, float2* data)
+{
+	for (unsigned i0 = threadIdx.x; i0 < p.hilbCount; i0 += kHilbertBatch * blockDim.x) {
+		float4 h[kHilbertBatch];
+#pragma unroll
+		for (int u = 0; u < kHilbertBatch; ++u) {
+			const unsigned i = i0 + u * blockDim.x;
+			h[u] = (i < p.hilbCount) ? __ldg(&p.hilb[i]) : make_float4(0.f, 0.f, __uint_as_float(kHilbertSkip), 0.f);
+		}
+#pragma unroll
+		for (int u = 0; u < kHilbertBatch; ++u) hilbert_pair(data, i0 + u * blockDim.x, h[u]);
+	}
+}
+
+// Steps 3-6 of the analytic path after the DC-free signal is in the buffer:
+// forward FFT (digit-reversed output), Hilbert multiplier and real-FFT
+// split, inverse FFT (natural-order output: y[n] * M at float index n), the
+// imaginary parts y[n] / M stored (the real parts were stored with the DC
+// removal), and a barrier (shared memory is reused by the next A-scan).
+template<int S>
+__device__ void prep_analytic_tail(const PrepParams& p, unsigned a, float2* data, const float* xs, const float2* twLo,
+		const float2* twHi, const float2* stw)
+{
+	fft_run<false>(data, p, twLo, twHi, stw);
+	hilbert_pass(p, data);
+	__syncthreads();
+	fft_run<true>(data, p, twLo, twHi, stw);
+	store_imag_pass<S>(p, xs, a);
+	__syncthreads();
+}
+
 // Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
 // the generic FIR loop. ENV: the envelope of the input itself instead
 // (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
@@ -645,6 +794,21 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 
 	// 1. Upsampled signal into the packed buffer, zero past L.
 	for (unsigned n = L + threadIdx.x; n < 2 * p.M; n += blockDim.x) xs[n] = 0.f;
+	if constexpr (!ENV && NT > 0) {
+		if (p.dcCoef) {
+			// The mean from the inputs (PrepParams::dcCoef), the DC removed
+			// inside the FIR pass, as the single-frame stream kernel does.
+			const unsigned K = (NT - 1) / 2;
+			const float m = dc_mean(rfs + K, p.dcCoef, p.ns, sm + lay.red, static_cast<float>(L - p.deadZone));
+			void* outRow = reinterpret_cast<typename Complex<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride;
+			fir_dc_free_pass<S, NT, U, PT, true>(p, rfs, taps, m, xs, outRow);
+			__syncthreads();
+			store_real_parts<S>(p, xs, outRow);
+			__syncthreads();
+			prep_analytic_tail<S>(p, a, data, xs, twLo, twHi, stw);
+			return;
+		}
+	}
 	const float part = fir_pass<NT, U, PT>(p, rfs, taps, xs);
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
 	//    (block_sum's barriers also order the writes above).
@@ -668,32 +832,19 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 	}
 	__syncthreads();
 
+	if constexpr (!ENV) {
+		prep_analytic_tail<S>(p, a, data, xs, twLo, twHi, stw);
+		return;
+	}
 	// 3. Forward FFT (digit-reversed output).
 	fft_run<false>(data, p, twLo, twHi, stw);
-
-	// 4. Hilbert multiplier and real-FFT split, on the pairs (k, M-k):
-	//    W[k] = i sin(pi k/M) Z[k] + cos(pi k/M) conj(Z[M-k]), W[0] = 0,
-	//    visited in digit-reversed position order (both members of
-	//    neighbouring lanes' pairs sit at neighbouring positions). A thread
-	//    loads the table entries of kHilbertBatch pairs before it works on
-	//    them, so their L2 latencies overlap (the pairs are disjoint).
-	for (unsigned i0 = threadIdx.x; i0 < p.hilbCount; i0 += kHilbertBatch * blockDim.x) {
-		float4 h[kHilbertBatch];
-#pragma unroll
-		for (int u = 0; u < kHilbertBatch; ++u) {
-			const unsigned i = i0 + u * blockDim.x;
-			h[u] = (i < p.hilbCount) ? __ldg(&p.hilb[i]) : make_float4(0.f, 0.f, __uint_as_float(kHilbertSkip), 0.f);
-		}
-#pragma unroll
-		for (int u = 0; u < kHilbertBatch; ++u) hilbert_pair(data, i0 + u * blockDim.x, h[u]);
-	}
+	// 4. Hilbert multiplier and real-FFT split (hilbert_pass).
+	hilbert_pass(p, data);
 	__syncthreads();
-
 	// 5. Inverse FFT (natural-order output: y[n] * M at float index n).
 	fft_run<true>(data, p, twLo, twHi, stw);
-
-	// 6. Store y[n] / M for n < L (the real parts were stored in step 2).
-	if constexpr (ENV) {
+	// 6. |x[n] + i y[n]|.
+	{
 		// |x[n] + i y[n]| (the input itself is the real part).
 		const float invM = 1.0f / static_cast<float>(p.M);
 		float* out = reinterpret_cast<float*>(p.out) + static_cast<size_t>(a) * p.outStride;
@@ -702,8 +853,6 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 			const float y = xs[n] * invM;
 			out[n] = sqrtf(x * x + y * y);
 		}
-	} else {
-		store_imag_pass<S>(p, xs, a);
 	}
 	__syncthreads();  // shared memory is reused by the next A-scan of a batch
 }
@@ -715,6 +864,16 @@ __device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
 	const PrepLayout lay(p, false);
 	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
 	const float* taps = PT ? p.paramTaps : sm + lay.taps;
+	if constexpr (NT > 0) {
+		if (p.dcCoef) {
+			const unsigned K = (NT - 1) / 2;
+			const float m = dc_mean(sm + lay.rfs + K, p.dcCoef, p.ns, sm + lay.red, static_cast<float>(p.L - p.deadZone));
+			fir_dc_free_pass<S, NT, U, PT, false>(p, sm + lay.rfs, taps, m, nullptr,
+					reinterpret_cast<typename Real<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride);
+			__syncthreads();
+			return;
+		}
+	}
 	const float part = fir_pass<NT, U, PT>(p, sm + lay.rfs, taps, nullptr);
 	const float mean = block_sum(part, sm + lay.red) / static_cast<float>(p.L - p.deadZone);
 	store_real_pass<S, NT, U, PT>(p, sm + lay.rfs, taps, mean, a);
@@ -752,6 +911,165 @@ __host__ __device__ inline int fir_shape(unsigned tapsPerPhase, unsigned U)
 	if (tapsPerPhase == 21 && U == 4) return 3;
 	if (tapsPerPhase == 1 && U == 1) return 4;
 	return 0;
+}
+
+// ------------------------------------------------------------------ stream
+// Single-frame launches of the specialised FIR shapes: persistent blocks
+// (as many as the SMs hold) walk the frame's A-scans. Per block, once: the
+// FIR taps, twiddle tables and DC weights into shared memory, and the zero
+// margins of two input buffers. Per A-scan: its RF row arrives by bulk copy
+// into one buffer while the previous A-scan is processed from the other
+// (plain loads when the RF is not bulk-copyable, e.g. host memory read
+// through the host's page tables); the DC mean of [deadZone, L) is the dot
+// product of the row with PrepParams::dcCoef, so the FIR pass writes the
+// DC-free signal (and, analytic path, its real parts to the output; real
+// path, the output itself) in one pass.
+struct StreamLayout {   // float offsets
+	unsigned data, rfs[2], taps, twLo, twHi, stw, dc, red, bar, total;
+	__host__ __device__ StreamLayout(const PrepParams& p, bool analytic)
+	{
+		const unsigned K = (p.tapsPerPhase - 1) / 2;
+		data = 0;
+		unsigned o = analytic ? ((2 * p.M + 3) & ~3u) : 0;
+		// rfs[b][i] = rf[i - K]: K zeros, the row, K + 1 zeros; rfs + K is
+		// 16-byte aligned (the bulk copy's destination).
+		const unsigned pad = (4 - K % 4) % 4;
+		const unsigned slot = (pad + 2 * K + p.ns + 1 + 3) & ~3u;
+		rfs[0] = o + pad;
+		rfs[1] = o + slot + pad;
+		o += 2 * slot;
+		taps = o;
+		o += p.U * p.tapsStride;
+		twLo = o;
+		twHi = twLo + (analytic ? 2 * kTwiddleSplit : 0);
+		stw = twHi + (analytic ? 2 * p.twHiCount : 0);
+		dc = stw + ((analytic && p.stw) ? 2 * p.stwCount : 0);
+		red = (dc + p.ns + 3) & ~3u;
+		bar = red + 32;            // two mbarriers (16-byte aligned)
+		total = bar + 4;
+	}
+};
+
+constexpr unsigned long long kPrepWaitLimitNs = 2000000000ull;   // 2 s
+
+template<int S, int NT, int U, int T, bool ANALYTIC>
+__global__ void __launch_bounds__(T, kPrepThreads / T)
+prep_stream_kernel(const __grid_constant__ PrepParams p)
+{
+	extern __shared__ __align__(16) float sm[];
+	__shared__ int sAbort;
+	constexpr bool PT = param_taps_fit<NT, U>() && (ANALYTIC || U <= 4);
+	constexpr unsigned K = (NT - 1) / 2;
+	const StreamLayout lay(p, ANALYTIC);
+	const unsigned ns = p.ns;
+	uint64_t* bar = reinterpret_cast<uint64_t*>(sm + lay.bar);
+	float* dc = sm + lay.dc;
+
+	// Once per block: tables, DC weights, zero margins, barriers.
+	for (unsigned i = threadIdx.x; i < p.U * p.tapsStride; i += T) sm[lay.taps + i] = __ldg(&p.polyTaps[i]);
+	if constexpr (ANALYTIC) {
+		const unsigned ntw = 2 * (kTwiddleSplit + p.twHiCount);
+		const float* twg = reinterpret_cast<const float*>(p.tw);
+		for (unsigned i = threadIdx.x; i < ntw; i += T) sm[lay.twLo + i] = __ldg(&twg[i]);
+		if (p.stw) {
+			const float* stg = reinterpret_cast<const float*>(p.stw);
+			for (unsigned i = threadIdx.x; i < 2 * p.stwCount; i += T) sm[lay.stw + i] = __ldg(&stg[i]);
+		}
+	}
+	for (unsigned i = threadIdx.x; i < ns; i += T) dc[i] = __ldg(&p.dcCoef[i]);
+	for (int b = 0; b < 2; ++b) {
+		float* rfs = sm + lay.rfs[b];
+		for (unsigned i = threadIdx.x; i < 2 * K + 1; i += T) rfs[static_cast<int>(i) < static_cast<int>(K) ? i : ns + i] = 0.f;   // [0, K), [K + ns, 2K + ns + 1)
+	}
+	if (threadIdx.x == 0) {
+		sAbort = 0;
+		mbar_init(&bar[0], 1);
+		mbar_init(&bar[1], 1);
+		fence_barrier_init();
+	}
+	__syncthreads();
+
+	const bool bulk = p.rfBulk != 0;
+	const unsigned rowBytes = ns * static_cast<unsigned>(sizeof(float));
+	unsigned a = blockIdx.x;
+	if (bulk && threadIdx.x == 0 && a < p.numSignals) {
+		mbar_arrive_expect_tx(&bar[0], rowBytes);
+		bulk_copy_g2s(sm + lay.rfs[0] + K, p.rf + static_cast<size_t>(a) * ns, rowBytes, &bar[0]);
+	}
+	const float* taps = PT ? p.paramTaps : sm + lay.taps;
+	for (unsigned k = 0; a < p.numSignals; a += gridDim.x, ++k) {
+		const unsigned cur = k & 1u;
+		float* rfs = sm + lay.rfs[cur];
+		if (bulk) {
+			if (threadIdx.x == 0) {
+				if (!mbar_wait_bounded(&bar[cur], (k >> 1) & 1u, kPrepWaitLimitNs)) {
+					sAbort = 1;
+					if (p.errWord) atomicOr(p.errWord, DEVERR_WAIT_TIMEOUT);
+				} else {
+					// The next row into the other buffer (its last readers, the
+					// previous A-scan's FIR pass, are past several barriers).
+					const unsigned an = a + gridDim.x;
+					if (an < p.numSignals) {
+						fence_proxy_async_smem();
+						mbar_arrive_expect_tx(&bar[cur ^ 1u], rowBytes);
+						bulk_copy_g2s(sm + lay.rfs[cur ^ 1u] + K, p.rf + static_cast<size_t>(an) * ns, rowBytes,
+								&bar[cur ^ 1u]);
+					}
+				}
+			}
+		} else {
+			const float* row = p.rf + static_cast<size_t>(a) * ns;
+			for (unsigned i = threadIdx.x; i < ns; i += T) rfs[K + i] = row[i];
+		}
+		__syncthreads();
+		if (sAbort) return;   // the row never arrived; no copy is left in flight
+
+		const float mean = dc_mean(rfs + K, dc, ns, sm + lay.red, static_cast<float>(p.L - p.deadZone));
+
+		float* xs = sm + lay.data;
+		void* outRow;
+		if constexpr (ANALYTIC) {
+			outRow = reinterpret_cast<typename Complex<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride;
+			for (unsigned n = p.L + threadIdx.x; n < 2 * p.M; n += T) xs[n] = 0.f;
+		} else {
+			outRow = reinterpret_cast<typename Real<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride;
+		}
+		fir_dc_free_pass<S, NT, U, PT, ANALYTIC>(p, rfs, taps, mean, xs, outRow);
+		__syncthreads();
+		if constexpr (ANALYTIC) {
+			store_real_parts<S>(p, xs, outRow);
+			__syncthreads();
+			prep_analytic_tail<S>(p, a, reinterpret_cast<float2*>(sm + lay.data), xs,
+					reinterpret_cast<const float2*>(sm + lay.twLo), reinterpret_cast<const float2*>(sm + lay.twHi),
+					p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr);
+		}
+	}
+}
+
+template<int S, int NT, int U, int T>
+cudaError_t launch_stream_t(const PrepParams& p, bool analytic, size_t smem, cudaStream_t stream)
+{
+	const auto kernel = analytic ? prep_stream_kernel<S, NT, U, T, true> : prep_stream_kernel<S, NT, U, T, false>;
+	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+	if (e != cudaSuccess) return e;
+	int perSM = 0, dev = 0, sms = 0;
+	if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, T, smem)) != cudaSuccess) return e;
+	if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+	if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+	const unsigned blocks = std::min(p.numSignals, static_cast<unsigned>(sms) * static_cast<unsigned>(perSM > 0 ? perSM : 1));
+	kernel<<<blocks, T, smem, stream>>>(p);
+	return cudaGetLastError();
+}
+
+template<int S, int NT, int U>
+cudaError_t launch_stream(const PrepParams& p, bool analytic, cudaStream_t stream)
+{
+	const size_t smem = static_cast<size_t>(StreamLayout(p, analytic).total) * sizeof(float);
+	switch (prep_threads(smem)) {
+	case 128: return launch_stream_t<S, NT, U, 128>(p, analytic, smem, stream);
+	case 256: return launch_stream_t<S, NT, U, 256>(p, analytic, smem, stream);
+	default: return launch_stream_t<S, NT, U, 512>(p, analytic, smem, stream);
+	}
 }
 
 // Many frames: persistent blocks walk the A-scans of every frame of the batch.
@@ -912,8 +1230,36 @@ cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream)
 	}
 }
 
+template<int S>
+cudaError_t dispatch_stream(const PrepParams& p, bool analytic, cudaStream_t stream)
+{
+	switch (fir_shape(p.tapsPerPhase, p.U)) {
+	case 1: return launch_stream<S, 27, 8>(p, analytic, stream);
+	case 2: return launch_stream<S, 27, 4>(p, analytic, stream);
+	case 3: return launch_stream<S, 21, 4>(p, analytic, stream);
+	default: return launch_stream<S, 1, 1>(p, analytic, stream);
+	}
+}
+
+bool prep_uses_stream(const PrepParams& p)
+{
+	return p.dcCoef != nullptr && fir_shape(p.tapsPerPhase, p.U) != 0;
+}
+
+size_t prep_stream_smem_bytes(const PrepParams& p, bool analytic)
+{
+	return static_cast<size_t>(StreamLayout(p, analytic).total) * sizeof(float);
+}
+
 cudaError_t launch_prep(const PrepParams& p, int storage, bool analytic, cudaStream_t stream)
 {
+	if (prep_uses_stream(p)) {
+		switch (storage) {
+		case STORE_F16: return dispatch_stream<STORE_F16>(p, analytic, stream);
+		case STORE_BF16: return dispatch_stream<STORE_BF16>(p, analytic, stream);
+		default: return dispatch_stream<STORE_F32>(p, analytic, stream);
+		}
+	}
 	const size_t smem = prep_smem_bytes(p, analytic);
 	switch (storage) {
 	case STORE_F16: return dispatch_fir<STORE_F16>(p, analytic, smem, stream);

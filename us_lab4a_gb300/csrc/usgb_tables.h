@@ -129,6 +129,31 @@ inline bool make_poly_taps(bool analytic, unsigned U, PolyTaps& out)
 	return true;
 }
 
+// Weights of the input samples in the sum of the upsampled signal over
+// [deadZone, L): y[bU + r] = sum_t poly[r][t] x[b + K - t] for b < ns, so
+// x[j] enters that sum through every (t, r) whose output n = (j - K + t) U + r
+// lies in [deadZone, L) with 0 <= j - K + t < ns (the DC mean of
+// Util::removeDC, src/util/Util.h:1009-1018, as a dot product with the input).
+inline std::vector<float> dc_coefficients(const PolyTaps& poly, unsigned U, unsigned ns, unsigned deadZone)
+{
+	const long long K = (poly.tapsPerPhase - 1) / 2;
+	const long long L = static_cast<long long>(ns) * U;
+	std::vector<float> c(ns);
+	for (long long j = 0; j < static_cast<long long>(ns); ++j) {
+		double sum = 0.0;
+		for (long long t = 0; t < static_cast<long long>(poly.tapsPerPhase); ++t) {
+			const long long b = j - K + t;
+			if (b < 0 || b >= static_cast<long long>(ns)) continue;
+			for (long long r = 0; r < static_cast<long long>(U); ++r) {
+				const long long n = b * U + r;
+				if (n >= static_cast<long long>(deadZone) && n < L) sum += poly.poly[r * poly.tapsStride + t];
+			}
+		}
+		c[j] = static_cast<float>(sum);
+	}
+	return c;
+}
+
 // Copies the polyphase taps into the launch parameters (zero past them; the
 // specialised FIR kernels read them only when they fit).
 inline void set_param_taps(PrepParams& pp, const std::vector<float>& poly)

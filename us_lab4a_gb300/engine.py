@@ -114,7 +114,8 @@ class StaEngine:
     def set_das_variant(self, variant: int, tile_rows: int = 0, stage_bytes: int = 0, stages: int = 0) -> None:
         """0: plain kernel; 1: staged kernel; 2: receiver-group kernel on
         32-column tiles (tile_rows in {4, 8, 16}); 3: receiver-group kernel on
-        64-column tiles (tile_rows 4 or 8); stages in [2, 16]."""
+        64-column tiles (tile_rows 1 to 8); 4: the same with two grid rows per
+        thread row (64 x 2 * tile_rows tiles); stages in [2, 16]."""
         self._check(self._lib.usgb_set_das_variant(self._h, variant, tile_rows, stage_bytes, stages))
 
     DELAY_PRECISION = {"auto": 0, "fp32": 1, "fp64": 2}
