@@ -268,6 +268,20 @@ __device__ __forceinline__ void twiddle_powers(float2* w)
 	for (int q = 2; q < R; ++q) w[q] = cmul(w[q / 2], w[q - q / 2]);
 }
 
+// One component (c = 0: real, 1: imaginary) of complex output sample n,
+// rounded as Complex<S>::pack rounds it.
+template<int S>
+__device__ __forceinline__ void store_component(typename Complex<S>::T* out, size_t n, int c, float v)
+{
+	if constexpr (S == STORE_F16) {
+		reinterpret_cast<__half*>(out)[2 * n + c] = __float2half_rn(v);
+	} else if constexpr (S == STORE_BF16) {
+		reinterpret_cast<__nv_bfloat16*>(out)[2 * n + c] = __float2bfloat16_rn(v);
+	} else {
+		reinterpret_cast<float*>(out)[2 * n + c] = v;
+	}
+}
+
 // One in-place stage over `data` (M points), blocks of span Ms, radix R.
 // Forward (DIF): DFT_R of the R inputs at stride Ms/R, then twiddle
 // W_Ms^(q j). Inverse (DIT, the transpose): conjugate twiddle, then DFT_R.
@@ -552,19 +566,6 @@ __device__ float fir_pass(const PrepParams& p, const float* rfs, const float* ta
 	return part;
 }
 
-// One component (c = 0: real, 1: imaginary) of complex output sample n,
-// rounded as Complex<S>::pack rounds it.
-template<int S>
-__device__ __forceinline__ void store_component(typename Complex<S>::T* out, size_t n, int c, float v)
-{
-	if constexpr (S == STORE_F16) {
-		reinterpret_cast<__half*>(out)[2 * n + c] = __float2half_rn(v);
-	} else if constexpr (S == STORE_BF16) {
-		reinterpret_cast<__nv_bfloat16*>(out)[2 * n + c] = __float2bfloat16_rn(v);
-	} else {
-		reinterpret_cast<float*>(out)[2 * n + c] = v;
-	}
-}
 
 // Imaginary parts y[n] / M of the analytic output (the real parts were
 // written by the DC-removal pass).
@@ -627,8 +628,8 @@ __device__ __forceinline__ void hilbert_pair(float2* data, unsigned i, const flo
 }
 
 // y[n] - mean for the U outputs of input position b: into xs (analytic path,
-// the FFT buffer; store_real_parts writes them to the output afterwards with
-// coalesced stores) or into the real output.
+// the FFT buffer; prep_analytic_tail stores them to the output) or into the
+// real output.
 template<int S, int U, bool ANALYTIC>
 __device__ __forceinline__ void fir_store_dc_free(const PrepParams& p, unsigned b, const float* o, float mean,
 		float* xs, void* outRow)
@@ -661,35 +662,17 @@ __device__ __forceinline__ void fir_store_dc_free(const PrepParams& p, unsigned 
 }
 
 // The real parts of the analytic output, (x[n] * scale, 0) for n < L, from the
-// DC-free signal in xs: four samples a thread and step (one 16-byte shared
-// load, 16-byte global stores), consecutive threads on consecutive samples.
-// Every 32-byte sector is written whole (the imaginary halves merge into the
-// lines in L2 later).
+// DC-free signal in xs, one sample a thread and step: consecutive threads
+// store consecutive 8-byte samples (measured twice as fast per byte as
+// 16-byte stores of two samples), every 32-byte sector written whole (the
+// imaginary halves merge into the lines in L2 later).
 template<int S>
 __device__ void store_real_parts(const PrepParams& p, const float* xs, void* outRow)
 {
 	using CT = typename Complex<S>::T;
 	CT* out = reinterpret_cast<CT*>(outRow);
 	const float sc = p.outScale;
-	const unsigned L4 = p.L & ~3u;
-	for (unsigned n = 4 * threadIdx.x; n < L4; n += 4 * blockDim.x) {
-		const float4 v = *reinterpret_cast<const float4*>(xs + n);
-		if constexpr (S == STORE_F32) {
-			float4* o = reinterpret_cast<float4*>(out + n);
-			o[0] = make_float4(v.x * sc, 0.0f, v.y * sc, 0.0f);
-			o[1] = make_float4(v.z * sc, 0.0f, v.w * sc, 0.0f);
-		} else {
-			const CT c0 = Complex<S>::pack(v.x * sc, 0.0f), c1 = Complex<S>::pack(v.y * sc, 0.0f);
-			const CT c2 = Complex<S>::pack(v.z * sc, 0.0f), c3 = Complex<S>::pack(v.w * sc, 0.0f);
-			uint4 w;
-			w.x = *reinterpret_cast<const unsigned*>(&c0);
-			w.y = *reinterpret_cast<const unsigned*>(&c1);
-			w.z = *reinterpret_cast<const unsigned*>(&c2);
-			w.w = *reinterpret_cast<const unsigned*>(&c3);
-			*reinterpret_cast<uint4*>(out + n) = w;
-		}
-	}
-	for (unsigned n = L4 + threadIdx.x; n < p.L; n += blockDim.x) out[n] = Complex<S>::pack(xs[n] * sc, 0.0f);
+	for (unsigned n = threadIdx.x; n < p.L; n += blockDim.x) out[n] = Complex<S>::pack(xs[n] * sc, 0.0f);
 }
 
 // The mean of [deadZone, L) from the inputs: sum_i x[i] dc[i] / count, in
@@ -757,14 +740,20 @@ __device__ __forceinline__ void hilbert_pass(const PrepParams& p, float2* data)
 }
 
 // Steps 3-6 of the analytic path after the DC-free signal is in the buffer:
-// forward FFT (digit-reversed output), Hilbert multiplier and real-FFT
-// split, inverse FFT (natural-order output: y[n] * M at float index n), the
-// imaginary parts y[n] / M stored (the real parts were stored with the DC
-// removal), and a barrier (shared memory is reused by the next A-scan).
+// the real parts of the output row (x[n] * scale, 0) stored, forward FFT
+// (digit-reversed output), Hilbert multiplier and real-FFT split, inverse
+// FFT (natural-order output: y[n] * M at float index n), the imaginary parts
+// y[n] / M * scale stored, and a barrier (shared memory is reused by the next
+// A-scan). The stores take passes of their own: folded into the outermost
+// FFT stages they share the load/store pipe with the butterflies' shared
+// memory traffic and measured slower (cf2d: 30.4 k -> 41.5 k cycles forward,
+// 29.5 k -> 39.0 k inverse, per A-scan).
 template<int S>
 __device__ void prep_analytic_tail(const PrepParams& p, unsigned a, float2* data, const float* xs, const float2* twLo,
 		const float2* twHi, const float2* stw)
 {
+	store_real_parts<S>(p, xs, reinterpret_cast<typename Complex<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride);
+	__syncthreads();
 	fft_run<false>(data, p, twLo, twHi, stw);
 	hilbert_pass(p, data);
 	__syncthreads();
@@ -803,32 +792,23 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 			void* outRow = reinterpret_cast<typename Complex<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride;
 			fir_dc_free_pass<S, NT, U, PT, true>(p, rfs, taps, m, xs, outRow);
 			__syncthreads();
-			store_real_parts<S>(p, xs, outRow);
-			__syncthreads();
 			prep_analytic_tail<S>(p, a, data, xs, twLo, twHi, stw);
 			return;
 		}
 	}
 	const float part = fir_pass<NT, U, PT>(p, rfs, taps, xs);
 	// 2. DC removal: mean of [deadZone, L) subtracted from all L samples
-	//    (block_sum's barriers also order the writes above).
-	//    The real parts of the output, (x[n] - mean) * scale, are stored here
-	//    (the FFT overwrites x) as whole complex samples with a zero
+	//    (block_sum's barriers also order the writes above). The real parts
+	//    of the output, (x[n] - mean) * scale, are stored with the first FFT
+	//    stage (prep_analytic_tail) as whole complex samples with a zero
 	//    imaginary part, so that every 32-byte sector is written whole: a
 	//    sector holding only real halves was written back to HBM partially
-	//    and read back when the imaginary parts (step 6) arrived, 0.7 GB each
-	//    way per cf2d frame. The imaginary parts then merge into the lines in L2.
+	//    and read back when the imaginary parts arrived, 0.7 GB each way per
+	//    cf2d frame. The imaginary parts then merge into the lines in L2.
 	float mean = 0.f;
 	if constexpr (!ENV) {
 		mean = block_sum(part, sm + lay.red) / static_cast<float>(L - p.deadZone);
-		using CT = typename Complex<S>::T;
-		CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
-		const float sc = p.outScale;
-		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) {
-			const float d = xs[n] - mean;
-			xs[n] = d;
-			out[n] = Complex<S>::pack(d * sc, 0.0f);
-		}
+		for (unsigned n = threadIdx.x; n < L; n += blockDim.x) xs[n] -= mean;
 	}
 	__syncthreads();
 
@@ -1037,8 +1017,6 @@ prep_stream_kernel(const __grid_constant__ PrepParams p)
 		fir_dc_free_pass<S, NT, U, PT, ANALYTIC>(p, rfs, taps, mean, xs, outRow);
 		__syncthreads();
 		if constexpr (ANALYTIC) {
-			store_real_parts<S>(p, xs, outRow);
-			__syncthreads();
 			prep_analytic_tail<S>(p, a, reinterpret_cast<float2*>(sm + lay.data), xs,
 					reinterpret_cast<const float2*>(sm + lay.twLo), reinterpret_cast<const float2*>(sm + lay.twHi),
 					p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr);
