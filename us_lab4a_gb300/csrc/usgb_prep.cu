@@ -390,8 +390,10 @@ struct PrepLayout {
 
 // Loads the A-scan into shared memory with K zeros on each side (and one
 // spare zero at the end), the polyphase taps and the twiddle tables.
+// tables: also the taps and twiddle tables (false: they are still in shared
+// memory from the previous A-scan of the same frame).
 __device__ void load_inputs(const PrepParams& p, const PrepLayout& lay, float* sm, const float* __restrict__ rf,
-		bool analytic)
+		bool analytic, bool tables = true)
 {
 	const unsigned K = (p.tapsPerPhase - 1) / 2;
 	float* rfs = sm + lay.rfs;
@@ -401,6 +403,10 @@ __device__ void load_inputs(const PrepParams& p, const PrepLayout& lay, float* s
 		rfs[i] = (j >= 0 && j < static_cast<int>(p.ns)) ? __ldg(&rf[j]) : 0.f;
 	}
 	float* taps = sm + lay.taps;
+	if (!tables) {
+		__syncthreads();
+		return;
+	}
 	for (unsigned i = threadIdx.x; i < p.U * p.tapsStride; i += blockDim.x) taps[i] = __ldg(&p.polyTaps[i]);
 	if (analytic) {
 		const unsigned ntw = 2 * (kTwiddleSplit + p.twHiCount);
@@ -768,10 +774,10 @@ __device__ void prep_analytic_tail(const PrepParams& p, unsigned a, float2* data
 // used with U = 1 on image columns). PT: FIR taps from p.paramTaps (p a
 // launch parameter) instead of shared memory.
 template<int S, int NT, int U, bool ENV = false, bool PT = false>
-__device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
+__device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm, bool tables = true)
 {
 	const PrepLayout lay(p, true);
-	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, true);
+	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, true, tables);
 	float2* data = reinterpret_cast<float2*>(sm + lay.data);
 	float* xs = sm + lay.data;  // the packed complex buffer read as floats: x[n] at n
 	const float* rfs = sm + lay.rfs;
@@ -839,10 +845,10 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm)
 
 // Real-RF path: upsampling (fixed 4x FIR) and DC removal only.
 template<int S, int NT, int U, bool PT = false>
-__device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm)
+__device__ void prep_real_body(const PrepParams& p, unsigned a, float* sm, bool tables = true)
 {
 	const PrepLayout lay(p, false);
-	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false);
+	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, false, tables);
 	const float* taps = PT ? p.paramTaps : sm + lay.taps;
 	if constexpr (NT > 0) {
 		if (p.dcCoef) {
@@ -1064,8 +1070,11 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 	for (unsigned g = blockIdx.x; g < total; g += gridDim.x) {
 		while (f + 1 < count && frames[f + 1].signalBegin <= g) ++f;
 		__syncthreads();  // the previous A-scan is done with sp
-		if (f != loaded) {
-			// The frame's parameters into shared memory, by the whole block.
+		// The frame's parameters into shared memory, by the whole block, and
+		// its tables with its first A-scan here (consecutive A-scans of a
+		// block mostly belong to one frame: only their RF rows are loaded).
+		const bool tables = f != loaded;
+		if (tables) {
 			const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&frames[f].prep);
 			unsigned long long* dst = reinterpret_cast<unsigned long long*>(&sp);
 			for (unsigned i = threadIdx.x; i < sizeof(PrepParams) / 8; i += blockDim.x) dst[i] = src[i];
@@ -1076,14 +1085,14 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 		const int shape = fir_shape(sp.tapsPerPhase, sp.U);
 		if (ANALYTIC) {
 			switch (shape) {
-			case 1: prep_analytic_body<S, 27, 8>(sp, a, sm); break;
-			case 2: prep_analytic_body<S, 27, 4>(sp, a, sm); break;
-			case 4: prep_analytic_body<S, 1, 1>(sp, a, sm); break;
-			default: prep_analytic_body<S, 0, 1>(sp, a, sm); break;
+			case 1: prep_analytic_body<S, 27, 8>(sp, a, sm, tables); break;
+			case 2: prep_analytic_body<S, 27, 4>(sp, a, sm, tables); break;
+			case 4: prep_analytic_body<S, 1, 1>(sp, a, sm, tables); break;
+			default: prep_analytic_body<S, 0, 1>(sp, a, sm, tables); break;
 			}
 		} else {
-			if (shape == 3) prep_real_body<S, 21, 4>(sp, a, sm);
-			else prep_real_body<S, 0, 1>(sp, a, sm);
+			if (shape == 3) prep_real_body<S, 21, 4>(sp, a, sm, tables);
+			else prep_real_body<S, 0, 1>(sp, a, sm, tables);
 		}
 	}
 }
