@@ -438,6 +438,11 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(frame, os.cpu_count() or 1, rf_host_full)
 
+    configs = None
+    if world == 1 and not args.no_configs:
+        torch.cuda.empty_cache()
+        configs = run_configs(dev)
+
     mixed = None
     if world == 1 and not args.no_mixed:
         eng.close()
@@ -481,7 +486,7 @@ def run_gpu(args):
             "das_gathers_per_s": gathers / (das_ms * 1e-3),
             "das_onchip": onchip,
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
-            "mixed": mixed, "single": single, "two_medium": two_medium,
+            "configs": configs, "mixed": mixed, "single": single, "two_medium": two_medium,
         }
         line["north_star"] = _north_star(line)   # last key: the summary the record's tail keeps
         print(json.dumps(line), flush=True)
@@ -536,6 +541,9 @@ def _north_star(line: dict) -> dict:
            "kernels_ms": line["kernels_ms"],
            "das_hbm_frac": line["roofline"]["frac"] if line["roofline"]["kernel"] == "das" else None,
            "das_smem_pipe_frac": (line.get("das_onchip") or {}).get("smem_frac")}
+    c = line.get("configs")
+    if c:
+        out["configs"] = {k: {"fps": v["frames_per_s"], "err_db": v["err_db_vs_fp64"]} for k, v in c.items()}
     m = line.get("mixed")
     if m:
         out["mixed_48"] = {
@@ -592,6 +600,77 @@ def _worst_db(refs, images) -> float:
         v = np.asarray(images[i], np.float64).reshape(-1)[idx]
         worst = max(worst, _db(float(np.abs(v - ref).max()), float(np.abs(ref).max())))
     return worst
+
+
+def _time_frame(dev, frame, storage: str, reps: int):
+    """One frame of the workload through usgb_process_device with the
+    context's default kernels, RF resident: median ms per frame over `reps`
+    CUDA-event-timed frames after 3 warm-up frames; returns (ms, image, host RF)."""
+    import torch
+    from us_lab4a_gb300 import StaEngine, workloads
+    fr = workloads.with_storage(frame, storage) if storage != frame.spec.storage else frame
+    rf = fr.make_rf_torch(dev)
+    g = torch.as_tensor(fr.grid_xyz, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    with StaEngine(fr.spec) as eng:
+        eng.set_stream(stream)
+        eng.set_grid_device(g)
+        v = torch.empty(fr.grid_xyz.shape[:2], device=dev)
+        f = torch.empty_like(v)
+        for _ in range(3):
+            eng.process_device(rf, v, f)
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.process_device(rf, v, f)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        eng.synchronize()
+        img = v.cpu().numpy()
+    return statistics.median(ts), img, rf.cpu().numpy()
+
+
+def run_configs(dev, reps: int = 10):
+    """The other benchmark configurations at their full sizes, one frame at a
+    time with the default kernels: the 32-element CPU configuration (FP32,
+    whole image against the FP64 oracle, the CPU oracle timed on the whole
+    frame) and the 16 x 16 matrix array (FP16 and BF16 storage against the
+    FP64 oracle at sampled voxels; the oracle prepares all 65 536 A-scans)."""
+    from us_lab4a_gb300 import workloads
+    import oracle
+    threads = os.cpu_count() or 1
+    out = {}
+    fr = workloads.plain2d()
+    ms, img, rf = _time_frame(dev, fr, "f32", reps)
+    t0 = time.perf_counter()
+    ref, _, _ = oracle.process(_oracle_spec(fr.spec, threads), rf.astype(np.float64), fr.grid_xyz, dtype=np.float64)
+    t_ref = time.perf_counter() - t0
+    cpu = time_oracle_frames(fr, rf, threads, 1, 2)
+    out["plain2d_f32"] = {
+        "workload": "32-element linear array, 2048 samples @40 MHz, 4x, rectangular, no CF, 128x256 grid",
+        "frames_per_s": 1e3 / ms, "ms_per_frame": ms, "voxels_per_s": 1e3 / ms * fr.npix,
+        "err_db_vs_fp64": _db(float(np.abs(img.astype(np.float64) - ref).max()), float(np.abs(ref).max())),
+        "err_points": "every grid point",
+        "cpu_oracle": {"frames_per_s": 1.0 / statistics.mean(cpu), "cores": threads, "kind": "port",
+                       "sample": "whole frames, FP32 oracle, 1 warm-up + 2 timed"},
+        "fp64_oracle_s": t_ref}
+    fr = workloads.matrix3d()
+    for storage in ("f16", "bf16"):
+        ms, img, rf = _time_frame(dev, fr, storage, reps)
+        idx = _sample_idx(img, 256, 1792, seed=7)
+        pts = fr.grid_xyz.reshape(-1, 3)[idx][:, None, :]
+        if storage == "f16":
+            ref, _, _ = oracle.process(_oracle_spec(fr.spec, threads), rf.astype(np.float64), pts, dtype=np.float64)
+            ref = ref[:, 0]
+        v = img.reshape(-1)[idx].astype(np.float64)
+        out[f"matrix3d_{storage}"] = {
+            "workload": "16x16 matrix array (pitch 0.3 mm), 1024 samples @24 MHz, 4x, PCF, 64x64x128 voxels",
+            "frames_per_s": 1e3 / ms, "ms_per_frame": ms, "voxels_per_s": 1e3 / ms * fr.npix,
+            "err_db_vs_fp64": _db(float(np.abs(v - ref).max()), float(np.abs(ref).max())),
+            "err_points": f"{idx.size} voxels (the 256 brightest of the GPU image and random ones)"}
+    return out
 
 
 def run_mixed(dev, num_frames: int = 48, reps: int = 2):
@@ -996,6 +1075,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the 48-frame mixed-size / serving section")
     ap.add_argument("--no-single", action="store_true", help="skip the single-term 3D processor section")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the section of the 32-element and 16 x 16 matrix-array configurations")
     ap.add_argument("--no-two-medium", action="store_true", help="skip the two-medium imaging section")
     args = ap.parse_args()
     if args.warmup < 3:
