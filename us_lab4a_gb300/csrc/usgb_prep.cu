@@ -166,6 +166,43 @@ template<> __device__ __forceinline__ float2 root<9>(int m)
 	default: return make_float2(0.76604444311897803520f, -0.64278760968653932632f);
 	}
 }
+// exp(2 pi i m / 10), m < 10: angles of 36 degrees.
+template<> __device__ __forceinline__ float2 root<10>(int m)
+{
+	constexpr float c1 = 0.80901699437494742410f, s1 = 0.58778525229247312917f;
+	constexpr float c2 = 0.30901699437494742410f, s2 = 0.95105651629515357212f;
+	switch (m) {
+	case 0: return make_float2(1.0f, 0.0f);
+	case 1: return make_float2(c1, s1);
+	case 2: return make_float2(c2, s2);
+	case 3: return make_float2(-c2, s2);
+	case 4: return make_float2(-c1, s1);
+	case 5: return make_float2(-1.0f, 0.0f);
+	case 6: return make_float2(-c1, -s1);
+	case 7: return make_float2(-c2, -s2);
+	case 8: return make_float2(c2, -s2);
+	default: return make_float2(c1, -s1);
+	}
+}
+// exp(2 pi i m / 12), m < 12: angles of 30 degrees.
+template<> __device__ __forceinline__ float2 root<12>(int m)
+{
+	constexpr float h = 0.86602540378443864676f;
+	switch (m) {
+	case 0: return make_float2(1.0f, 0.0f);
+	case 1: return make_float2(h, 0.5f);
+	case 2: return make_float2(0.5f, h);
+	case 3: return make_float2(0.0f, 1.0f);
+	case 4: return make_float2(-0.5f, h);
+	case 5: return make_float2(-h, 0.5f);
+	case 6: return make_float2(-1.0f, 0.0f);
+	case 7: return make_float2(-h, -0.5f);
+	case 8: return make_float2(-0.5f, -h);
+	case 9: return make_float2(0.0f, -1.0f);
+	case 10: return make_float2(0.5f, -h);
+	default: return make_float2(h, -0.5f);
+	}
+}
 // exp(2 pi i m / 15), m < 15: angles of 24 degrees (m > 7: conjugates of 15 - m).
 template<> __device__ __forceinline__ float2 root<15>(int m)
 {
@@ -251,6 +288,12 @@ template<int SIGN> struct SmallDFT<15, SIGN> {
 };
 template<int SIGN> struct SmallDFT<16, SIGN> {
 	static __device__ __forceinline__ void run(float2* v) { composite_dft<4, 4, SIGN>(v); }
+};
+template<int SIGN> struct SmallDFT<10, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<5, 2, SIGN>(v); }
+};
+template<int SIGN> struct SmallDFT<12, SIGN> {
+	static __device__ __forceinline__ void run(float2* v) { composite_dft<4, 3, SIGN>(v); }
 };
 
 // W^m from the two-level table in shared memory.
@@ -346,6 +389,8 @@ __device__ __noinline__ void fft_run(float2* data, const PrepParams& p, const fl
 		case 6: fft_stage<6, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		case 8: fft_stage<8, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		case 9: fft_stage<9, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 10: fft_stage<10, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
+		case 12: fft_stage<12, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		case 15: fft_stage<15, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		default: fft_stage<16, INVERSE>(data, twLo, twHi, st, p.M, spans[s], p.divMagic[s]); break;
 		}
