@@ -657,11 +657,12 @@ def run_configs(dev, reps: int = 10):
                        "sample": "whole frames, FP32 oracle, 1 warm-up + 2 timed"},
         "fp64_oracle_s": t_ref}
     fr = workloads.matrix3d()
+    idx = ref = None
     for storage in ("f16", "bf16"):
         ms, img, rf = _time_frame(dev, fr, storage, reps)
-        idx = _sample_idx(img, 256, 1792, seed=7)
-        pts = fr.grid_xyz.reshape(-1, 3)[idx][:, None, :]
-        if storage == "f16":
+        if ref is None:   # the same sampled voxels for both storage types (the RF is the same)
+            idx = _sample_idx(img, 256, 1792, seed=7)
+            pts = fr.grid_xyz.reshape(-1, 3)[idx][:, None, :]
             ref, _, _ = oracle.process(_oracle_spec(fr.spec, threads), rf.astype(np.float64), pts, dtype=np.float64)
             ref = ref[:, 0]
         v = img.reshape(-1)[idx].astype(np.float64)
