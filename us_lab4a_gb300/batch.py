@@ -43,7 +43,8 @@ class Batch:
 
     # (variant, tile rows, stage bytes, stages) tried by autotune(), most likely first;
     # variant 3 is the receiver-group kernel on 64-column tiles.
-    CANDIDATES = ((4, 4, 102400, 2), (4, 4, 65536, 2), (4, 4, 49152, 2), (4, 8, 102400, 2), (4, 8, 65536, 2),
+    CANDIDATES = ((4, 7, 102400, 2), (4, 7, 65536, 2), (4, 4, 102400, 2), (4, 4, 65536, 2), (4, 4, 49152, 2),
+                  (4, 8, 102400, 2), (4, 8, 65536, 2),
                   (3, 8, 98304, 2), (3, 8, 65536, 2), (2, 16, 98304, 2),
                   (3, 4, 32768, 2), (3, 4, 49152, 2), (3, 8, 49152, 2), (3, 4, 24576, 3), (2, 8, 24576, 2),
                   (2, 8, 32768, 2), (2, 4, 32768, 2), (2, 4, 24576, 2), (2, 8, 20480, 2),
@@ -52,8 +53,8 @@ class Batch:
     def set_das_config(self, tile_rows: int, stage_bytes: int, stages: int, variant: int = None) -> None:
         """Tile shape of the batched delay-and-sum; variant 2 = receiver-group
         kernel on 32-column tiles, 3 = on 64-column tiles, 4 = on 64 x 2*rows
-        tiles with two points per thread, 1 = staged kernel (None keeps the
-        current one)."""
+        tiles with two points per thread (rows 4, 7 or 8), 1 = staged kernel
+        (None keeps the current one)."""
         if variant is not None and variant != getattr(self, "_variant", 2):
             # Shrink first so that the variant switch fits, then set the shape.
             self._check(self._lib.usgb_batch_set_das_config(self._h, 4, 8192, 2))

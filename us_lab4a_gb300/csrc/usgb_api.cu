@@ -943,6 +943,7 @@ int usgb_batch_set_das_variant(usgb_batch* b, int variant)
 	return batch_guarded(b, [&] {
 		if (variant < 1 || variant > 4) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Batched delay-and-sum variant must be 1, 2, 3 or 4.");
 		if (variant >= 3 && b->tileRows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
+		if (variant != 4 && b->tileRows == 7) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "7 tile rows need two points per thread (variant 4).");
 		if (batch_das_smem(b, variant, b->tileRows, b->stageBytes, b->stages) > max_smem()) {
 			USGB_FAIL(USGB_ERR_UNSUPPORTED, "the current tile shape does not fit in shared memory for this variant.");
 		}
@@ -957,7 +958,9 @@ int usgb_batch_set_das_variant(usgb_batch* b, int variant)
 int usgb_batch_set_das_config(usgb_batch* b, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages)
 {
 	return batch_guarded(b, [&] {
-		if (tile_rows != 4 && tile_rows != 8 && tile_rows != 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16.");
+		if (tile_rows != 4 && tile_rows != 8 && tile_rows != 16 && !(tile_rows == 7 && b->dasVariant == 4)) {
+			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Tile rows must be 4, 8 or 16 (or 7 with two points per thread).");
+		}
 		if (b->dasVariant >= 3 && tile_rows == 16) USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "64-column tiles have 4 or 8 rows.");
 		if (stage_bytes < 1024 || stage_bytes % 128 != 0 || stage_bytes > (1u << 20)) {
 			USGB_FAIL(USGB_ERR_INVALID_PARAMETER, "Stage size must be a multiple of 128 bytes in [1 KiB, 1 MiB].");

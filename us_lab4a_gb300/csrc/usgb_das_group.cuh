@@ -675,6 +675,9 @@ cudaError_t launch_group_rows(const DasParams& p, cudaStream_t stream)
 {
 	if (p.tileCols == 64) {   // 1-8 thread rows: blocks of 4 or 8, the rest of the rows idle
 		if (p.pointsPerThread == 2) {
+			// (5-8 rows on the 20-warp block with the register split: 64 x 14
+			// tiles there measured 1.437 ms against 1.481 ms on a 15-warp
+			// block at 128 registers a thread)
 			return p.tileRows <= 4 ? launch_group_one<S, CF, ANALYTIC, 64, 4, 2>(p, stream)
 			                       : launch_group_one<S, CF, ANALYTIC, 64, 8, 2>(p, stream);
 		}
@@ -783,8 +786,15 @@ cudaError_t group_batch_rows(const BatchDasFrame* frames, const BatchHeader* hdr
 {
 	if (c.tileCols == 64) {
 		if (c.pointsPerThread == 2) {
-			return c.tileRows == 4 ? launch_group_batch_one<S, ANALYTIC, 64, 4, 2>(frames, hdr, c, stream)
-			                       : launch_group_batch_one<S, ANALYTIC, 64, 8, 2>(frames, hdr, c, stream);
+			// 64 x 8 (9 warps), 64 x 14 (15 warps) or 64 x 16 (17 warps) grid
+			// points: up to 16 warps an SM keep 128 registers a thread; a 17th
+			// puts five warps on one of the SM's four register-file partitions
+			// (96 registers a thread, and the two-point consumers spill).
+			switch (c.tileRows) {
+			case 4: return launch_group_batch_one<S, ANALYTIC, 64, 4, 2>(frames, hdr, c, stream);
+			case 7: return launch_group_batch_one<S, ANALYTIC, 64, 7, 2>(frames, hdr, c, stream);
+			default: return launch_group_batch_one<S, ANALYTIC, 64, 8, 2>(frames, hdr, c, stream);
+			}
 		}
 		return c.tileRows == 4 ? launch_group_batch_one<S, ANALYTIC, 64, 4>(frames, hdr, c, stream)
 		                       : launch_group_batch_one<S, ANALYTIC, 64, 8>(frames, hdr, c, stream);
