@@ -953,8 +953,8 @@ __host__ __device__ inline int fir_shape(unsigned tapsPerPhase, unsigned U)
 // (plain loads when the RF is not bulk-copyable, e.g. host memory read
 // through the host's page tables); the DC mean of [deadZone, L) is the dot
 // product of the row with PrepParams::dcCoef, so the FIR pass writes the
-// DC-free signal (and, analytic path, its real parts to the output; real
-// path, the output itself) in one pass.
+// DC-free signal in one pass: into the FFT buffer (analytic path; the tail
+// stores its real parts, then transforms it) or as the output (real path).
 struct StreamLayout {   // float offsets
 	unsigned data, rfs[2], taps, twLo, twHi, stw, dc, red, bar, total;
 	__host__ __device__ StreamLayout(const PrepParams& p, bool analytic)
