@@ -174,7 +174,7 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * delays in a per-point table), 2 = receiver-group (the same ring, filled
  * receiver group by receiver group; a group's receive delays and sums stay in
  * registers, no per-point table, so arrays of hundreds of elements stage as
- * well), 3 = receiver-group on tiles of 64 columns x tile_rows (4 or 8) rows
+ * well), 3 = receiver-group on tiles of 64 columns x tile_rows (1 to 8) rows
  * (windows only a little longer for twice the points: fewer bytes and half
  * the copies staged per frame), 4 = as 3 with two grid points (neighbouring
  * rows) per consumer thread, tiles of 64 columns x 2 * tile_rows rows (twice
@@ -183,10 +183,11 @@ int usgb_signal_info(const usgb_ctx* ctx, uint32_t* signal_length, uint32_t* fft
  * the current value. New
  * contexts start with the receiver-group kernel (32 x 4 tiles, 2 x 32 KiB)
  * where it fits; setting a grid of at least 1.5 tiles of 64 x 16 points per
- * SM then selects variant 4 (tile_rows 8, 2 x 100 KiB stages), else one of at
- * least two 64-column tiles per SM variant 3 (64 x 8 with 2 x 100 or 96 KiB
- * stages, else 64 x 4 with 2 x 48 KiB) where it fits, unless a variant was
- * set here or by usgb_autotune_das. */
+ * SM then selects variant 4 with 2 x 100 KiB stages and tile_rows in [5, 8]
+ * for the fewest whole waves of tiles (512 x 512 on 152 SMs: 7, 64 x 14
+ * tiles), else one of at least two 64-column tiles per SM variant 3 (64 x 8
+ * with 2 x 100 or 96 KiB stages, else 64 x 4 with 2 x 48 KiB) where it fits,
+ * unless a variant was set here or by usgb_autotune_das. */
 int usgb_set_das_variant(usgb_ctx* ctx, int variant, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 int usgb_get_das_config(const usgb_ctx* ctx, int* variant, uint32_t* tile_rows, uint32_t* stage_bytes,
 		uint32_t* stages);
@@ -295,7 +296,7 @@ const char* usgb_batch_last_error(const usgb_batch* batch);
 int usgb_batch_set_das_config(usgb_batch* batch, uint32_t tile_rows, uint32_t stage_bytes, uint32_t stages);
 /* Delay-and-sum kernel of the batch: 2 = receiver-group (default), 3 =
  * receiver-group on 64-column tiles, 4 = receiver-group on 64 x 2*tile_rows
- * tiles with two points per thread, 1 = staged. */
+ * tiles with two points per thread (tile_rows 4, 7 or 8), 1 = staged. */
 int usgb_batch_set_das_variant(usgb_batch* batch, int variant);
 int usgb_batch_run(usgb_batch* batch, const usgb_batch_item* items, uint32_t count, void* cuda_stream, int use_graph);
 int usgb_batch_synchronize(usgb_batch* batch);
