@@ -319,28 +319,27 @@ __device__ __forceinline__ void group_gathers(const DasParams& p, const int2 un,
 {
 	using T = typename SP::T;
 	if (FULL && (un.y & kUnitInterior)) {
-		if constexpr (PY == 2 && !Q && SP::kAnalytic && sizeof(typename SP::T) == 8) {
-			// FP32 samples, two points: the two points' delay splits and
-			// accumulations as packed FP32x2 operations, each half rounded
-			// as the scalar form (fl(tx + rx), the round-down split against
-			// 2^23, k = d - floor(d) exactly, then fma(1 - k, s[i], acc) and
-			// fma(k, s[i + 1], acc) per component): the same bits, half the
-			// instructions.
+		if constexpr (PY == 2 && !Q && SP::kAnalytic) {
+			// Two points: the two points' delay splits and accumulations as
+			// packed FP32x2 operations, each half rounded as the scalar form
+			// (fl(tx + rx), the round-down split against 2^23, k = d -
+			// floor(d) exactly, then fma(1 - k, s[i], acc) and fma(k, s[i + 1],
+			// acc) per component on the samples widened to FP32): the same
+			// bits, half the instructions.
 			const float2 tx2 = make_float2(txv[0], txv[1]);
 			const float2 big = make_float2(8388608.0f, 8388608.0f);
 			const float2 nbig = make_float2(-8388608.0f, -8388608.0f);
 			const float2 m1 = make_float2(-1.0f, -1.0f);
 			const float2 one = make_float2(1.0f, 1.0f);
-			const float2* b2 = reinterpret_cast<const float2*>(buf);
 #pragma unroll
 			for (int j = 0; j < kGroup; ++j) {
 				const float2 d = __fadd2_rn(tx2, make_float2(rxd[0][j], rxd[1][j]));
 				const float2 t0 = __fadd2_rd(d, big);
 				const float2 k = __ffma2_rn(__fadd2_rn(t0, nbig), m1, d);
 				const float2 w0 = __ffma2_rn(k, m1, one);
-				const float2* s0 = b2 + (static_cast<int>(__float_as_uint(t0.x) - 0x4B000000u) + base[j]);
-				const float2* s1 = b2 + (static_cast<int>(__float_as_uint(t0.y) - 0x4B000000u) + base[j]);
-				const float2 a0 = s0[0], c0 = s0[1], a1 = s1[0], c1 = s1[1];
+				const T* s0 = buf + (static_cast<int>(__float_as_uint(t0.x) - 0x4B000000u) + base[j]);
+				const T* s1 = buf + (static_cast<int>(__float_as_uint(t0.y) - 0x4B000000u) + base[j]);
+				const float2 a0 = SP::load(s0), c0 = SP::load(s0 + 1), a1 = SP::load(s1), c1 = SP::load(s1 + 1);
 				acc[0][j] = __ffma2_rn(make_float2(k.x, k.x), c0, __ffma2_rn(make_float2(w0.x, w0.x), a0, acc[0][j]));
 				acc[1][j] = __ffma2_rn(make_float2(k.y, k.y), c1, __ffma2_rn(make_float2(w0.y, w0.y), a1, acc[1][j]));
 			}

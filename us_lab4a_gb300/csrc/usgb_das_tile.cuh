@@ -27,6 +27,7 @@ template<int S> struct Sample<true, S> {
 	using T = typename Complex<S>::T;
 	static constexpr bool kAnalytic = true;
 	static constexpr int kAlign = 16 / static_cast<int>(sizeof(T));  // elements per 16 bytes
+	static __device__ __forceinline__ float2 load(const T* s) { return Complex<S>::load(s); }
 	static __device__ __forceinline__ void accumulate(const T* s, float k, float2& acc)
 	{
 		const float2 a = Complex<S>::load(s);
