@@ -70,13 +70,14 @@ class ClockSampler:
         self.samples = []
         self._proc = None
         self._thread = None
+        self._mark = 0
 
     def start(self):
         cmd = ["nvidia-smi", "-i", str(self.index),
                "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
                "clocks_event_reasons.sw_power_cap",
-               "--format=csv,noheader,nounits", "-lms", "200"]
+               "--format=csv,noheader,nounits", "-lms", "50"]
         try:
             self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
@@ -88,10 +89,24 @@ class ClockSampler:
                 self.samples.append([x.strip() for x in line.split(",")])
         self._thread = threading.Thread(target=reader, daemon=True)
         self._thread.start()
+        # nvidia-smi takes a while to start: wait for its first sample so that
+        # the samples taken from here on fall inside the timed region.
+        t0 = time.time()
+        while not self.samples and time.time() - t0 < 10.0 and self._proc.poll() is None:
+            time.sleep(0.01)
+        self._mark = len(self.samples)
 
     def stop(self):
         if self._proc is None:
             return None
+        # A timed region shorter than the sampling interval may hold no
+        # sample: then take the first one after it (flagged by in_region 0).
+        n_region = len(self.samples) - self._mark
+        if n_region == 0:
+            t0 = time.time()
+            while len(self.samples) <= self._mark and time.time() - t0 < 2.0 and self._proc.poll() is None:
+                time.sleep(0.005)
+        self.samples = self.samples[self._mark:]
         self._proc.terminate()
         try:
             self._proc.wait(timeout=5)
@@ -112,7 +127,8 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "in_region": n_region,
+                "interval_ms": 50}
 
 
 def _dist():

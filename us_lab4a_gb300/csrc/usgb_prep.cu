@@ -52,10 +52,18 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b)  // a * conj(b)
 {
 	return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex sums as one packed FP32x2 operation each (a - b as fma(b, -1, a):
+// the exact difference rounded once, as a subtraction rounds it).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
 // Multiply by i * s (s = +1 or -1).
 __device__ __forceinline__ float2 cmuli(float2 a, float s) { return make_float2(-s * a.y, s * a.x); }
+__device__ __forceinline__ float2 splat(float c) { return make_float2(c, c); }
+// (a - b) with its components swapped: (a.y - b.y, a.x - b.x). A product
+// i * s * (a - b) = (-s (a.y - b.y), s (a.x - b.x)) then enters a packed
+// fma with the sign pair (-s, s), and a +/- i * s * (a - b) is one packed
+// fma per output, each component rounded once as the scalar sum rounds it.
+__device__ __forceinline__ float2 csub_swapped(float2 a, float2 b) { return make_float2(a.y - b.y, a.x - b.x); }
 
 // In-register DFT of size R; SIGN = -1 forward, +1 backward (unnormalised).
 template<int R, int SIGN> struct SmallDFT;
@@ -73,24 +81,24 @@ template<int SIGN> struct SmallDFT<3, SIGN> {
 	{
 		const float s1 = 0.86602540378443864676f * SIGN;
 		const float2 t1 = cadd(v[1], v[2]);
-		const float2 t2 = make_float2(v[0].x - 0.5f * t1.x, v[0].y - 0.5f * t1.y);
-		const float2 d = csub(v[1], v[2]);
-		const float2 t3 = make_float2(-s1 * d.y, s1 * d.x);
+		const float2 t2 = __ffma2_rn(splat(-0.5f), t1, v[0]);
+		const float2 ds = csub_swapped(v[1], v[2]);
 		v[0] = cadd(v[0], t1);
-		v[1] = cadd(t2, t3);
-		v[2] = csub(t2, t3);
+		v[1] = __ffma2_rn(ds, make_float2(-s1, s1), t2);
+		v[2] = __ffma2_rn(ds, make_float2(s1, -s1), t2);
 	}
 };
 template<int SIGN> struct SmallDFT<4, SIGN> {
 	static __device__ __forceinline__ void run(float2* v)
 	{
+		constexpr float sg = static_cast<float>(SIGN);
 		const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
 		const float2 t2 = cadd(v[1], v[3]);
-		const float2 t3 = cmuli(csub(v[1], v[3]), static_cast<float>(SIGN));
+		const float2 ds = csub_swapped(v[1], v[3]);
 		v[0] = cadd(t0, t2);
 		v[2] = csub(t0, t2);
-		v[1] = cadd(t1, t3);
-		v[3] = csub(t1, t3);
+		v[1] = __ffma2_rn(ds, make_float2(-sg, sg), t1);
+		v[3] = __ffma2_rn(ds, make_float2(sg, -sg), t1);
 	}
 };
 template<int SIGN> struct SmallDFT<5, SIGN> {
@@ -100,17 +108,18 @@ template<int SIGN> struct SmallDFT<5, SIGN> {
 		const float s1 = 0.95105651629515357212f * SIGN, s2 = 0.58778525229247312917f * SIGN;
 		const float2 a = v[0];
 		const float2 b1 = cadd(v[1], v[4]), b2 = cadd(v[2], v[3]);
-		const float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-		const float2 r1 = make_float2(a.x + c1 * b1.x + c2 * b2.x, a.y + c1 * b1.y + c2 * b2.y);
-		const float2 r2 = make_float2(a.x + c2 * b1.x + c1 * b2.x, a.y + c2 * b1.y + c1 * b2.y);
-		const float2 q1 = make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y);
-		const float2 q2 = make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y);
-		const float2 i1 = make_float2(-q1.y, q1.x), i2 = make_float2(-q2.y, q2.x);
-		v[0] = make_float2(a.x + b1.x + b2.x, a.y + b1.y + b2.y);
-		v[1] = cadd(r1, i1);
-		v[4] = csub(r1, i1);
-		v[2] = cadd(r2, i2);
-		v[3] = csub(r2, i2);
+		const float2 d1 = csub_swapped(v[1], v[4]), d2 = csub_swapped(v[2], v[3]);
+		const float2 r1 = __ffma2_rn(splat(c2), b2, __ffma2_rn(splat(c1), b1, a));
+		const float2 r2 = __ffma2_rn(splat(c1), b2, __ffma2_rn(splat(c2), b1, a));
+		// q1, q2 with swapped components (d1, d2 are swapped).
+		const float2 q1 = __ffma2_rn(splat(s2), d2, __fmul2_rn(splat(s1), d1));
+		const float2 q2 = __ffma2_rn(splat(-s1), d2, __fmul2_rn(splat(s2), d1));
+		const float2 mp = make_float2(-1.0f, 1.0f), pm = make_float2(1.0f, -1.0f);
+		v[0] = cadd(cadd(a, b1), b2);
+		v[1] = __ffma2_rn(q1, mp, r1);
+		v[4] = __ffma2_rn(q1, pm, r1);
+		v[2] = __ffma2_rn(q2, mp, r2);
+		v[3] = __ffma2_rn(q2, pm, r2);
 	}
 };
 
