@@ -141,6 +141,53 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Tensor memory (TMEM, 128 lanes x 512 columns of 32 bits per SM), inline
+// PTX (tcgen05, sm_100a family). A warp reaches only the 32 lanes of its SM
+// sub-partition (lanes 32 (warp % 4) .. + 31); an address is lane << 16 |
+// column. Allocation and release are whole-warp operations of one warp of
+// the block; the column count is a power of two in [32, 512].
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols)
+{
+	asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+			:: "r"(smem_addr(dst)), "r"(ncols) : "memory");
+	asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+	asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(ncols) : "memory");
+}
+// Orders this thread's tensor-memory operations before (after) a barrier.
+__device__ __forceinline__ void tmem_fence_before_sync()
+{
+	asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_fence_after_sync()
+{
+	asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// Eight consecutive columns of this thread's lane: store (complete when the
+// call returns) and load (the values valid when the call returns).
+__device__ __forceinline__ void tmem_store8(uint32_t taddr, const float (&v)[8])
+{
+	asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n\t"
+			"tcgen05.wait::st.sync.aligned;"
+			:: "r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+			"r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+			"r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])) : "memory");
+}
+__device__ __forceinline__ void tmem_load8(uint32_t taddr, float (&v)[8])
+{
+	uint32_t r0, r1, r2, r3, r4, r5, r6, r7;
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+			"tcgen05.wait::ld.sync.aligned;"
+			: "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3), "=r"(r4), "=r"(r5), "=r"(r6), "=r"(r7)
+			: "r"(taddr) : "memory");
+	v[0] = __uint_as_float(r0); v[1] = __uint_as_float(r1); v[2] = __uint_as_float(r2); v[3] = __uint_as_float(r3);
+	v[4] = __uint_as_float(r4); v[5] = __uint_as_float(r5); v[6] = __uint_as_float(r6); v[7] = __uint_as_float(r7);
+}
+
 // Bulk global -> shared copy completing on `bar` (both addresses 16-byte
 // aligned, bytes a multiple of 16).
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)

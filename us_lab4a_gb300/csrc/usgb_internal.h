@@ -65,6 +65,10 @@ struct PrepParams {
 	// The rows of `rf` are device memory, 16-byte aligned, ns a multiple of 4:
 	// they may be fetched with bulk copies.
 	unsigned rfBulk;
+	// Tensor-memory columns of a single-frame analytic block (the real parts
+	// parked there during the FFTs), 0: two store passes instead. Set by the
+	// launch.
+	unsigned tmemCols;
 	unsigned* errWord;           // device status word of the bounded waits, or null
 };
 

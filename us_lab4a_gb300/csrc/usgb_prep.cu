@@ -822,6 +822,66 @@ __device__ void prep_analytic_tail(const PrepParams& p, unsigned a, float2* data
 	__syncthreads();
 }
 
+// Tensor-memory columns a thread needs for L samples, one per step of T
+// threads (ceil(L / T) rounded up to 8), and a block's allocation: the
+// T / 128 warps of an SM sub-partition side by side, as a power of two >= 32.
+__host__ __device__ inline unsigned tmem_thread_columns(unsigned L, unsigned T)
+{
+	return ((L + T - 1) / T + 7) & ~7u;
+}
+__host__ __device__ inline unsigned tmem_block_columns(unsigned L, unsigned T)
+{
+	const unsigned need = tmem_thread_columns(L, T) * (T / 128);
+	unsigned c = 32;
+	while (c < need) c <<= 1;
+	return c;
+}
+
+// prep_analytic_tail with the real parts parked in tensor memory: this
+// thread's samples x[n], n = threadIdx.x + T j, go to its TMEM lane (columns
+// tcol + j) before the FFTs overwrite the buffer, and one pass after the
+// inverse FFT stores whole complex samples (x[n] * scale, y[n] / M * scale):
+// the same values as the two store passes, in one. Those passes are bound by
+// the SM's store path (about 8 cycles a warp store instruction, whatever its
+// width), so the second pass's 4-byte stores cost as much as whole samples.
+template<int S, int T>
+__device__ void prep_analytic_tail_tmem(const PrepParams& p, unsigned a, float2* data, const float* xs,
+		const float2* twLo, const float2* twHi, const float2* stw, uint32_t tcol)
+{
+	const unsigned L = p.L;
+	const unsigned J8 = tmem_thread_columns(L, T);
+	for (unsigned c = 0; c < J8; c += 8) {
+		float v[8];
+#pragma unroll
+		for (int i = 0; i < 8; ++i) {
+			const unsigned n = threadIdx.x + T * (c + i);
+			v[i] = n < L ? xs[n] : 0.0f;
+		}
+		__syncwarp();
+		tmem_store8(tcol + c, v);
+	}
+	__syncthreads();
+	fft_run<false>(data, p, twLo, twHi, stw);
+	hilbert_pass(p, data);
+	__syncthreads();
+	fft_run<true>(data, p, twLo, twHi, stw);
+	using CT = typename Complex<S>::T;
+	CT* out = reinterpret_cast<CT*>(p.out) + static_cast<size_t>(a) * p.outStride;
+	const float invM = 1.0f / static_cast<float>(p.M);
+	const float sc = p.outScale;
+	for (unsigned c = 0; c < J8; c += 8) {
+		float v[8];
+		__syncwarp();
+		tmem_load8(tcol + c, v);
+#pragma unroll
+		for (int i = 0; i < 8; ++i) {
+			const unsigned n = threadIdx.x + T * (c + i);
+			if (n < L) out[n] = Complex<S>::pack(v[i] * sc, xs[n] * invM * sc);
+		}
+	}
+	__syncthreads();
+}
+
 // Analytic path, one A-scan `a` of the frame described by p. NT = 0 selects
 // the generic FIR loop. ENV: the envelope of the input itself instead
 // (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
@@ -998,7 +1058,9 @@ prep_stream_kernel(const __grid_constant__ PrepParams p)
 {
 	extern __shared__ __align__(16) float sm[];
 	__shared__ int sAbort;
+	__shared__ uint32_t sTmem;
 	constexpr bool PT = param_taps_fit<NT, U>() && (ANALYTIC || U <= 4);
+	const bool useTmem = ANALYTIC && p.tmemCols != 0;
 	constexpr unsigned K = (NT - 1) / 2;
 	const StreamLayout lay(p, ANALYTIC);
 	const unsigned ns = p.ns;
@@ -1027,7 +1089,16 @@ prep_stream_kernel(const __grid_constant__ PrepParams p)
 		mbar_init(&bar[1], 1);
 		fence_barrier_init();
 	}
+	__syncwarp();
+	if (useTmem && threadIdx.x < 32) tmem_alloc(&sTmem, p.tmemCols);
+	tmem_fence_before_sync();
 	__syncthreads();
+	tmem_fence_after_sync();
+	uint32_t tcol = 0;
+	if (useTmem) {
+		const unsigned w = threadIdx.x >> 5;
+		tcol = sTmem + (((w & 3u) * 32u) << 16) + (w >> 2) * tmem_thread_columns(p.L, T);
+	}
 
 	const bool bulk = p.rfBulk != 0;
 	const unsigned rowBytes = ns * static_cast<unsigned>(sizeof(float));
@@ -1062,7 +1133,7 @@ prep_stream_kernel(const __grid_constant__ PrepParams p)
 			for (unsigned i = threadIdx.x; i < ns; i += T) rfs[K + i] = row[i];
 		}
 		__syncthreads();
-		if (sAbort) return;   // the row never arrived; no copy is left in flight
+		if (sAbort) break;   // the row never arrived; no copy is left in flight
 
 		const float mean = dc_mean(rfs + K, dc, ns, sm + lay.red, static_cast<float>(p.L - p.deadZone));
 
@@ -1077,10 +1148,25 @@ prep_stream_kernel(const __grid_constant__ PrepParams p)
 		fir_dc_free_pass<S, NT, U, PT, ANALYTIC>(p, rfs, taps, mean, xs, outRow);
 		__syncthreads();
 		if constexpr (ANALYTIC) {
-			prep_analytic_tail<S>(p, a, reinterpret_cast<float2*>(sm + lay.data), xs,
-					reinterpret_cast<const float2*>(sm + lay.twLo), reinterpret_cast<const float2*>(sm + lay.twHi),
-					p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr);
+			float2* data = reinterpret_cast<float2*>(sm + lay.data);
+			const float2* twLo = reinterpret_cast<const float2*>(sm + lay.twLo);
+			const float2* twHi = reinterpret_cast<const float2*>(sm + lay.twHi);
+			const float2* stw = p.stw ? reinterpret_cast<const float2*>(sm + lay.stw) : nullptr;
+			if (useTmem) {
+				prep_analytic_tail_tmem<S, T>(p, a, data, xs, twLo, twHi, stw, tcol);
+			} else {
+				prep_analytic_tail<S>(p, a, data, xs, twLo, twHi, stw);
+			}
 		}
+	}
+	if (useTmem) {
+		// Every thread's loads completed inside tmem_load8; the block's
+		// columns go back before it exits.
+		tmem_fence_before_sync();
+		__syncthreads();
+		tmem_fence_after_sync();
+		__syncwarp();
+		if (threadIdx.x < 32) tmem_dealloc(sTmem, p.tmemCols);
 	}
 }
 
@@ -1095,7 +1181,16 @@ cudaError_t launch_stream_t(const PrepParams& p, bool analytic, size_t smem, cud
 	if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
 	if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
 	const unsigned blocks = std::min(p.numSignals, static_cast<unsigned>(sms) * static_cast<unsigned>(perSM > 0 ? perSM : 1));
-	kernel<<<blocks, T, smem, stream>>>(p);
+	// Tensor memory for the real parts when the blocks an SM can hold fit in
+	// its 512 columns together (an allocation never waits on this launch's
+	// own blocks).
+	PrepParams q = p;
+	q.tmemCols = 0;
+	if (analytic) {
+		const unsigned cols = tmem_block_columns(p.L, T);
+		if (cols <= 512u && static_cast<unsigned>(perSM > 0 ? perSM : 1) * cols <= 512u) q.tmemCols = cols;
+	}
+	kernel<<<blocks, T, smem, stream>>>(q);
 	return cudaGetLastError();
 }
 
