@@ -64,6 +64,44 @@ def test_batch_equals_frames_alone(cuda, use_graph, storage, variant, rows):
         e.close()
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_batch_equals_long_frames_alone(cuda, storage):
+    """A-scans of 4096 samples at 4x (16384 upsampled): alone, the
+    single-frame preparation runs one 512-thread block an SM and parks the
+    real parts in tensor memory (one store pass of whole samples); in the
+    batch, the batch kernel stores real and imaginary parts in two passes.
+    The images agree bit for bit."""
+    import torch
+    from dataclasses import replace
+    from us_lab4a_gb300 import StaEngine, workloads
+    from us_lab4a_gb300.batch import Batch, BatchItem
+    frames = workloads.mixed(num_frames=3, small=True, storage=storage)
+    for fr in frames:
+        fr.spec = replace(fr.spec, num_samples=4096)
+    cfg = (4, 16384, 2)
+    stream = torch.cuda.current_stream()
+    engines, items = [], []
+    with Batch(max_frames=4, max_elements=16) as batch:
+        batch.set_das_config(*cfg, variant=1)
+        for fr in frames:
+            eng = StaEngine(fr.spec)
+            eng.set_stream(stream)
+            eng.set_grid_device(torch.as_tensor(fr.grid_xyz, device=cuda))
+            engines.append(eng)
+            v = torch.full(fr.grid_xyz.shape[:2], -1.0, device=cuda)
+            items.append(BatchItem(eng, torch.as_tensor(fr.make_rf_numpy(), device=cuda), v, torch.empty_like(v)))
+        batch.run(items, stream, use_graph=False)
+        batch.synchronize()
+        for fr, it in zip(frames, items):
+            va, fa = _alone(fr, cuda, cfg)
+            vb, fb = it.value.cpu().numpy(), it.factor.cpu().numpy()
+            assert np.abs(va).max() > 0
+            assert np.array_equal(va, vb), np.abs(va - vb).max()
+            assert np.array_equal(fa, fb)
+    for e in engines:
+        e.close()
+
+
 def test_serving_results_same_alone_and_in_mix(cuda):
     import torch
     from us_lab4a_gb300 import workloads
