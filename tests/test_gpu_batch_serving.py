@@ -66,18 +66,21 @@ def test_batch_equals_frames_alone(cuda, use_graph, storage, variant, rows):
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 def test_batch_equals_long_frames_alone(cuda, storage):
-    """A-scans of 4096 samples at 4x (16384 upsampled): alone, the
-    single-frame preparation runs one 512-thread block an SM and parks the
-    real parts in tensor memory (one store pass of whole samples); in the
-    batch, the batch kernel stores real and imaginary parts in two passes.
-    The images agree bit for bit."""
+    """Two frames of A-scans of 4096 samples at 8x (32768 upsampled) and one
+    of at most 512 samples at 4x: alone, a long frame's preparation runs one
+    512-thread block an SM and parks the real parts in tensor memory (one
+    store pass of whole samples), the short frame's runs 128-thread blocks
+    with two store passes; in the batch the longest A-scan makes the blocks
+    512 threads, one an SM, and every frame's real parts are parked. The
+    images agree bit for bit."""
     import torch
     from dataclasses import replace
     from us_lab4a_gb300 import StaEngine, workloads
     from us_lab4a_gb300.batch import Batch, BatchItem
     frames = workloads.mixed(num_frames=3, small=True, storage=storage)
-    for fr in frames:
-        fr.spec = replace(fr.spec, num_samples=4096)
+    for fr in frames[:2]:
+        fr.spec = replace(fr.spec, num_samples=4096, upsampling=8)
+    assert frames[2].spec.num_samples <= 512
     cfg = (4, 16384, 2)
     stream = torch.cuda.current_stream()
     engines, items = [], []

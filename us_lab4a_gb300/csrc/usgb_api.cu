@@ -1043,6 +1043,10 @@ int usgb_batch_run(usgb_batch* b, const usgb_batch_item* items, uint32_t count, 
 				+ b->maxFrames * sizeof(usgb::BatchPrepFrame));
 		const size_t prepSmem = batch_prep_smem(items, count);
 		if (prepSmem > max_smem()) USGB_FAIL(USGB_ERR_UNSUPPORTED, "An A-scan of the batch is too long for on-chip preparation.");
+		unsigned maxL = 0;
+		for (uint32_t i = 0; i < count; ++i) maxL = std::max(maxL, items[i].ctx->L);
+		const unsigned tmemCols = usgb::prep_batch_tmem_columns(prepSmem, maxL, items[0].ctx->analytic);
+		for (uint32_t i = 0; i < count; ++i) prepF[i].prep.tmemCols = tmemCols;
 		const unsigned prepPerSM = std::max<unsigned>(1, static_cast<unsigned>((228u * 1024u) / (prepSmem + 1024u)));
 		const unsigned prepBlocks = b->numSMs * std::min(prepPerSM, 4u);
 		usgb::BatchDasConfig dc{};

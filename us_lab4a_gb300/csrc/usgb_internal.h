@@ -76,6 +76,9 @@ size_t prep_smem_bytes(const PrepParams& p, bool analytic);
 // Threads per preparation block for `smem` bytes of shared memory a block:
 // 128 when four blocks fit on an SM, 256 when two fit, else 512.
 int prep_threads(size_t smem);
+// Tensor-memory columns of a batch preparation launch of `smem` bytes a block
+// whose longest A-scan has maxL samples (the 512-thread form only), else 0.
+unsigned prep_batch_tmem_columns(size_t smem, unsigned maxL, bool analytic);
 // Envelope (|analytic signal|, no DC removal) of p.numSignals real sequences of
 // p.ns = p.L samples (U = 1, one FIR tap of 1), float output, p.outStride apart.
 cudaError_t launch_envelope(const PrepParams& p, cudaStream_t stream);

@@ -886,9 +886,12 @@ __device__ void prep_analytic_tail_tmem(const PrepParams& p, unsigned a, float2*
 // the generic FIR loop. ENV: the envelope of the input itself instead
 // (HilbertEnvelope::calculate: no DC removal, |analytic signal| as floats;
 // used with U = 1 on image columns). PT: FIR taps from p.paramTaps (p a
-// launch parameter) instead of shared memory.
-template<int S, int NT, int U, bool ENV = false, bool PT = false>
-__device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm, bool tables = true)
+// launch parameter) instead of shared memory. PARK_T > 0 (a block of PARK_T
+// threads holding tensor memory, `tlane` = its base address with this warp's
+// lane field): with p.tmemCols set, the real parts wait in tensor memory
+// (prep_analytic_tail_tmem).
+template<int S, int NT, int U, bool ENV = false, bool PT = false, int PARK_T = 0>
+__device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm, bool tables = true, uint32_t tlane = 0)
 {
 	const PrepLayout lay(p, true);
 	load_inputs(p, lay, sm, p.rf + static_cast<size_t>(a) * p.ns, true, tables);
@@ -912,6 +915,13 @@ __device__ void prep_analytic_body(const PrepParams& p, unsigned a, float* sm, b
 			void* outRow = reinterpret_cast<typename Complex<S>::T*>(p.out) + static_cast<size_t>(a) * p.outStride;
 			fir_dc_free_pass<S, NT, U, PT, true>(p, rfs, taps, m, xs, outRow);
 			__syncthreads();
+			if constexpr (PARK_T > 0) {
+				if (p.tmemCols) {
+					const uint32_t tcol = tlane + (threadIdx.x >> 7) * tmem_thread_columns(L, PARK_T);
+					prep_analytic_tail_tmem<S, PARK_T>(p, a, data, xs, twLo, twHi, stw, tcol);
+					return;
+				}
+			}
 			prep_analytic_tail<S>(p, a, data, xs, twLo, twHi, stw);
 			return;
 		}
@@ -1226,10 +1236,27 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 {
 	extern __shared__ __align__(16) float sm[];
 	__shared__ PrepParams sp;
+	__shared__ uint32_t sTmem;
 	static_assert(sizeof(PrepParams) % 8 == 0 && alignof(PrepParams) == 8, "PrepParams is copied as 8-byte words");
 	const unsigned count = hdr->count;
 	const unsigned total = hdr->totalSignals;
 	unsigned f = 0, loaded = ~0u;
+	// The 512-thread form (one block an SM) parks the real parts in tensor
+	// memory when the launch asks for it (every frame's tmemCols: the columns
+	// of the batch's longest A-scan); the forms that share an SM carry no
+	// tensor-memory code (measured slower with it).
+	constexpr bool kTmem = ANALYTIC && T == 512;
+	constexpr int kParkT = kTmem ? T : 0;
+	unsigned tmemCols = 0;
+	uint32_t tlane = 0;
+	if constexpr (kTmem) {
+		tmemCols = count ? frames[0].prep.tmemCols : 0u;
+		if (tmemCols && threadIdx.x < 32) tmem_alloc(&sTmem, tmemCols);
+		tmem_fence_before_sync();
+		__syncthreads();
+		tmem_fence_after_sync();
+		if (tmemCols) tlane = sTmem + ((((threadIdx.x >> 5) & 3u) * 32u) << 16);
+	}
 	for (unsigned g = blockIdx.x; g < total; g += gridDim.x) {
 		while (f + 1 < count && frames[f + 1].signalBegin <= g) ++f;
 		__syncthreads();  // the previous A-scan is done with sp
@@ -1248,14 +1275,23 @@ prep_batch_kernel(const BatchPrepFrame* __restrict__ frames, const BatchHeader* 
 		const int shape = fir_shape(sp.tapsPerPhase, sp.U);
 		if (ANALYTIC) {
 			switch (shape) {
-			case 1: prep_analytic_body<S, 27, 8>(sp, a, sm, tables); break;
-			case 2: prep_analytic_body<S, 27, 4>(sp, a, sm, tables); break;
+			case 1: prep_analytic_body<S, 27, 8, false, false, kParkT>(sp, a, sm, tables, tlane); break;
+			case 2: prep_analytic_body<S, 27, 4, false, false, kParkT>(sp, a, sm, tables, tlane); break;
 			case 4: prep_analytic_body<S, 1, 1>(sp, a, sm, tables); break;
 			default: prep_analytic_body<S, 0, 1>(sp, a, sm, tables); break;
 			}
 		} else {
 			if (shape == 3) prep_real_body<S, 21, 4>(sp, a, sm, tables);
 			else prep_real_body<S, 0, 1>(sp, a, sm, tables);
+		}
+	}
+	if constexpr (kTmem) {
+		if (tmemCols) {
+			tmem_fence_before_sync();
+			__syncthreads();
+			tmem_fence_after_sync();
+			__syncwarp();
+			if (threadIdx.x < 32) tmem_dealloc(sTmem, tmemCols);
 		}
 	}
 }
@@ -1343,6 +1379,13 @@ cudaError_t launch_prep_batch(const BatchPrepFrame* frames, const BatchHeader* h
 	case STORE_BF16: return launch_batch<STORE_BF16, false>(frames, hdr, smem, blocks, stream);
 	default: return launch_batch<STORE_F32, false>(frames, hdr, smem, blocks, stream);
 	}
+}
+
+unsigned prep_batch_tmem_columns(size_t smem, unsigned maxL, bool analytic)
+{
+	if (!analytic || prep_threads(smem) != 512) return 0;
+	const unsigned cols = tmem_block_columns(maxL, 512);
+	return cols <= 512u ? cols : 0u;
 }
 
 int prep_threads(size_t smem)
