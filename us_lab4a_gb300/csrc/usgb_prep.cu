@@ -25,9 +25,14 @@
 //   pass over digit-reversed pairs (k, M-k), and the inverse is an in-place
 //   decimation-in-time FFT that consumes the digit-reversed order and returns
 //   the imaginary part y[n] in natural order. The real part of the analytic
-//   signal is the DC-free input itself: the DC-removal pass writes it to the
-//   output (before the FFT overwrites it in shared memory), the last pass the
-//   imaginary part.
+//   signal is the DC-free input itself. Blocks of 512 threads (one an SM)
+//   park it in tensor memory (tcgen05.st, each thread in its own lane) before
+//   the FFT overwrites it in shared memory and store whole complex samples in
+//   one last pass (tcgen05.ld); smaller blocks store the real parts before
+//   the FFT and the imaginary parts in the last pass.
+// * Butterflies use packed FP32x2 arithmetic for complex sums and for the
+//   i-products of the 3-, 4- and 5-point DFTs (each component rounded as the
+//   scalar form rounds it).
 // * Each butterfly reads one twiddle W_Ms^j and forms its powers in
 //   registers: the first stage from a two-level table (W^m = hi[m / 128] *
 //   lo[m % 128]), later stages from per-stage tables indexed by j, so that
