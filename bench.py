@@ -504,7 +504,7 @@ def run_gpu(args):
             "clocks": clk, "e2e": e2e, "gpu_launches": 2 * args.steps, "cpu_baseline": cpu,
             "configs": configs, "mixed": mixed, "single": single, "two_medium": two_medium,
         }
-        line["north_star"] = _north_star(line)   # last key: the summary the record's tail keeps
+        line["summary"] = _summary(line)   # last key: the summary the record's tail keeps
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
@@ -548,7 +548,7 @@ def staged_bytes_model(frame, tile_cols: int, tile_rows: int, esize: int) -> flo
     return total
 
 
-def _north_star(line: dict) -> dict:
+def _summary(line: dict) -> dict:
     """Compact summary of the headline and the mixed-precision / batching /
     serving comparison (target: the FP16 batched serving form at >= 3x the
     frames/s of the plain FP32 GPU form at <= -60 dB against the FP64 oracle)."""
